@@ -1,0 +1,184 @@
+/* staqdic.h — C ABI of the GB300 (sm_103a) STAQ-DIC augmented-Lagrangian hot path.
+ *
+ * Each entry point replaces one routine of the reference (paths relative to the
+ * STAQ-DIC repository) and keeps its argument meaning, so a MEX gateway can call
+ * it with the arrays MATLAB already holds:
+ *
+ *   stdic_interp_bicubic   ba_interp2.cpp:318-335 (mexFunction) / :184-234
+ *   stdic_img_gradient     func/funImgGradient.m:1-88
+ *   stdic_integer_search   func/funIntegerSearch.m:3-203 + func/findpeak.m:1-68
+ *   stdic_icgn_subsets     func_quadtree/funICGNQuadtree.m:1-451 (N nodes at once)
+ *   stdic_icgn_local       func_quadtree/LocalICGNQuadtree.m:1-177
+ *   stdic_subpb1_subsets   func/funICGN_Subpb1.m:1-474 (N nodes at once)
+ *   stdic_subpb1           func_quadtree/Subpb1Quadtree.m:1-191
+ *   stdic_subpb2           func_quadtree/Subpb2Quadtree.m:1-413
+ *   stdic_icgn_adjoint     no counterpart in the reference (gradient of the
+ *                          summed ZNSSD cost of the IC-GN subsets)
+ *
+ * Conventions (MATLAB's):
+ *   - arrays are column-major, first index contiguous; an image is W x H with
+ *     x = dim 1 (the reference stores images transposed, Img(x, y));
+ *   - node coordinates are 1-based pixel positions (N x 2, x column first);
+ *   - U is interleaved [u1 v1 u2 v2 ...]; F is [F11 F21 F12 F22] per node;
+ *   - packed Hessians are N x 21 (lower triangle, column by column);
+ *   - elementsFEM is E x 8 int32, 1-based, 0 = no hanging node.
+ *
+ * Memory: every pointer may be host memory (MATLAB's arrays) or device memory
+ * of the context's GPU.  Host buffers are staged through a context-owned device
+ * workspace and the call returns after the results are copied back.  When every
+ * pointer of a call is device memory the call is asynchronous on the context's
+ * stream (per-node codes are ready after stream synchronisation).
+ *
+ * Errors: 0 on success, a negative STDIC_E_* code otherwise (stdic_last_error
+ * gives text).  Per-node failures never raise: they are reported through the
+ * ConvItPerEle codes exactly as the reference writes them (1..100 converged at
+ * that iteration, 101 not converged / NaN / warp out of image, 102 >= 40 % of
+ * the subset masked, 103 empty subset, -1 MATLAB run-time error in
+ * funICGNQuadtree; 0 with NaN U for a run-time error inside Subpb1Quadtree).
+ *
+ * Threading: a context owns one CUDA stream and a workspace; calls on one
+ * context must not overlap.  Distinct contexts are independent.
+ */
+#ifndef STAQDIC_H
+#define STAQDIC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  STDIC_OK = 0,
+  STDIC_E_ARG = -1,         /* invalid argument (sizes, odd subset size, ...) */
+  STDIC_E_CUDA = -2,        /* CUDA runtime error */
+  STDIC_E_NOMEM = -3,       /* device allocation failed */
+  STDIC_E_UNSUPPORTED = -4, /* option the reference path cannot take */
+  STDIC_E_TIMEOUT = -5,     /* a bounded device wait gave up */
+  STDIC_E_NOTCONV = -6      /* iterative solver did not reach its tolerance */
+};
+
+enum { STDIC_F64 = 0, STDIC_F32 = 1 };
+
+/* precision/form of the IC-GN solvers */
+enum {
+  STDIC_PLAIN_F64 = 0,   /* one subset per CTA, FP64, reproduces the reference */
+  STDIC_BATCHED_F32 = 1  /* persistent kernel over a size-sorted queue, FP32
+                            interpolation/residual/Hessian sums with FP64
+                            cross-thread reduction and FP64 solves */
+};
+
+typedef struct stdic_ctx stdic_ctx;
+
+/* One reference/deformed frame pair as funICGNQuadtree sees it:
+ * ImgRef (f), ImgDef (g), Df.ImgRefMask, Df.DfDx, Df.DfDy ((W-6) x (H-6)).
+ * dtype applies to f, g, dfdx and dfdy.  STDIC_PLAIN_F64 needs STDIC_F64 data;
+ * STDIC_BATCHED_F32 takes either (FP64 data is converted once per call). */
+typedef struct {
+  const void* f;
+  const void* g;
+  const uint8_t* mask;
+  const void* dfdx;
+  const void* dfdy;
+  int W, H;
+  int dtype;
+} stdic_frame;
+
+/* Context on CUDA device `device`. */
+int stdic_ctx_create(stdic_ctx** ctx, int device);
+int stdic_ctx_destroy(stdic_ctx* ctx);
+/* Use an external cudaStream_t (NULL restores the context's own stream). */
+int stdic_ctx_set_stream(stdic_ctx* ctx, void* cuda_stream);
+const char* stdic_last_error(const stdic_ctx* ctx);
+/* Number of kernels this context launched since creation (instrumentation). */
+long long stdic_kernel_launches(const stdic_ctx* ctx);
+
+/* Z = ba_interp2(F, X, Y, 'cubic').  F is M x N x P (P layers), X/Y hold n
+ * points (X indexes dim 2, Y dim 1, 1-based); out is n x P.  dtype STDIC_F64 or
+ * STDIC_F32 for all of F, X, Y, out.  Bit-identical to the reference's
+ * compiled ba_interp2.cpp on x86-64 (no fused multiply-add). */
+int stdic_interp_bicubic(stdic_ctx* ctx, const void* F, int64_t M, int64_t N, int64_t P,
+                         const void* X, const void* Y, int64_t n, void* out, int dtype);
+
+/* Df = funImgGradient(ImgRef, ImgDef, ImgRefMask): dfdx, dfdy are (W-6) x (H-6).
+ * dtype is the element type of img, dfdx and dfdy. */
+int stdic_img_gradient(stdic_ctx* ctx, const void* img, const uint8_t* mask, int W, int H,
+                       void* dfdx, void* dfdy, int dtype);
+
+/* Grid of funIntegerSearch after its border shrink (funIntegerSearch.m:14-25):
+ * returns nx, ny of the ny x nx outputs. */
+int stdic_integer_search_grid(int W, int H, const int S[2], const double gridx[2],
+                              const double gridy[2], const int winsize[2],
+                              const int winstepsize[2], int* nx, int* ny);
+
+/* [x,y,u,v,cc] = funIntegerSearch(f, g, S, gridx, gridy, winsize, winstepsize, 0, ..).
+ * f, g are W x H double.  Outputs are ny x nx (row = y index) column-major;
+ * cc is cc.max.  peak_rc (optional, 2 x ny x nx planes) receives the 1-based
+ * integer argmax (row, col) of each cropped (2S+3)^2 correlation map; 0 where
+ * normxcorr2 throws (constant template), where u, v, cc are NaN. */
+int stdic_integer_search(stdic_ctx* ctx, const double* f, const double* g, int W, int H,
+                         const int S[2], const double gridx[2], const double gridy[2],
+                         const int winsize[2], const int winstepsize[2], double* x, double* y,
+                         double* u, double* v, double* cc, int32_t* peak_rc);
+
+/* LocalICGNQuadtree(U0, coordinatesFEM, Df, ImgRef, ImgDef, DICpara, 'GaussNewton', tol)
+ * without its NaN-fill tail (out of this path): U (2N) and F (4N) carry NaN at
+ * the bad subsets the reference marks.  winsize is DICpara.winsize; ws_list
+ * (optional, N int32) gives a subset size per node instead.  Hpk is HtempPar
+ * (N x 21), conv is ConvItPerEle, mark_hole (optional, N) flags the nodes of
+ * markCoordHoleStrain, badnum (optional) receives LocalICGNBadPtNum.
+ * Only 'GaussNewton' exists: the reference's 'LevenbergMarquardt' branch calls
+ * ImgDef.eval on a spline object and cannot run on image arrays. */
+int stdic_icgn_local(stdic_ctx* ctx, const stdic_frame* fr, const double* U0,
+                     const double* coords, int N, int winsize, const int32_t* ws_list, double tol,
+                     double* U, double* F, double* Hpk, int32_t* conv, uint8_t* mark_hole,
+                     int* badnum, int precision);
+
+/* [U,F,stepwithinwhile,HGlobal] = funICGNQuadtree(U0, x0, y0, Df, ImgRef, ImgDef,
+ * winsize, tol, 'GaussNewton') for N nodes at once (x0, y0 = round(coords)):
+ * the per-node loop of LocalICGNQuadtree without its bad-subset filter.  A
+ * MATLAB run-time error of the routine gives code -1 and NaN outputs.
+ * Replaces func_quadtree/funICGNQuadtree.m:1-451. */
+int stdic_icgn_subsets(stdic_ctx* ctx, const stdic_frame* fr, const double* U0,
+                       const double* coords, int N, int winsize, const int32_t* ws_list,
+                       double tol, double* U, double* F, double* Hpk, int32_t* conv,
+                       int precision);
+
+/* [U,~,stepwithinwhile] = funICGN_Subpb1(x0, y0, Df, ImgRef, ImgDef, winsize_x,
+ * winsize_y, H, beta, mu, udual, vdual, UOld, FOld, tol, 'GaussNewton') for N
+ * nodes (func/funICGN_Subpb1.m:1-474): the per-node loop of Subpb1Quadtree
+ * without its bad-subset filter; a run-time error gives code 0 and NaN U. */
+int stdic_subpb1_subsets(stdic_ctx* ctx, const stdic_frame* fr, const double* UOld,
+                         const double* FOld, const double* vdual, const double* coords, int N,
+                         const int32_t* winsize_list, double mu, double tol, double* U,
+                         int32_t* conv, int precision);
+
+/* Subpb1Quadtree(UOld, FOld, udual, vdual, coordinatesFEM, Df, ImgRef, ImgDef,
+ * mu, beta, HPar, ALSolveStep, DICpara, 'GaussNewton', tol) for ALSolveStep > 1
+ * without its NaN-fill tail.  winsize_list is DICpara.winsize_List (N x 2).
+ * udual, beta and HPar do not change the result in the reference
+ * (funICGN_Subpb1.m overwrites H and never reads udual or beta); they are
+ * accepted for signature parity and may be NULL/0. */
+int stdic_subpb1(stdic_ctx* ctx, const stdic_frame* fr, const double* UOld, const double* FOld,
+                 const double* udual, const double* vdual, const double* coords, int N,
+                 const int32_t* winsize_list, double mu, double beta, double tol, double* U,
+                 int32_t* conv, int* badnum, int precision);
+
+/* Uhat = Subpb2Quadtree(DICmesh, GaussPtOrder, beta, mu, U, F, udual, vdual,
+ * alpha, winstepsize, ~).  The duals enter the reference multiplied by zero
+ * (Subpb2Quadtree.m:42-44), so they are not taken.  neumann is nn x 4 (node1,
+ * node2, nx, ny; column-major, may be NULL).  The system is solved by
+ * Jacobi-preconditioned CG in FP64 to relative residual tol (<= 0 -> 1e-10),
+ * at most maxit iterations (<= 0 -> 10000); iters receives the count. */
+int stdic_subpb2(stdic_ctx* ctx, const double* coords, int N, const int32_t* elems, int E,
+                 const int32_t* dirichlet, int nd, const double* neumann, int nn,
+                 int gauss_order, double beta, double mu, const double* U, const double* F,
+                 double alpha, double winstepsize, double tol, int maxit, double* Uhat,
+                 int* iters);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STAQDIC_H */

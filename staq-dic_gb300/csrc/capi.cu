@@ -1,0 +1,642 @@
+// C ABI of libstaqdic (declared in include/staqdic.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/staqdic.h"
+#include "kernels.h"
+
+namespace stdic {
+int batched_blocks_per_sm(int tw, bool two, int threads, int npx_max);
+}
+
+struct stdic_ctx {
+  int device = 0;
+  int nsm = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  void* ws = nullptr;
+  size_t ws_size = 0;
+  int* scal = nullptr;  // device scalars: [0] queue head, [1] badnum, [2] iters, [3] status
+  double* scald = nullptr;  // device double scalars: [0] residual
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  long long launches = 0;
+  // autotuner cache: (N bucket, npx_max, two_dof, frames) -> (warps per subset, threads)
+  std::map<std::tuple<int, int, int, int>, std::pair<int, int>> tune;
+  int tuning = 1;
+};
+
+namespace {
+
+int fail(stdic_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(stdic_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, STDIC_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Plans device placement for one call: device pointers pass through, host
+// buffers and scratch get regions of the context workspace.
+struct Plan {
+  struct Item {
+    const void* host;
+    void* host_out;
+    size_t bytes;
+    size_t off;
+    bool dev;
+    int dir;  // 0 in, 1 out, 2 scratch
+    void** slot;
+  };
+  std::vector<Item> items;
+  size_t total = 0;
+  bool any_host = false;
+
+  template <class T>
+  void in(const T* p, size_t count, T** slot) {
+    Item it{p, nullptr, sizeof(T) * count, 0, is_device_ptr(p), 0, (void**)slot};
+    if (!p) { *slot = nullptr; return; }
+    if (!it.dev) { it.off = total; total += al(it.bytes); any_host = true; }
+    items.push_back(it);
+  }
+  template <class T>
+  void out(T* p, size_t count, T** slot) {
+    Item it{nullptr, p, sizeof(T) * count, 0, is_device_ptr(p), 1, (void**)slot};
+    if (!p) { *slot = nullptr; return; }
+    if (!it.dev) { it.off = total; total += al(it.bytes); any_host = true; }
+    items.push_back(it);
+  }
+  template <class T>
+  void scratch(size_t count, T** slot) {
+    Item it{nullptr, nullptr, sizeof(T) * count, total, false, 2, (void**)slot};
+    total += al(it.bytes);
+    items.push_back(it);
+  }
+  // out-or-scratch: user buffer when given, else workspace
+  template <class T>
+  void out_opt(T* p, size_t count, T** slot) {
+    if (p) out(p, count, slot);
+    else scratch(count, slot);
+  }
+
+  int commit(stdic_ctx* c) {
+    if (total > c->ws_size) {
+      if (c->ws) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->ws);
+        c->ws = nullptr;
+        c->ws_size = 0;
+      }
+      const size_t want = std::max(total, c->ws_size + c->ws_size / 2);
+      cudaError_t e = cudaMalloc(&c->ws, want);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, STDIC_E_NOMEM, "workspace allocation failed");
+      }
+      c->ws_size = want;
+    }
+    for (auto& it : items) {
+      if (it.dir == 0 && it.dev) *it.slot = const_cast<void*>(it.host);
+      else if (it.dir == 1 && it.dev) *it.slot = it.host_out;
+      else *it.slot = (char*)c->ws + it.off;
+      if (it.dir == 0 && !it.dev) {
+        cudaError_t e = cudaMemcpyAsync(*it.slot, it.host, it.bytes, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "host-to-device copy");
+      }
+    }
+    return STDIC_OK;
+  }
+
+  int finish(stdic_ctx* c) {
+    for (auto& it : items) {
+      if (it.dir == 1 && !it.dev) {
+        cudaError_t e = cudaMemcpyAsync(it.host_out, *it.slot, it.bytes, cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "device-to-host copy");
+      }
+    }
+    if (any_host) {
+      cudaError_t e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "stream synchronise");
+    }
+    return STDIC_OK;
+  }
+};
+
+int check_launch(stdic_ctx* c, cudaError_t e, const char* what) {
+  if (e != cudaSuccess) return cuda_fail(c, e, what);
+  ++c->launches;
+  return STDIC_OK;
+}
+
+// read a device int into the host (synchronises the stream)
+int read_scalar(stdic_ctx* c, const int* dev, int* host) {
+  cudaError_t e = cudaMemcpyAsync(host, dev, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return e == cudaSuccess ? STDIC_OK : cuda_fail(c, e, "scalar read-back");
+}
+
+int deliver_int(stdic_ctx* c, const int* dev, int* dst) {
+  if (!dst) return STDIC_OK;
+  if (is_device_ptr(dst)) {
+    cudaError_t e = cudaMemcpyAsync(dst, dev, sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
+    return e == cudaSuccess ? STDIC_OK : cuda_fail(c, e, "scalar copy");
+  }
+  return read_scalar(c, dev, dst);
+}
+
+}  // namespace
+
+extern "C" {
+
+int stdic_ctx_create(stdic_ctx** out, int device) {
+  if (!out) return STDIC_E_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    cudaGetLastError();
+    return STDIC_E_CUDA;
+  }
+  stdic_ctx* c = new stdic_ctx();
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->scal, 64 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&c->scald, 8 * sizeof(double));
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return STDIC_E_CUDA;
+  }
+  c->stream = c->own;
+  *out = c;
+  return STDIC_OK;
+}
+
+int stdic_ctx_destroy(stdic_ctx* c) {
+  if (!c) return STDIC_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->ws) cudaFree(c->ws);
+  if (c->scal) cudaFree(c->scal);
+  if (c->scald) cudaFree(c->scald);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+  return STDIC_OK;
+}
+
+int stdic_ctx_set_stream(stdic_ctx* c, void* s) {
+  if (!c) return STDIC_E_ARG;
+  c->stream = s ? (cudaStream_t)s : c->own;
+  return STDIC_OK;
+}
+
+const char* stdic_last_error(const stdic_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+long long stdic_kernel_launches(const stdic_ctx* c) { return c ? c->launches : 0; }
+
+// ---------------------------------------------------------------------------
+int stdic_interp_bicubic(stdic_ctx* c, const void* F, int64_t M, int64_t N, int64_t P, const void* X,
+                         const void* Y, int64_t n, void* out, int dtype) {
+  if (!c) return STDIC_E_ARG;
+  if (M <= 0 || N <= 0 || P <= 0 || n < 0 || (dtype != STDIC_F64 && dtype != STDIC_F32) ||
+      (n > 0 && (!F || !X || !Y || !out)))
+    return fail(c, STDIC_E_ARG, "ba_interp2: bad sizes or pointers");
+  cudaSetDevice(c->device);
+  const size_t es = dtype == STDIC_F64 ? 8 : 4;
+  Plan pl;
+  const unsigned char *dF, *dX, *dY;
+  unsigned char* dO;
+  pl.in((const unsigned char*)F, es * M * N * P, (unsigned char**)&dF);
+  pl.in((const unsigned char*)X, es * n, (unsigned char**)&dX);
+  pl.in((const unsigned char*)Y, es * n, (unsigned char**)&dY);
+  pl.out((unsigned char*)out, es * n * P, &dO);
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  if (n > 0) {
+    rc = check_launch(c, stdic::launch_interp(dF, M, N, P, dX, dY, n, dO, dtype, c->stream), "ba_interp2");
+    if (rc) return rc;
+  }
+  return pl.finish(c);
+}
+
+int stdic_img_gradient(stdic_ctx* c, const void* img, const uint8_t* mask, int W, int H, void* dfdx,
+                       void* dfdy, int dtype) {
+  if (!c) return STDIC_E_ARG;
+  if (W < 7 || H < 7 || !img || !mask || !dfdx || !dfdy || (dtype != STDIC_F64 && dtype != STDIC_F32))
+    return fail(c, STDIC_E_ARG, "funImgGradient: image must be at least 7 x 7");
+  cudaSetDevice(c->device);
+  const size_t es = dtype == STDIC_F64 ? 8 : 4;
+  Plan pl;
+  const unsigned char* di;
+  const uint8_t* dm;
+  unsigned char *dx, *dy;
+  pl.in((const unsigned char*)img, es * W * H, (unsigned char**)&di);
+  pl.in(mask, (size_t)W * H, (uint8_t**)&dm);
+  pl.out((unsigned char*)dfdx, es * (W - 6) * (H - 6), &dx);
+  pl.out((unsigned char*)dfdy, es * (W - 6) * (H - 6), &dy);
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  rc = check_launch(c, stdic::launch_gradient(di, dm, W, H, dx, dy, dtype, c->stream), "funImgGradient");
+  if (rc) return rc;
+  return pl.finish(c);
+}
+
+// ---------------------------------------------------------------------------
+static void grid_shrink(int W, int H, const int S[2], const double gridx[2], const double gridy[2],
+                        const int ws[2], const int st[2], double gx[2], double gy[2], int* nx,
+                        int* ny) {
+  double gx0 = gridx[0], gx1 = gridx[1], gy0 = gridy[0], gy1 = gridy[1];
+  while (gx0 - S[0] - 0.5 * ws[0] < 1) gx0 += 1;
+  while (gy0 - S[1] - 0.5 * ws[1] < 1) gy0 += 1;
+  while (gx1 + 1.5 * ws[0] + S[0] > (double)W) gx1 -= 1;
+  while (gy1 + 1.5 * ws[1] + S[1] > (double)H) gy1 -= 1;
+  gx[0] = gx0; gx[1] = gx1; gy[0] = gy0; gy[1] = gy1;
+  *nx = (gx1 - st[0] >= gx0) ? (int)std::floor((gx1 - st[0] - gx0) / st[0]) + 1 : 0;
+  *ny = (gy1 - st[1] >= gy0) ? (int)std::floor((gy1 - st[1] - gy0) / st[1]) + 1 : 0;
+}
+
+int stdic_integer_search_grid(int W, int H, const int S[2], const double gridx[2],
+                              const double gridy[2], const int winsize[2], const int winstepsize[2],
+                              int* nx, int* ny) {
+  if (!S || !gridx || !gridy || !winsize || !winstepsize || !nx || !ny || winstepsize[0] <= 0 ||
+      winstepsize[1] <= 0 || S[0] < 0 || S[1] < 0 || winsize[0] <= 0 || winsize[1] <= 0)
+    return STDIC_E_ARG;
+  double gx[2], gy[2];
+  grid_shrink(W, H, S, gridx, gridy, winsize, winstepsize, gx, gy, nx, ny);
+  return STDIC_OK;
+}
+
+int stdic_integer_search(stdic_ctx* c, const double* f, const double* g, int W, int H, const int S[2],
+                         const double gridx[2], const double gridy[2], const int winsize[2],
+                         const int winstepsize[2], double* x, double* y, double* u, double* v,
+                         double* cc, int32_t* peak_rc) {
+  if (!c) return STDIC_E_ARG;
+  int nx, ny;
+  if (stdic_integer_search_grid(W, H, S, gridx, gridy, winsize, winstepsize, &nx, &ny) ||
+      !f || !g || !x || !y || !u || !v || !cc)
+    return fail(c, STDIC_E_ARG, "funIntegerSearch: bad arguments");
+  double gx[2], gy[2];
+  grid_shrink(W, H, S, gridx, gridy, winsize, winstepsize, gx, gy, &nx, &ny);
+  cudaSetDevice(c->device);
+  const size_t npt = (size_t)nx * ny;
+  Plan pl;
+  const double *df, *dg;
+  double *dx, *dy, *du, *dv, *dc;
+  int32_t* dp;
+  pl.in(f, (size_t)W * H, (double**)&df);
+  pl.in(g, (size_t)W * H, (double**)&dg);
+  pl.out(x, npt, &dx); pl.out(y, npt, &dy); pl.out(u, npt, &du); pl.out(v, npt, &dv);
+  pl.out(cc, npt, &dc);
+  pl.out(peak_rc, 2 * npt, &dp);
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  if (npt > 0) {
+    rc = check_launch(c, stdic::launch_intsearch(df, dg, W, H, S[0], S[1], gx[0], gy[0], nx, ny, winsize[0],
+                                                 winsize[1], winstepsize[0], winstepsize[1], dx, dy, du,
+                                                 dv, dc, dp, c->stream),
+                      "funIntegerSearch");
+    if (rc) return rc;
+  }
+  return pl.finish(c);
+}
+
+// ---------------------------------------------------------------------------
+// IC-GN drivers
+// ---------------------------------------------------------------------------
+namespace {
+
+struct FrameDev {
+  const void *f, *g, *dfdx, *dfdy;
+  const uint8_t* mask;
+  const float *f32, *g32, *dfdx32, *dfdy32;
+};
+
+int stage_frame(stdic_ctx* c, Plan& pl, const stdic_frame* fr, FrameDev* d, bool want_f32,
+                int frames) {
+  const size_t es = fr->dtype == STDIC_F64 ? 8 : 4;
+  const size_t np = (size_t)fr->W * fr->H, ng = (size_t)(fr->W - 6) * (fr->H - 6);
+  pl.in((const unsigned char*)fr->f, es * np, (unsigned char**)&d->f);
+  pl.in((const unsigned char*)fr->g, es * np * frames, (unsigned char**)&d->g);
+  pl.in((const unsigned char*)fr->dfdx, es * ng, (unsigned char**)&d->dfdx);
+  pl.in((const unsigned char*)fr->dfdy, es * ng, (unsigned char**)&d->dfdy);
+  pl.in(fr->mask, np, (uint8_t**)&d->mask);
+  d->f32 = d->g32 = d->dfdx32 = d->dfdy32 = nullptr;
+  if (want_f32 && fr->dtype == STDIC_F64) {
+    pl.scratch(np, (float**)&d->f32);
+    pl.scratch(np * frames, (float**)&d->g32);
+    pl.scratch(ng, (float**)&d->dfdx32);
+    pl.scratch(ng, (float**)&d->dfdy32);
+  }
+  (void)c;
+  return STDIC_OK;
+}
+
+int convert_frame(stdic_ctx* c, const stdic_frame* fr, FrameDev* d, int frames) {
+  if (fr->dtype == STDIC_F32) {
+    d->f32 = (const float*)d->f; d->g32 = (const float*)d->g;
+    d->dfdx32 = (const float*)d->dfdx; d->dfdy32 = (const float*)d->dfdy;
+    return STDIC_OK;
+  }
+  const long long np = (long long)fr->W * fr->H, ng = (long long)(fr->W - 6) * (fr->H - 6);
+  int rc = check_launch(c, stdic::launch_to_f32((const double*)d->f, (float*)d->f32, np, c->stream), "to_f32");
+  if (!rc) rc = check_launch(c, stdic::launch_to_f32((const double*)d->g, (float*)d->g32, np * frames, c->stream), "to_f32");
+  if (!rc) rc = check_launch(c, stdic::launch_to_f32((const double*)d->dfdx, (float*)d->dfdx32, ng, c->stream), "to_f32");
+  if (!rc) rc = check_launch(c, stdic::launch_to_f32((const double*)d->dfdy, (float*)d->dfdy32, ng, c->stream), "to_f32");
+  return rc;
+}
+
+bool frame_ok(const stdic_frame* fr) {
+  return fr && fr->f && fr->g && fr->mask && fr->dfdx && fr->dfdy && fr->W >= 7 && fr->H >= 7 &&
+         (fr->dtype == STDIC_F64 || fr->dtype == STDIC_F32);
+}
+
+// Run the persistent batched kernel with the autotuned (warps per subset,
+// threads per CTA).  On a new problem class every candidate is timed once on
+// the real data (outputs are idempotent) and the fastest is cached.
+int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot) {
+  const bool two = b.two_dof != 0;
+  auto launch = [&](int tw, int threads) -> int {
+    const int per_sm = stdic::batched_blocks_per_sm(tw, two, threads, b.a.npx_max);
+    if (per_sm <= 0) return STDIC_E_UNSUPPORTED;
+    const int teams_per_block = threads / (32 * tw);
+    int blocks = c->nsm * per_sm;
+    blocks = std::max(1, std::min(blocks, (Ntot + teams_per_block - 1) / teams_per_block));
+    cudaError_t e = cudaMemsetAsync(b.queue_head, 0, sizeof(int), c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "queue reset");
+    b.warps_per_subset = tw;
+    return check_launch(c, stdic::launch_icgn_batched(b, blocks, threads, c->stream), "IC-GN batched");
+  };
+  const int nb = Ntot <= 0 ? 0 : (int)std::ceil(std::log2((double)Ntot));
+  const auto key = std::make_tuple(nb, b.a.npx_max, (int)two, b.frames);
+  auto it = c->tune.find(key);
+  if (it == c->tune.end()) {
+    std::pair<int, int> best{1, 128};
+    if (c->tuning && Ntot > 0) {
+      const std::pair<int, int> cands[] = {{1, 128}, {1, 256}, {2, 256}, {4, 256}, {8, 256}};
+      float bt = 1e30f;
+      for (auto cd : cands) {
+        cudaEventRecord(c->ev0, c->stream);
+        const int rc = launch(cd.first, cd.second);
+        cudaEventRecord(c->ev1, c->stream);
+        if (rc == STDIC_E_UNSUPPORTED) continue;
+        if (rc) return rc;
+        cudaEventSynchronize(c->ev1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        if (ms < bt) { bt = ms; best = cd; }
+      }
+    }
+    it = c->tune.emplace(key, best).first;
+  }
+  return launch(it->second.first, it->second.second);
+}
+
+}  // namespace
+
+static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0, const double* coords,
+                           int N, int winsize, const int32_t* ws_list, double tol, double* U, double* F,
+                           double* Hpk, int32_t* conv, uint8_t* mark_hole, int* badnum, int precision,
+                           bool filter) {
+  if (!c) return STDIC_E_ARG;
+  if (N < 0 || !frame_ok(fr) || (N > 0 && (!U0 || !coords || !U)) || winsize <= 0 || (winsize & 1) ||
+      winsize > 96 || !(tol > 0))
+    return fail(c, STDIC_E_ARG, "LocalICGNQuadtree: bad arguments (winsize even, 2..96)");
+  if (precision == STDIC_PLAIN_F64 && fr->dtype != STDIC_F64)
+    return fail(c, STDIC_E_ARG, "plain FP64 IC-GN needs double images");
+  if (precision != STDIC_PLAIN_F64 && precision != STDIC_BATCHED_F32)
+    return fail(c, STDIC_E_ARG, "unknown precision");
+  cudaSetDevice(c->device);
+  const bool batched = precision == STDIC_BATCHED_F32;
+  Plan pl;
+  FrameDev d;
+  stage_frame(c, pl, fr, &d, batched, 1);
+  stdic::IcgnArgs a{};
+  pl.in(U0, 2 * (size_t)N, (double**)&a.U0);
+  pl.in(coords, 2 * (size_t)N, (double**)&a.coords);
+  pl.in(ws_list, (size_t)N, (int32_t**)&a.ws_list);
+  pl.out(U, 2 * (size_t)N, &a.U);
+  pl.out_opt(F, 4 * (size_t)N, &a.F);
+  pl.out(Hpk, 21 * (size_t)N, &a.Hpk);
+  pl.out_opt(conv, (size_t)N, &a.conv);
+  pl.out(mark_hole, (size_t)N, &a.mark);
+  int32_t* order = nullptr;
+  if (batched) pl.scratch((size_t)std::max(N, 1), &order);
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  a.f = d.f; a.g = d.g; a.mask = d.mask; a.dfdx = d.dfdx; a.dfdy = d.dfdy;
+  a.W = fr->W; a.H = fr->H; a.N = N;
+  a.ws_all = winsize; a.ws_max = winsize; a.tol = tol;
+  a.npx_max = stdic::grown_tile_pixels(winsize);
+  if (N > 0) {
+    if (!batched) {
+      rc = check_launch(c, stdic::launch_icgn6_plain(a, c->stream), "IC-GN plain");
+    } else {
+      rc = convert_frame(c, fr, &d, 1);
+      if (!rc) rc = check_launch(c, stdic::launch_build_queue(a.ws_list, nullptr, winsize, N, order, nullptr, c->stream), "queue");
+      if (!rc) {
+        stdic::BatchedArgs b{};
+        b.a = a;
+        b.f32 = d.f32; b.g32 = d.g32; b.dfdx32 = d.dfdx32; b.dfdy32 = d.dfdy32;
+        b.order = order; b.queue_head = c->scal; b.two_dof = 0; b.frames = 1; b.g_stride = 0;
+        rc = run_batched(c, b, N);
+      }
+    }
+    if (rc) return rc;
+    if (filter) {
+      rc = check_launch(c, stdic::launch_badpoints(a.conv, N, a.U, a.F, 0, c->scal + 1, c->stream), "bad points");
+      if (rc) return rc;
+    }
+  } else if (filter) {
+    cudaMemsetAsync(c->scal + 1, 0, sizeof(int), c->stream);
+  }
+  rc = pl.finish(c);
+  if (rc) return rc;
+  return filter ? deliver_int(c, c->scal + 1, badnum) : STDIC_OK;
+}
+
+int stdic_icgn_local(stdic_ctx* c, const stdic_frame* fr, const double* U0, const double* coords, int N,
+                     int winsize, const int32_t* ws_list, double tol, double* U, double* F, double* Hpk,
+                     int32_t* conv, uint8_t* mark_hole, int* badnum, int precision) {
+  return icgn_local_impl(c, fr, U0, coords, N, winsize, ws_list, tol, U, F, Hpk, conv, mark_hole, badnum,
+                         precision, true);
+}
+
+int stdic_icgn_subsets(stdic_ctx* c, const stdic_frame* fr, const double* U0, const double* coords, int N,
+                       int winsize, const int32_t* ws_list, double tol, double* U, double* F, double* Hpk,
+                       int32_t* conv, int precision) {
+  return icgn_local_impl(c, fr, U0, coords, N, winsize, ws_list, tol, U, F, Hpk, conv, nullptr, nullptr,
+                         precision, false);
+}
+
+static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, const double* FOld,
+                       const double* udual, const double* vdual, const double* coords, int N,
+                       const int32_t* winsize_list, double mu, double beta, double tol, double* U,
+                       int32_t* conv, int* badnum, int precision, bool filter);
+
+int stdic_subpb1(stdic_ctx* c, const stdic_frame* fr, const double* UOld, const double* FOld,
+                 const double* udual, const double* vdual, const double* coords, int N,
+                 const int32_t* winsize_list, double mu, double beta, double tol, double* U, int32_t* conv,
+                 int* badnum, int precision) {
+  return subpb1_impl(c, fr, UOld, FOld, udual, vdual, coords, N, winsize_list, mu, beta, tol, U, conv,
+                     badnum, precision, true);
+}
+
+int stdic_subpb1_subsets(stdic_ctx* c, const stdic_frame* fr, const double* UOld, const double* FOld,
+                         const double* vdual, const double* coords, int N, const int32_t* winsize_list,
+                         double mu, double tol, double* U, int32_t* conv, int precision) {
+  return subpb1_impl(c, fr, UOld, FOld, nullptr, vdual, coords, N, winsize_list, mu, 0.0, tol, U, conv,
+                     nullptr, precision, false);
+}
+
+static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, const double* FOld,
+                 const double* udual, const double* vdual, const double* coords, int N,
+                       const int32_t* winsize_list, double mu, double beta, double tol, double* U,
+                       int32_t* conv, int* badnum, int precision, bool filter) {
+  (void)udual;
+  (void)beta;
+  if (!c) return STDIC_E_ARG;
+  if (N < 0 || !frame_ok(fr) || (N > 0 && (!UOld || !FOld || !vdual || !coords || !winsize_list || !U)) ||
+      !(tol > 0))
+    return fail(c, STDIC_E_ARG, "Subpb1Quadtree: bad arguments");
+  if (precision == STDIC_PLAIN_F64 && fr->dtype != STDIC_F64)
+    return fail(c, STDIC_E_ARG, "plain FP64 IC-GN needs double images");
+  if (precision != STDIC_PLAIN_F64 && precision != STDIC_BATCHED_F32)
+    return fail(c, STDIC_E_ARG, "unknown precision");
+  cudaSetDevice(c->device);
+  const bool batched = precision == STDIC_BATCHED_F32;
+  // the largest tile follows from the largest requested subset edge
+  int wmax = 2;
+  {
+    std::vector<int32_t> wl(2 * (size_t)N);
+    if (N > 0) {
+      if (is_device_ptr(winsize_list)) {
+        cudaMemcpyAsync(wl.data(), winsize_list, wl.size() * 4, cudaMemcpyDeviceToHost, c->stream);
+        cudaStreamSynchronize(c->stream);
+      } else {
+        std::memcpy(wl.data(), winsize_list, wl.size() * 4);
+      }
+    }
+    for (int32_t w : wl) wmax = std::max(wmax, (int)w);
+  }
+  if (wmax > 96) return fail(c, STDIC_E_ARG, "Subpb1Quadtree: winsize_List entries must be <= 96");
+  Plan pl;
+  FrameDev d;
+  stage_frame(c, pl, fr, &d, batched, 1);
+  stdic::IcgnArgs a{};
+  pl.in(UOld, 2 * (size_t)N, (double**)&a.UOld);
+  pl.in(FOld, 4 * (size_t)N, (double**)&a.FOld);
+  pl.in(vdual, 2 * (size_t)N, (double**)&a.vdual);
+  pl.in(coords, 2 * (size_t)N, (double**)&a.coords);
+  pl.in(winsize_list, 2 * (size_t)N, (int32_t**)&a.wsl2);
+  pl.out(U, 2 * (size_t)N, &a.U);
+  pl.out_opt(conv, (size_t)N, &a.conv);
+  int32_t* order = nullptr;
+  if (batched) pl.scratch((size_t)std::max(N, 1), &order);
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  a.f = d.f; a.g = d.g; a.mask = d.mask; a.dfdx = d.dfdx; a.dfdy = d.dfdy;
+  a.W = fr->W; a.H = fr->H; a.N = N; a.mu = mu; a.tol = tol; a.ws_max = wmax;
+  a.npx_max = stdic::grown_tile_pixels(wmax);
+  if (N > 0) {
+    if (!batched) {
+      rc = check_launch(c, stdic::launch_icgn2_plain(a, c->stream), "Subpb1 plain");
+    } else {
+      rc = convert_frame(c, fr, &d, 1);
+      if (!rc) rc = check_launch(c, stdic::launch_build_queue(nullptr, a.wsl2, 0, N, order, nullptr, c->stream), "queue");
+      if (!rc) {
+        stdic::BatchedArgs b{};
+        b.a = a;
+        b.f32 = d.f32; b.g32 = d.g32; b.dfdx32 = d.dfdx32; b.dfdy32 = d.dfdy32;
+        b.order = order; b.queue_head = c->scal; b.two_dof = 1; b.frames = 1; b.g_stride = 0;
+        rc = run_batched(c, b, N);
+      }
+    }
+    if (rc) return rc;
+    if (filter) {
+      rc = check_launch(c, stdic::launch_badpoints(a.conv, N, a.U, nullptr, 1, c->scal + 1, c->stream), "bad points");
+      if (rc) return rc;
+    }
+  } else if (filter) {
+    cudaMemsetAsync(c->scal + 1, 0, sizeof(int), c->stream);
+  }
+  rc = pl.finish(c);
+  if (rc) return rc;
+  return filter ? deliver_int(c, c->scal + 1, badnum) : STDIC_OK;
+}
+
+int stdic_subpb2(stdic_ctx* c, const double* coords, int N, const int32_t* elems, int E,
+                 const int32_t* dirichlet, int nd, const double* neumann, int nn, int gauss_order,
+                 double beta, double mu, const double* U, const double* F, double alpha, double winstepsize,
+                 double tol, int maxit, double* Uhat, int* iters) {
+  if (!c) return STDIC_E_ARG;
+  if (N < 0 || E < 0 || nd < 0 || nn < 0 || (N > 0 && (!coords || !U || !F || !Uhat)) ||
+      (E > 0 && !elems) || (nd > 0 && !dirichlet) || (nn > 0 && !neumann) || gauss_order < 2 ||
+      gauss_order > 5 || (nn > 0 && !(winstepsize != 0)))
+    return fail(c, STDIC_E_ARG, "Subpb2Quadtree: bad arguments (GaussPtOrder 2..5)");
+  cudaSetDevice(c->device);
+  Plan pl;
+  stdic::Subpb2Args a{};
+  pl.in(coords, 2 * (size_t)N, (double**)&a.coords);
+  pl.in(elems, 8 * (size_t)E, (int32_t**)&a.elems);
+  pl.in(dirichlet, (size_t)nd, (int32_t**)&a.dirichlet);
+  pl.in(neumann, 4 * (size_t)nn, (double**)&a.neumann);
+  pl.in(U, 2 * (size_t)N, (double**)&a.U);
+  pl.in(F, 4 * (size_t)N, (double**)&a.F);
+  pl.out(Uhat, 2 * (size_t)N, &a.Uhat);
+  unsigned char* wsp = nullptr;
+  pl.scratch(stdic::subpb2_workspace_bytes(N, E), &wsp);
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  a.N = N; a.E = E; a.nd = nd; a.nn = nn; a.gauss_order = gauss_order;
+  a.beta = beta; a.mu = mu; a.alpha = alpha; a.winstepsize = winstepsize;
+  a.tol = tol > 0 ? tol : 1e-10;
+  a.maxit = maxit > 0 ? maxit : 10000;
+  if (N > 0) {
+    long long nl = 0;
+    cudaError_t e = stdic::run_subpb2(a, wsp, c->scal + 2, c->scald, c->scal + 3, c->stream, &nl);
+    c->launches += nl;
+    if (e != cudaSuccess) return cuda_fail(c, e, "Subpb2Quadtree");
+  }
+  rc = pl.finish(c);
+  if (rc) return rc;
+  if (N <= 0) { if (iters) *iters = 0; return STDIC_OK; }
+  int hs[2] = {0, 0};
+  cudaError_t e = cudaMemcpyAsync(hs, c->scal + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "Subpb2Quadtree status");
+  if (iters) {
+    if (is_device_ptr(iters)) cudaMemcpyAsync(iters, c->scal + 2, sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
+    else *iters = hs[0];
+  }
+  if (hs[1] == 2) return fail(c, STDIC_E_TIMEOUT, "Subpb2Quadtree: grid barrier wait gave up");
+  if (hs[1] == 3) return fail(c, STDIC_E_ARG, "Subpb2Quadtree: invalid node index or node in >16 elements");
+  if (hs[1] == 1) return fail(c, STDIC_E_NOTCONV, "Subpb2Quadtree: PCG did not reach the tolerance");
+  return STDIC_OK;
+}
+
+}  // extern "C"

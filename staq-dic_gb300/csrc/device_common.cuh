@@ -1,0 +1,315 @@
+// Device helpers shared by the STAQ-DIC kernels (sm_103a).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define STDIC_DEV __device__ __forceinline__
+
+namespace stdic {
+
+constexpr int kMaxIter = 100;  // maxIterNum of funICGNQuadtree.m:59
+
+// ---------------------------------------------------------------------------
+// Keys cubic (a = -1/2) interpolation with clamp-to-edge borders, evaluated in
+// the exact operation order of ba_interp2.cpp:188-233 with every product and
+// sum rounded separately (no fused multiply-add), so results match the
+// reference's compiled C++ bit for bit.  F is M x N column-major; X indexes
+// dim 2 (column), Y dim 1 (row), both 1-based.
+// ---------------------------------------------------------------------------
+STDIC_DEV long long clamp_access(long long M, long long N, long long x, long long y) {
+  x = x < 0 ? 0 : (x >= N ? N - 1 : x);
+  y = y < 0 ? 0 : (y >= M ? M - 1 : y);
+  return M * x + y;
+}
+
+STDIC_DEV double dm(double a, double b) { return __dmul_rn(a, b); }
+STDIC_DEV double da(double a, double b) { return __dadd_rn(a, b); }
+STDIC_DEV double ds(double a, double b) { return __dsub_rn(a, b); }
+
+STDIC_DEV void cubic_weights_exact(double d, double w[4]) {
+  const double dd = dm(d, d), ddd = dm(dd, d);
+  // 0.5 * (-d + 2 dd - ddd), 0.5 * (2 - 5 dd + 3 ddd), 0.5 * (d + 4 dd - 3 ddd), 0.5 * (-dd + ddd)
+  w[0] = dm(0.5, ds(da(-d, dm(2.0, dd)), ddd));
+  w[1] = dm(0.5, da(ds(2.0, dm(5.0, dd)), dm(3.0, ddd)));
+  w[2] = dm(0.5, ds(da(d, dm(4.0, dd)), dm(3.0, ddd)));
+  w[3] = dm(0.5, da(-dd, ddd));
+}
+
+// The reference's single-precision template computes the weights in double
+// (its literals are double) and rounds them once to float.
+STDIC_DEV void cubic_weights_exact_f32(float d, float w[4]) {
+  const float dd = __fmul_rn(d, d), ddd = __fmul_rn(dd, d);
+  const double D = d, DD = dd, DDD = ddd;
+  w[0] = (float)dm(0.5, ds(da(-D, dm(2.0, DD)), DDD));
+  w[1] = (float)dm(0.5, da(ds(2.0, dm(5.0, DD)), dm(3.0, DDD)));
+  w[2] = (float)dm(0.5, ds(da(D, dm(4.0, DD)), dm(3.0, DDD)));
+  w[3] = (float)dm(0.5, da(-DD, DDD));
+}
+
+STDIC_DEV double ba_cubic_exact(const double* __restrict__ F, long long M, long long N, double X,
+                                double Y) {
+  const double xf = floor(X), yf = floor(Y);
+  double wx[4], wy[4];
+  cubic_weights_exact(ds(X, xf), wx);
+  cubic_weights_exact(ds(Y, yf), wy);
+  const long long x = (long long)(xf - 1), y = (long long)(yf - 1);
+  const bool fast = !(x <= 2 || y <= 2 || x >= N - 3 || y >= M - 3);
+  double acc = 0.0;
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    double row;
+    if (fast) {
+      const long long base = M * (x - 1) + (y - 1 + b);
+      row = dm(wx[0], __ldg(F + base));
+      row = da(row, dm(wx[1], __ldg(F + base + M)));
+      row = da(row, dm(wx[2], __ldg(F + base + 2 * M)));
+      row = da(row, dm(wx[3], __ldg(F + base + 3 * M)));
+    } else {
+      row = dm(wx[0], __ldg(F + clamp_access(M, N, x - 1, y - 1 + b)));
+      row = da(row, dm(wx[1], __ldg(F + clamp_access(M, N, x, y - 1 + b))));
+      row = da(row, dm(wx[2], __ldg(F + clamp_access(M, N, x + 1, y - 1 + b))));
+      row = da(row, dm(wx[3], __ldg(F + clamp_access(M, N, x + 2, y - 1 + b))));
+    }
+    acc = b == 0 ? dm(wy[0], row) : da(acc, dm(wy[b], row));
+  }
+  return acc;
+}
+
+STDIC_DEV float ba_cubic_exact_f32(const float* __restrict__ F, long long M, long long N, float X,
+                                   float Y) {
+  const float xf = floorf(X), yf = floorf(Y);
+  float wx[4], wy[4];
+  cubic_weights_exact_f32(__fsub_rn(X, xf), wx);
+  cubic_weights_exact_f32(__fsub_rn(Y, yf), wy);
+  const long long x = (long long)(xf - 1), y = (long long)(yf - 1);
+  float acc = 0.f;
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    float row = __fmul_rn(wx[0], __ldg(F + clamp_access(M, N, x - 1, y - 1 + b)));
+    row = __fadd_rn(row, __fmul_rn(wx[1], __ldg(F + clamp_access(M, N, x, y - 1 + b))));
+    row = __fadd_rn(row, __fmul_rn(wx[2], __ldg(F + clamp_access(M, N, x + 1, y - 1 + b))));
+    row = __fadd_rn(row, __fmul_rn(wx[3], __ldg(F + clamp_access(M, N, x + 2, y - 1 + b))));
+    acc = b == 0 ? __fmul_rn(wy[0], row) : __fadd_rn(acc, __fmul_rn(wy[b], row));
+  }
+  return acc;
+}
+
+// ---------------------------------------------------------------------------
+// Block-wide sums of K doubles: warp shuffles, then one warp over the partials.
+// scratch must hold K * 32 doubles.  Every thread returns the totals.
+// ---------------------------------------------------------------------------
+template <int K>
+STDIC_DEV void block_sum(double (&v)[K], double* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  }
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) scratch[k * 32 + warp] = v[k];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double t = lane < nw ? scratch[k * 32 + lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      if (lane == 0) scratch[k * 32] = t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = scratch[k * 32];
+  __syncthreads();
+}
+
+STDIC_DEV int block_sum_int(int v, int* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    int t = lane < nw ? scratch[lane] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) scratch[0] = t;
+  }
+  __syncthreads();
+  const int r = scratch[0];
+  __syncthreads();
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// bwselect(BW, c, r, conn) on an m x n tile in shared memory (BW[i + j*m]):
+// the conn-connected component of the nonzero pixels that holds the 1-based
+// seed (r = row along dim 1, c = column along dim 2).  An out-of-range or
+// background seed selects nothing.  Line sweeps along both dimensions repeat
+// until a full pass adds no pixel; every productive pass adds at least one
+// pixel, so the loop ends after at most m*n passes.  Concurrent sweeps only
+// ever set 0 -> 1, so reading a neighbour that another thread is setting can
+// only delay propagation to the next pass, never change the fixed point.
+// ---------------------------------------------------------------------------
+STDIC_DEV bool sel_nb(const volatile uint8_t* s, int m, int n, int i, int j, int conn) {
+  bool r = false;
+  if (i > 0) r |= s[(i - 1) + j * m];
+  if (i + 1 < m) r |= s[(i + 1) + j * m];
+  if (j > 0) r |= s[i + (j - 1) * m];
+  if (j + 1 < n) r |= s[i + (j + 1) * m];
+  if (conn == 8) {
+    if (i > 0 && j > 0) r |= s[(i - 1) + (j - 1) * m];
+    if (i + 1 < m && j > 0) r |= s[(i + 1) + (j - 1) * m];
+    if (i > 0 && j + 1 < n) r |= s[(i - 1) + (j + 1) * m];
+    if (i + 1 < m && j + 1 < n) r |= s[(i + 1) + (j + 1) * m];
+  }
+  return r;
+}
+
+STDIC_DEV void bwselect_block(const uint8_t* allow, uint8_t* sel_, int m, int n, int r1, int c1,
+                              int conn) {
+  volatile uint8_t* sel = sel_;
+  const int npx = m * n;
+  for (int p = threadIdx.x; p < npx; p += blockDim.x) sel[p] = 0;
+  __syncthreads();
+  if (threadIdx.x == 0 && r1 >= 1 && r1 <= m && c1 >= 1 && c1 <= n) {
+    const int s = (r1 - 1) + (c1 - 1) * m;
+    if (allow[s]) sel[s] = 1;
+  }
+  __syncthreads();
+  for (;;) {
+    int changed = 0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      for (int i = 0; i < m; ++i) {
+        const int p = i + j * m;
+        if (!sel[p] && allow[p] && sel_nb(sel, m, n, i, j, conn)) { sel[p] = 1; changed = 1; }
+      }
+      for (int i = m - 1; i >= 0; --i) {
+        const int p = i + j * m;
+        if (!sel[p] && allow[p] && sel_nb(sel, m, n, i, j, conn)) { sel[p] = 1; changed = 1; }
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      for (int j = 0; j < n; ++j) {
+        const int p = i + j * m;
+        if (!sel[p] && allow[p] && sel_nb(sel, m, n, i, j, conn)) { sel[p] = 1; changed = 1; }
+      }
+      for (int j = n - 1; j >= 0; --j) {
+        const int p = i + j * m;
+        if (!sel[p] && allow[p] && sel_nb(sel, m, n, i, j, conn)) { sel[p] = 1; changed = 1; }
+      }
+    }
+    if (!__syncthreads_or(changed)) break;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// x = A \ b for n <= 6: Cholesky when the diagonal is positive and the
+// factorisation succeeds (MATLAB mldivide's path for a symmetric matrix with
+// positive diagonal), otherwise LU with partial pivoting.  A is row-major.
+// ---------------------------------------------------------------------------
+STDIC_DEV void small_solve(const double* Ain, const double* b, int n, double* x) {
+  double A[36], L[36];
+  for (int k = 0; k < n * n; ++k) A[k] = Ain[k];
+  bool spd = true;
+  for (int i = 0; i < n; ++i)
+    if (!(A[i * n + i] > 0)) spd = false;
+  if (spd) {
+    for (int k = 0; k < n * n; ++k) L[k] = 0;
+    for (int j = 0; j < n && spd; ++j) {
+      double d = A[j * n + j];
+      for (int k = 0; k < j; ++k) d -= L[j * n + k] * L[j * n + k];
+      if (!(d > 0)) { spd = false; break; }
+      const double ljj = sqrt(d);
+      L[j * n + j] = ljj;
+      for (int i = j + 1; i < n; ++i) {
+        double s = A[i * n + j];
+        for (int k = 0; k < j; ++k) s -= L[i * n + k] * L[j * n + k];
+        L[i * n + j] = s / ljj;
+      }
+    }
+    if (spd) {
+      double y[6];
+      for (int i = 0; i < n; ++i) {
+        double s = b[i];
+        for (int k = 0; k < i; ++k) s -= L[i * n + k] * y[k];
+        y[i] = s / L[i * n + i];
+      }
+      for (int i = n - 1; i >= 0; --i) {
+        double s = y[i];
+        for (int k = i + 1; k < n; ++k) s -= L[k * n + i] * x[k];
+        x[i] = s / L[i * n + i];
+      }
+      return;
+    }
+  }
+  double bb[6];
+  for (int i = 0; i < n; ++i) bb[i] = b[i];
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    double amax = fabs(A[k * n + k]);
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(A[i * n + k]) > amax) { amax = fabs(A[i * n + k]); p = i; }
+    if (p != k) {
+      for (int j = 0; j < n; ++j) { const double t = A[k * n + j]; A[k * n + j] = A[p * n + j]; A[p * n + j] = t; }
+      const double t = bb[k]; bb[k] = bb[p]; bb[p] = t;
+    }
+    for (int i = k + 1; i < n; ++i) {
+      const double f = A[i * n + k] / A[k * n + k];
+      for (int j = k; j < n; ++j) A[i * n + j] -= f * A[k * n + j];
+      bb[i] -= f * bb[k];
+    }
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = bb[i];
+    for (int j = i + 1; j < n; ++j) s -= A[i * n + j] * x[j];
+    x[i] = s / A[i * n + i];
+  }
+}
+
+// Inverse-compositional update of P by DeltaP (funICGNQuadtree.m:393-411).
+// Returns false when det(DeltaP) == 0 (the reference then leaves the loop).
+STDIC_DEV bool compose_update(double P[6], const double D[6]) {
+  const double det = (1 + D[0]) * (1 + D[3]) - D[1] * D[2];
+  if (!(det != 0)) return false;
+  const double t1 = (-D[0] - D[0] * D[3] + D[1] * D[2]) / det;
+  const double t2 = -D[1] / det;
+  const double t3 = -D[2] / det;
+  const double t4 = (-D[3] - D[0] * D[3] + D[1] * D[2]) / det;
+  const double t5 = (-D[4] - D[3] * D[4] + D[2] * D[5]) / det;
+  const double t6 = (-D[5] - D[0] * D[5] + D[1] * D[4]) / det;
+  const double a11 = 1 + P[0], a12 = P[2], a13 = P[4];
+  const double a21 = P[1], a22 = 1 + P[3], a23 = P[5];
+  const double b11 = 1 + t1, b12 = t3, b13 = t5;
+  const double b21 = t2, b22 = 1 + t4, b23 = t6;
+  const double m11 = a11 * b11 + a12 * b21;
+  const double m21 = a21 * b11 + a22 * b21;
+  const double m12 = a11 * b12 + a12 * b22;
+  const double m22 = a21 * b12 + a22 * b22;
+  const double m13 = a11 * b13 + a12 * b23 + a13;
+  const double m23 = a21 * b13 + a22 * b23 + a23;
+  P[0] = m11 - 1; P[1] = m21; P[2] = m12; P[3] = m22 - 1; P[4] = m13; P[5] = m23;
+  return true;
+}
+
+// Warped position of tile pixel (dx, dy) = (X - x0, Y - y0), evaluated as
+// (1+P1)*dx + P3*dy + (x0+P5) with separate roundings (funICGNQuadtree.m:151-152).
+STDIC_DEV void warp_exact(const double P[6], double dx, double dy, double x0, double y0,
+                          double* u22, double* v22) {
+  *u22 = da(da(dm(1 + P[0], dx), dm(P[2], dy)), x0 + P[4]);
+  *v22 = da(da(dm(P[1], dx), dm(1 + P[3], dy)), y0 + P[5]);
+}
+
+// Window growth used when part of a subset is masked (funICGNQuadtree.m:70):
+// 2*ceil(sqrt(num/den) * ws / 2) in IEEE double.
+STDIC_DEV double grow_window(double num, double den, int ws) {
+  return 2.0 * ceil(sqrt(num / den) * ws / 2);
+}
+
+}  // namespace stdic

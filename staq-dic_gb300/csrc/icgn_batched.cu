@@ -1,0 +1,669 @@
+// Batched IC-GN (6-DOF first pass and 2-DOF Subpb1) as one persistent kernel.
+//
+// Each CTA holds several teams of TW warps; a team pulls the next subset from a
+// global work queue (nodes ordered by decreasing subset size, so the longest
+// jobs start first) and solves it with the same control flow, mask logic and
+// result codes as the plain FP64 kernels (funICGNQuadtree.m / funICGN_Subpb1.m).
+//
+// Precision: warped positions are formed as integer + FP32 offset, bicubic
+// weights, interpolation and residuals are FP32; the b-vector and the g
+// statistics are accumulated per lane with Kahan compensation, the Hessian
+// with plain FP32 (it only scales the step, never the converged point); lane
+// partials are reduced in FP64 and the 6x6 / 2x2 solves are FP64.
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace stdic {
+namespace {
+
+template <int TW>
+struct Team {
+  int id;    // team index in the CTA
+  int tl;    // thread index in the team
+  static constexpr int TT = TW * 32;
+  STDIC_DEV void sync() const {
+    if constexpr (TW == 1) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" ::"r"(id + 1), "r"(TT) : "memory");
+  }
+  STDIC_DEV int any(int v, int* scratch) const {
+    if constexpr (TW == 1) return __any_sync(0xffffffffu, v);
+    const int w = tl >> 5;
+    const int r = __any_sync(0xffffffffu, v);
+    sync();
+    if ((tl & 31) == 0) scratch[w] = r;
+    sync();
+    int o = 0;
+#pragma unroll
+    for (int k = 0; k < TW; ++k) o |= scratch[k];
+    sync();
+    return o;
+  }
+  STDIC_DEV int sum_int(int v, int* scratch) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if constexpr (TW == 1) return v;
+    sync();
+    if ((tl & 31) == 0) scratch[tl >> 5] = v;
+    sync();
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < TW; ++k) s += scratch[k];
+    sync();
+    return s;
+  }
+  template <int K>
+  STDIC_DEV void sum(double (&v)[K], double* scratch) const {
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    if constexpr (TW == 1) return;
+    sync();
+    if ((tl & 31) == 0)
+#pragma unroll
+      for (int k = 0; k < K; ++k) scratch[k * TW + (tl >> 5)] = v[k];
+    sync();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double s = 0;
+#pragma unroll
+      for (int w = 0; w < TW; ++w) s += scratch[k * TW + w];
+      v[k] = s;
+    }
+    sync();
+  }
+};
+
+struct Kahan {
+  float s = 0.f, c = 0.f;
+  STDIC_DEV void add(float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  STDIC_DEV double value() const { return (double)s - (double)c; }
+};
+
+// flood fill of bwselect restricted to a team (see bwselect_block)
+template <int TW>
+STDIC_DEV void bwselect_team(const Team<TW>& tm, const uint8_t* allow, uint8_t* sel_, int m, int n,
+                             int r1, int c1, int conn, int* iscr) {
+  volatile uint8_t* sel = sel_;
+  const int npx = m * n;
+  for (int p = tm.tl; p < npx; p += tm.TT) sel[p] = 0;
+  tm.sync();
+  if (tm.tl == 0 && r1 >= 1 && r1 <= m && c1 >= 1 && c1 <= n) {
+    const int s = (r1 - 1) + (c1 - 1) * m;
+    if (allow[s]) sel[s] = 1;
+  }
+  tm.sync();
+  for (;;) {
+    int changed = 0;
+    for (int j = tm.tl; j < n; j += tm.TT) {
+      for (int i = 0; i < m; ++i) {
+        const int p = i + j * m;
+        if (!sel[p] && allow[p] && sel_nb(sel, m, n, i, j, conn)) { sel[p] = 1; changed = 1; }
+      }
+      for (int i = m - 1; i >= 0; --i) {
+        const int p = i + j * m;
+        if (!sel[p] && allow[p] && sel_nb(sel, m, n, i, j, conn)) { sel[p] = 1; changed = 1; }
+      }
+    }
+    tm.sync();
+    for (int i = tm.tl; i < m; i += tm.TT) {
+      for (int j = 0; j < n; ++j) {
+        const int p = i + j * m;
+        if (!sel[p] && allow[p] && sel_nb(sel, m, n, i, j, conn)) { sel[p] = 1; changed = 1; }
+      }
+      for (int j = n - 1; j >= 0; --j) {
+        const int p = i + j * m;
+        if (!sel[p] && allow[p] && sel_nb(sel, m, n, i, j, conn)) { sel[p] = 1; changed = 1; }
+      }
+    }
+    if (!tm.any(changed, iscr)) break;
+  }
+  tm.sync();
+}
+
+struct Frame32 {
+  const float* __restrict__ f;
+  const float* __restrict__ g;
+  const uint8_t* __restrict__ mask;
+  const float* __restrict__ gx;
+  const float* __restrict__ gy;
+  int W, H;
+  STDIC_DEV float F(long long x1, long long y1) const { return __ldg(f + (y1 - 1) * W + (x1 - 1)); }
+  STDIC_DEV float M(long long x1, long long y1) const {
+    return (float)__ldg(mask + (y1 - 1) * W + (x1 - 1));
+  }
+  STDIC_DEV float GX(long long x1, long long y1) const {
+    return __ldg(gx + (y1 - 4) * (long long)(W - 6) + (x1 - 4));
+  }
+  STDIC_DEV float GY(long long x1, long long y1) const {
+    return __ldg(gy + (y1 - 4) * (long long)(W - 6) + (x1 - 4));
+  }
+};
+
+STDIC_DEV bool crop_ok32(const Frame32& fr, long long x1, long long x3, long long y1, long long y3) {
+  return x1 >= 4 && x3 <= fr.W - 3 && y1 >= 4 && y3 <= fr.H - 3;
+}
+STDIC_DEV bool mask_crop_ok32(const Frame32& fr, long long x1, long long x3, long long y1,
+                              long long y3) {
+  return x1 >= 1 && x3 <= fr.W && y1 >= 1 && y3 <= fr.H;
+}
+
+// Affine warp is linear in (dx, dy): the tile's extreme positions are at its corners.
+STDIC_DEV bool corners_oob(const Frame32& fr, const double P[6], long long x0, long long y0,
+                           long long x1, long long y1, int mx, int my) {
+  const double dxs[2] = {(double)(x1 - x0), (double)(x1 + mx - 1 - x0)};
+  const double dys[2] = {(double)(y1 - y0), (double)(y1 + my - 1 - y0)};
+  bool bad = false;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const double u22 = (1 + P[0]) * dxs[a] + P[2] * dys[b] + ((double)x0 + P[4]);
+      const double v22 = P[1] * dxs[a] + (1 + P[3]) * dys[b] + ((double)y0 + P[5]);
+      bad |= (u22 < 3 || u22 > (double)fr.W - 2 || v22 < 3 || v22 > (double)fr.H - 2);
+    }
+  return bad;
+}
+
+// Bicubic sample of g at (iu + su, iv + sv): integer base + FP32 offset.
+STDIC_DEV float cubic32(const float* __restrict__ g, int W, int H, int iu, float su, int iv,
+                        float sv) {
+  const float fu = floorf(su), fv = floorf(sv);
+  const float dx = su - fu, dy = sv - fv;
+  // 0-based first tap (x = dim 1); the FP64 corner test keeps positions in
+  // [3, W-2] x [3, H-2], the clamp only guards FP32 rounding at that edge
+  const int xb = min(max(iu + (int)fu - 2, 0), W - 4);
+  const int yb = min(max(iv + (int)fv - 2, 0), H - 4);
+  const float dx2 = dx * dx, dx3 = dx2 * dx, dy2 = dy * dy, dy3 = dy2 * dy;
+  const float wx0 = 0.5f * (-dx + 2.f * dx2 - dx3), wx1 = 0.5f * (2.f - 5.f * dx2 + 3.f * dx3);
+  const float wx2 = 0.5f * (dx + 4.f * dx2 - 3.f * dx3), wx3 = 0.5f * (-dx2 + dx3);
+  const float wy0 = 0.5f * (-dy + 2.f * dy2 - dy3), wy1 = 0.5f * (2.f - 5.f * dy2 + 3.f * dy3);
+  const float wy2 = 0.5f * (dy + 4.f * dy2 - 3.f * dy3), wy3 = 0.5f * (-dy2 + dy3);
+  const float* r = g + (long long)yb * W + xb;
+  float acc;
+  {
+    const float s0 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
+    r += W;
+    const float s1 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
+    r += W;
+    const float s2 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
+    r += W;
+    const float s3 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
+    acc = wy0 * s0 + wy1 * s1 + wy2 * s2 + wy3 * s3;
+  }
+  return acc;
+}
+
+// (i, j) of tile pixel p = i + j*mx, advanced by a fixed stride without division
+struct PixIter {
+  int i, j, di, dj, mx;
+  STDIC_DEV PixIter(int p0, int stride, int mx_) : mx(mx_) {
+    i = p0 % mx_; j = p0 / mx_; di = stride % mx_; dj = stride / mx_;
+  }
+  STDIC_DEV void next() {
+    i += di; j += dj;
+    if (i >= mx) { i -= mx; ++j; }
+  }
+};
+
+struct TeamCtl {
+  double P[6];
+  double Hm[36];
+  double nN, nA, nI;
+  int flag;
+  int item;
+};
+
+}  // namespace
+
+// Dynamic shared memory per team: npx_max floats (tempg) + npx_max floats
+// (tempf, 2-DOF only) + 4 npx_max bytes + reduction scratch.
+template <int TW, bool TWO>
+__global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  const IcgnArgs& a = B.a;
+  Team<TW> tm;
+  tm.id = threadIdx.x / Team<TW>::TT;
+  tm.tl = threadIdx.x % Team<TW>::TT;
+  const int npxm = a.npx_max;
+  const size_t team_bytes =
+      ((size_t)npxm * (TWO ? 8 : 4) + 4 * (size_t)npxm + 15) / 16 * 16 + sizeof(TeamCtl) +
+      sizeof(double) * 24 * TW + 16 * TW + 64;
+  unsigned char* base = dsm + team_bytes * tm.id;
+  float* tg = (float*)base;
+  float* tf = tg + npxm;  // 2-DOF only
+  uint8_t* mtile = (uint8_t*)(tg + (TWO ? 2 : 1) * npxm);
+  uint8_t* bwf = mtile + npxm;
+  uint8_t* bwg = bwf + npxm;
+  uint8_t* tmp = bwg + npxm;
+  TeamCtl* ctl = (TeamCtl*)(base + ((size_t)npxm * (TWO ? 8 : 4) + 4 * (size_t)npxm + 15) / 16 * 16);
+  double* dscr = (double*)(ctl + 1);
+  int* iscr = (int*)(dscr + 24 * TW);
+
+  const int Ntot = a.N * (B.frames > 0 ? B.frames : 1);
+  const double tol = a.tol;
+  for (;;) {
+    if (tm.tl == 0) {
+      // frames interleaved so that every frame's largest subsets start first
+      const int q = atomicAdd(B.queue_head, 1);
+      const int nf = B.frames > 0 ? B.frames : 1;
+      ctl->item = q < Ntot ? B.order[q / nf] + (q % nf) * a.N : -1;
+    }
+    tm.sync();
+    const int item = ctl->item;
+    tm.sync();
+    if (item < 0) break;
+    const int node = item % a.N;
+    const int frame = item / a.N;
+    Frame32 fr{B.f32, B.g32 + (long long)frame * B.g_stride, a.mask, B.dfdx32, B.dfdy32, a.W, a.H};
+    const long long x0 = llround(a.coords[node]), y0 = llround(a.coords[a.N + node]);
+
+    // ---------------- per-subset set-up ----------------
+    int wx, wy;
+    double P[6];
+    if constexpr (TWO) {
+      wx = a.wsl2[node]; wy = a.wsl2[a.N + node];
+      for (int k = 0; k < 4; ++k) P[k] = a.FOld[4 * item + k];
+      P[4] = a.UOld[2 * item]; P[5] = a.UOld[2 * item + 1];
+    } else {
+      wx = wy = a.ws_list ? a.ws_list[node] : a.ws_all;
+      P[0] = P[1] = P[2] = P[3] = 0;
+      P[4] = a.U0[2 * item]; P[5] = a.U0[2 * item + 1];
+    }
+    const int ws0 = wx;
+    long long x1 = x0 - wx / 2, x3 = x0 + wx / 2, y1 = y0 - wy / 2, y3 = y0 + wy / 2;
+    int code = 0;       // final code
+    bool nan_out = false;
+    bool hdone = false;  // Hm valid for the packed output
+    const int err_code = TWO ? 0 : -1;  // value the reference leaves on a run-time error
+    bool crop_valid = !((wx & 1) || (wy & 1)) && wx >= 0 && wy >= 0 && wx <= a.ws_max &&
+                      wy <= a.ws_max && mask_crop_ok32(fr, x1, x3, y1, y3);
+    int cntf = 0, nanf = 0;
+    if (crop_valid) {
+      const int mx = wx + 1, npx = (wx + 1) * (wy + 1);
+      for (int p = tm.tl; p < npx; p += tm.TT) {
+        const int i = p % mx, j = p / mx;
+        const float t = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j);
+        if (t != t) nanf = 1;
+        if (t == 0.f) ++cntf;
+      }
+    }
+    cntf = tm.sum_int(cntf, iscr);
+    nanf = tm.any(nanf, iscr);
+    if constexpr (!TWO) {
+      if (a.mark && tm.tl == 0) a.mark[item] = (!crop_valid || cntf > 0) ? 1 : 0;
+    }
+    const double npx0 = (double)(wx + 1) * (double)(wy + 1);
+    double meanf = 0, bottomf = 0, A11 = 0, A12 = 0, A22 = 0, sabs = 0;
+    int mx = 0, my = 0, npx = 0, sc = 0, sr = 0;
+    if (!crop_valid || !crop_ok32(fr, x1, x3, y1, y3) || nanf) {
+      code = err_code; nan_out = true;
+    } else if (!((double)cntf < 0.4 * npx0)) {
+      code = kMaxIter + 2;
+      if constexpr (!TWO) { P[0] = P[1] = P[2] = P[3] = 0; }
+    } else {
+      if ((double)cntf > 0.0 * npx0) {
+        if constexpr (TWO) {
+          {
+            const double aa = (double)(wx + 1) * (double)(wy + 1);
+            wx = (int)grow_window(aa, aa - (double)cntf, wx);
+          }
+          {
+            const double aa = (double)(wx + 1) * (double)(wy + 1);
+            wy = (int)grow_window(aa, aa - (double)cntf, wy);
+          }
+        } else {
+          wx = wy = (int)grow_window(npx0, npx0 - (double)cntf, wx);
+        }
+        x1 = x0 - wx / 2; x3 = x0 + wx / 2; y1 = y0 - wy / 2; y3 = y0 + wy / 2;
+        if (!mask_crop_ok32(fr, x1, x3, y1, y3) || !crop_ok32(fr, x1, x3, y1, y3) ||
+            (wx + 1) * (wy + 1) > npxm) {
+          code = err_code; nan_out = true;
+        }
+      }
+      if (!nan_out) {
+        mx = wx + 1; my = wy + 1; npx = mx * my;
+        sc = (wx + 1) / 2; sr = (wy + 1) / 2;
+        int z = 0;
+        for (int p = tm.tl; p < npx; p += tm.TT) {
+          const int i = p % mx, j = p / mx;
+          const uint8_t mk = __ldg(fr.mask + (y1 + j - 1) * fr.W + (x1 + i - 1)) != 0;
+          mtile[p] = mk;
+          if (!mk) z = 1;
+        }
+        if (tm.any(z, iscr)) bwselect_team(tm, mtile, bwf, mx, my, sr, sc, 4, iscr);
+        else {
+          for (int p = tm.tl; p < npx; p += tm.TT) bwf[p] = 1;
+          tm.sync();
+        }
+      }
+    }
+
+    const uint8_t* bw = bwf;
+    // f-side statistics: Hessian (6x6 or 2x2), meanf, bottomf, sum |tempf|
+    auto f_side = [&]() {
+      double h[21];
+#pragma unroll
+      for (int k = 0; k < 21; ++k) h[k] = 0;
+      float hs[21];
+#pragma unroll
+      for (int k = 0; k < 21; ++k) hs[k] = 0.f;
+      Kahan sf, nf;
+      float sa = 0.f;
+      PixIter it(tm.tl, tm.TT, mx);
+      for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+        const int i = it.i, j = it.j;
+        const float s = (float)bw[p];
+        const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
+        const float fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
+        if constexpr (TWO) tf[p] = fv;
+        sa += fabsf(fv);
+        if (fabsf(fv) > 1e-10f) { sf.add(fv); nf.add(1.f); }
+        if constexpr (TWO) {
+          hs[0] += gx * gx; hs[1] += gx * gy; hs[2] += gy * gy;
+        } else {
+          const float dx = (float)(x1 + i - x0), dy = (float)(y1 + j - y0);
+          const float J[6] = {dx * gx, dx * gy, dy * gx, dy * gy, gx, gy};
+          int q = 0;
+#pragma unroll
+          for (int aa = 0; aa < 6; ++aa)
+#pragma unroll
+            for (int bb = aa; bb < 6; ++bb) hs[q++] += J[aa] * J[bb];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 21; ++k) h[k] = hs[k];
+      tm.template sum<21>(h, dscr);
+      double st[3] = {sf.value(), nf.value(), (double)sa};
+      tm.template sum<3>(st, dscr);
+      const double cnt = st[1];
+      const double mean = st[0] / cnt;
+      Kahan q;
+      PixIter it2(tm.tl, tm.TT, mx);
+      for (int p = tm.tl; p < npx; p += tm.TT, it2.next()) {
+        const int i = it2.i, j = it2.j;
+        float fv;
+        if constexpr (TWO) fv = tf[p];
+        else fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * (float)bw[p];
+        if (fabsf(fv) > 1e-10f) { const float d = fv - (float)mean; q.add(d * d); }
+      }
+      double qq[1] = {q.value()};
+      tm.template sum<1>(qq, dscr);
+      const double var = cnt == 0 ? nan("") : (cnt == 1 ? 0.0 : qq[0] / (cnt - 1));
+      meanf = mean;
+      bottomf = sqrt((cnt - 1) * var);
+      sabs = st[2];
+      if constexpr (TWO) {
+        const double b2 = bottomf * bottomf;
+        A11 = h[0] * 2 / b2 + a.mu;
+        A12 = h[1] * 2 / b2;
+        A22 = h[2] * 2 / b2 + a.mu;
+      } else if (tm.tl == 0) {
+        int q2 = 0;
+        for (int aa = 0; aa < 6; ++aa)
+          for (int bb = aa; bb < 6; ++bb) { ctl->Hm[aa * 6 + bb] = h[q2]; ctl->Hm[bb * 6 + aa] = h[q2]; ++q2; }
+      }
+      tm.sync();
+    };
+
+    bool run = (code == 0 && !nan_out);
+    if (run) { f_side(); hdone = true; }
+    double normNew = 1, normAbs = 1, normInit = 0;
+    int step = 0, cg = 0;
+    bool err = false;
+    while (run && step <= kMaxIter && normNew > tol && normAbs > tol) {
+      ++step;
+      if constexpr (!TWO) {
+        if (step > 1 && (double)cntf > 0.0 * npx0) {
+          const double r = sqrt((double)((ws0 + 1) * (ws0 + 1)) / (double)cg) * wx / 2;
+          if (!isfinite(r)) { err = true; break; }
+          const int nws = 2 * (int)ceil(r);
+          if (nws != wx) {
+            const long long nx1 = x0 - nws / 2, nx3 = x0 + nws / 2, ny1 = y0 - nws / 2, ny3 = y0 + nws / 2;
+            if (!mask_crop_ok32(fr, nx1, nx3, ny1, ny3)) { err = true; break; }
+            if (corners_oob(fr, P, x0, y0, nx1, ny1, nws + 1, nws + 1)) { normNew = 1e6; break; }
+            err = true;
+            break;
+          }
+        }
+      }
+      if (corners_oob(fr, P, x0, y0, x1, y1, mx, my)) { normNew = 1e6; break; }
+      // integer base + FP32 offsets of the warp
+      const double bu = (double)x0 + P[4], bv = (double)y0 + P[5];
+      const int iu = (int)floor(bu), iv = (int)floor(bv);
+      const float fu = (float)(bu - iu), fv0 = (float)(bv - iv);
+      const float p0 = (float)(1 + P[0]), p1 = (float)P[1], p2 = (float)P[2], p3 = (float)(1 + P[3]);
+      const float dx0 = (float)(x1 - x0), dy0 = (float)(y1 - y0);
+      int zg = 0, nang = 0;
+      PixIter it(tm.tl, tm.TT, mx);
+      for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+        const int i = it.i, j = it.j;
+        const float dx = dx0 + (float)i, dy = dy0 + (float)j;
+        const float su = fu + p0 * dx + p2 * dy;
+        const float sv = fv0 + p1 * dx + p3 * dy;
+        const float t = cubic32(fr.g, fr.W, fr.H, iu, su, iv, sv);
+        tg[p] = t;
+        if (t != t) nang = 1;
+        if (t == 0.f) ++zg;
+      }
+      zg = tm.sum_int(zg, iscr);
+      if (tm.any(nang, iscr)) { err = true; break; }
+      if (cntf > 0 || zg > 0) {
+        for (int p = tm.tl; p < npx; p += tm.TT) tmp[p] = tg[p] != 0.f;
+        tm.sync();
+        bwselect_team(tm, tmp, bwg, mx, my, sr, sc, TWO ? 4 : 8, iscr);
+        int anyzero = 0;
+        for (int p = tm.tl; p < npx; p += tm.TT) anyzero |= !bwg[p];
+        if (!tm.any(anyzero, iscr)) bwselect_team(tm, mtile, bwg, mx, my, sr, sc, 8, iscr);
+        int cnt = 0;
+        for (int p = tm.tl; p < npx; p += tm.TT) {
+          tg[p] *= (float)bwg[p];
+          cnt += bwg[p];
+        }
+        cg = tm.sum_int(cnt, iscr);
+        if constexpr (TWO) {
+          bw = bwg;
+          f_side();
+        }
+      }
+      // g statistics
+      Kahan sg, ng;
+      for (int p = tm.tl; p < npx; p += tm.TT) {
+        const float t = tg[p];
+        if (fabsf(t) > 1e-10f) { sg.add(t); ng.add(1.f); }
+      }
+      double st[2] = {sg.value(), ng.value()};
+      tm.template sum<2>(st, dscr);
+      const double meang = st[0] / st[1];
+      Kahan qg;
+      for (int p = tm.tl; p < npx; p += tm.TT) {
+        const float t = tg[p];
+        if (fabsf(t) > 1e-10f) { const float d = t - (float)meang; qg.add(d * d); }
+      }
+      double qq[1] = {qg.value()};
+      tm.template sum<1>(qq, dscr);
+      const double cntg = st[1];
+      const double varg = cntg == 0 ? nan("") : (cntg == 1 ? 0.0 : qq[0] / (cntg - 1));
+      const double bottomg = sqrt((cntg - 1) * varg);
+      const float mf = (float)meanf, ibf = (float)(1.0 / bottomf);
+      const float mg = (float)meang, ibg = (float)(1.0 / bottomg);
+      double b2[6];
+      if constexpr (TWO) {
+        Kahan k0, k1;
+        PixIter it3(tm.tl, tm.TT, mx);
+        for (int p = tm.tl; p < npx; p += tm.TT, it3.next()) {
+          const int i = it3.i, j = it3.j;
+          const float s = (float)bw[p];
+          const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
+          const float r = (tf[p] - mf) * ibf - (tg[p] - mg) * ibg;
+          k0.add(gx * r);
+          k1.add(gy * r);
+        }
+        b2[0] = k0.value(); b2[1] = k1.value();
+        double t2[2] = {b2[0], b2[1]};
+        tm.template sum<2>(t2, dscr);
+        b2[0] = t2[0]; b2[1] = t2[1];
+      } else {
+        Kahan k[6];
+        PixIter it3(tm.tl, tm.TT, mx);
+        for (int p = tm.tl; p < npx; p += tm.TT, it3.next()) {
+          const int i = it3.i, j = it3.j;
+          const float s = (float)bw[p];
+          const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
+          const float fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
+          const float dx = dx0 + (float)i, dy = dy0 + (float)j;
+          const float r = (fv - mf) * ibf - (tg[p] - mg) * ibg;
+          const float gxr = gx * r, gyr = gy * r;
+          k[0].add(dx * gxr); k[1].add(dx * gyr); k[2].add(dy * gxr); k[3].add(dy * gyr);
+          k[4].add(gxr); k[5].add(gyr);
+        }
+#pragma unroll
+        for (int q = 0; q < 6; ++q) b2[q] = k[q].value();
+        tm.template sum<6>(b2, dscr);
+      }
+      if (tm.tl == 0) {
+        int done = 0;
+        double Pn[6];
+        for (int k = 0; k < 6; ++k) Pn[k] = P[k];
+        double nN, nA;
+        if constexpr (TWO) {
+          const double b0 = bottomf * b2[0], b1 = bottomf * b2[1];
+          const double tb0 = b0 * 2 / (bottomf * bottomf) + a.mu * (P[4] - a.UOld[2 * item] - a.vdual[2 * item]);
+          const double tb1 = b1 * 2 / (bottomf * bottomf) + a.mu * (P[5] - a.UOld[2 * item + 1] - a.vdual[2 * item + 1]);
+          const double dmax = isnan(A11) ? A22 : (isnan(A22) ? A11 : fmax(A11, A22));
+          const double Hm[4] = {A11 + 1e-3 * dmax, A12, A12, A22 + 1e-3 * dmax};
+          const double rhs[2] = {tb0, tb1};
+          double dP[2];
+          small_solve(Hm, rhs, 2, dP);
+          nN = sqrt(tb0 * tb0 + tb1 * tb1);
+          nA = nN;
+          const double nI = step == 1 ? nN : normInit;
+          ctl->nI = nI;
+          nN = nI > tol ? nN / nI : 0;
+          if (nN < tol || nA < tol) done = 1;
+          else {
+            const double D[6] = {0, 0, 0, 0, -dP[0], -dP[1]};
+            if (!compose_update(Pn, D)) done = 2;
+          }
+        } else {
+          double b[6], nb = 0;
+          for (int k = 0; k < 6; ++k) { b[k] = bottomf * b2[k]; nb += b[k] * b[k]; }
+          nN = sqrt(nb);
+          nA = nN;
+          const double nI = step == 1 ? nN : normInit;
+          ctl->nI = nI;
+          nN = nI > tol ? nN / nI : 0;
+          if (nN < tol || nA < tol) done = 1;
+          else {
+            double D[6];
+            small_solve(ctl->Hm, b, 6, D);
+            for (int k = 0; k < 6; ++k) D[k] = -D[k];
+            if (!compose_update(Pn, D)) done = 2;
+          }
+        }
+        for (int k = 0; k < 6; ++k) ctl->P[k] = Pn[k];
+        ctl->nN = nN;
+        ctl->nA = nA;
+        ctl->flag = done;
+      }
+      tm.sync();
+      normInit = ctl->nI;
+      normNew = ctl->nN;
+      normAbs = ctl->nA;
+      const int done = ctl->flag;
+      for (int k = 0; k < 6; ++k) P[k] = ctl->P[k];
+      tm.sync();
+      if (done) break;
+    }
+    if (run) {
+      if (err) { code = err_code; nan_out = true; }
+      else {
+        code = step;
+        if (!(normNew < tol || normAbs < tol)) code = kMaxIter + 1;
+        if (isnan(normNew)) code = kMaxIter + 1;
+        if constexpr (TWO) {
+          double v[1] = {0};
+          for (int p = tm.tl; p < npx; p += tm.TT) v[0] += fabsf(tf[p]);
+          tm.template sum<1>(v, dscr);
+          sabs = v[0];
+        }
+        if (sabs < 1e-6) code = kMaxIter + 3;
+      }
+    }
+    if (tm.tl == 0) {
+      a.conv[item] = code;
+      a.U[2 * item] = nan_out ? nan("") : P[4];
+      a.U[2 * item + 1] = nan_out ? nan("") : P[5];
+      if constexpr (!TWO) {
+        for (int k = 0; k < 4; ++k) a.F[4 * item + k] = nan_out ? nan("") : P[k];
+        if (a.Hpk) {
+          int q = 0;
+          const bool hv = hdone && !nan_out && code != kMaxIter + 2;
+          for (int col = 0; col < 6; ++col)
+            for (int row = col; row < 6; ++row)
+              a.Hpk[(size_t)q++ * Ntot + item] = hv ? ctl->Hm[row * 6 + col] : 0.0;
+        }
+      }
+    }
+    tm.sync();
+  }
+}
+
+size_t batched_team_bytes(int npx_max, bool two, int tw) {
+  return ((size_t)npx_max * (two ? 8 : 4) + 4 * (size_t)npx_max + 15) / 16 * 16 + sizeof(TeamCtl) +
+         sizeof(double) * 24 * tw + 16 * tw + 64;
+}
+
+template <int TW, bool TWO>
+static cudaError_t launch_tw(const BatchedArgs& b, int blocks, int threads, cudaStream_t s) {
+  const int teams = threads / (TW * 32);
+  const size_t smem = batched_team_bytes(b.a.npx_max, TWO, TW) * teams;
+  if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaFuncSetAttribute(icgn_batched_kernel<TW, TWO>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  icgn_batched_kernel<TW, TWO><<<blocks, threads, smem, s>>>(b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, cudaStream_t s) {
+  const bool two = b.two_dof != 0;
+  switch (b.warps_per_subset) {
+    case 1: return two ? launch_tw<1, true>(b, blocks, threads, s) : launch_tw<1, false>(b, blocks, threads, s);
+    case 2: return two ? launch_tw<2, true>(b, blocks, threads, s) : launch_tw<2, false>(b, blocks, threads, s);
+    case 4: return two ? launch_tw<4, true>(b, blocks, threads, s) : launch_tw<4, false>(b, blocks, threads, s);
+    case 8: return two ? launch_tw<8, true>(b, blocks, threads, s) : launch_tw<8, false>(b, blocks, threads, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// Occupancy of one configuration (blocks per SM), for the autotuner.
+int batched_blocks_per_sm(int tw, bool two, int threads, int npx_max) {
+  const int teams = threads / (tw * 32);
+  const size_t smem = batched_team_bytes(npx_max, two, tw) * teams;
+  int nb = 0;
+  cudaError_t e = cudaSuccess;
+#define STDIC_OCC(TWv, TWOv)                                                                 \
+  e = cudaFuncSetAttribute(icgn_batched_kernel<TWv, TWOv>,                                   \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);          \
+  if (e == cudaSuccess)                                                                      \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, icgn_batched_kernel<TWv, TWOv>,   \
+                                                      threads, smem);
+  switch (tw) {
+    case 1: if (two) { STDIC_OCC(1, true) } else { STDIC_OCC(1, false) } break;
+    case 2: if (two) { STDIC_OCC(2, true) } else { STDIC_OCC(2, false) } break;
+    case 4: if (two) { STDIC_OCC(4, true) } else { STDIC_OCC(4, false) } break;
+    case 8: if (two) { STDIC_OCC(8, true) } else { STDIC_OCC(8, false) } break;
+    default: return 0;
+  }
+#undef STDIC_OCC
+  if (smem > 227 * 1024) return 0;
+  return e == cudaSuccess ? nb : 0;
+}
+
+}  // namespace stdic

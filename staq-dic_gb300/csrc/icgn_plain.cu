@@ -1,0 +1,523 @@
+// Plain FP64 drop-in IC-GN: one CTA per subset (node), reproducing
+//   func_quadtree/funICGNQuadtree.m:29-448   (6-DOF first pass, LocalICGNQuadtree)
+//   func/funICGN_Subpb1.m:34-471            (2-DOF augmented-Lagrangian Subpb1)
+// with the reference's mask logic (bwselect flood fills, window growth, the
+// size-mismatch error of the 6-DOF pass) and result codes.  Per-pixel values
+// (warped positions, interpolated g) are rounded exactly as the reference
+// rounds them; only the order of the block-wide sums differs from a serial loop.
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace stdic {
+
+namespace {
+
+struct Frame64 {
+  const double* __restrict__ f;
+  const double* __restrict__ g;
+  const uint8_t* __restrict__ mask;
+  const double* __restrict__ dfdx;
+  const double* __restrict__ dfdy;
+  int W, H;
+  STDIC_DEV double F(long long x1, long long y1) const { return __ldg(f + (y1 - 1) * W + (x1 - 1)); }
+  STDIC_DEV double M(long long x1, long long y1) const {
+    return (double)__ldg(mask + (y1 - 1) * W + (x1 - 1));
+  }
+  STDIC_DEV double GX(long long x1, long long y1) const {
+    return __ldg(dfdx + (y1 - 4) * (long long)(W - 6) + (x1 - 4));
+  }
+  STDIC_DEV double GY(long long x1, long long y1) const {
+    return __ldg(dfdy + (y1 - 4) * (long long)(W - 6) + (x1 - 4));
+  }
+};
+
+// crops ImgRef(x1:x3,..), Df.DfDx(x1-3:x3-3,..) exist only for 4 <= x1, x3 <= W-3
+STDIC_DEV bool crop_ok(const Frame64& fr, long long x1, long long x3, long long y1, long long y3) {
+  return x1 >= 4 && x3 <= fr.W - 3 && y1 >= 4 && y3 <= fr.H - 3;
+}
+STDIC_DEV bool mask_crop_ok(const Frame64& fr, long long x1, long long x3, long long y1,
+                            long long y3) {
+  return x1 >= 1 && x3 <= fr.W && y1 >= 1 && y3 <= fr.H;
+}
+
+// mean and sqrt((n-1)*var) over |t| > 1e-10 (funICGNQuadtree.m:119-120), two
+// passes like MATLAB's mean/var; var of one sample is 0, of none NaN.
+STDIC_DEV void masked_stats(const double* t, int npx, double* scratch, double* mean_out,
+                            double* bottom_out) {
+  double v[2] = {0.0, 0.0};
+  for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+    const double x = t[p];
+    if (fabs(x) > 1e-10) { v[0] += x; v[1] += 1.0; }
+  }
+  block_sum<2>(v, scratch);
+  const double cnt = v[1];
+  const double mean = v[0] / cnt;
+  double q[1] = {0.0};
+  for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+    const double x = t[p];
+    if (fabs(x) > 1e-10) { const double d = x - mean; q[0] += d * d; }
+  }
+  block_sum<1>(q, scratch);
+  double var;
+  if (cnt == 0) var = nan("");
+  else if (cnt == 1) var = 0.0;
+  else var = q[0] / (cnt - 1);
+  *mean_out = mean;
+  *bottom_out = sqrt((cnt - 1) * var);
+}
+
+// Any warped tile pixel outside [3, W-2] x [3, H-2] (funICGNQuadtree.m:154)
+STDIC_DEV bool any_oob(const Frame64& fr, const double P[6], long long x0, long long y0,
+                       long long x1, long long y1, int mx, int my) {
+  int bad = 0;
+  const int npx = mx * my;
+  for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+    const int i = p % mx, j = p / mx;
+    double u22, v22;
+    warp_exact(P, (double)(x1 + i - x0), (double)(y1 + j - y0), (double)x0, (double)y0, &u22, &v22);
+    if (u22 < 3 || u22 > (double)fr.W - 2 || v22 < 3 || v22 > (double)fr.H - 2) bad = 1;
+  }
+  return __syncthreads_or(bad) != 0;
+}
+
+struct Shared {
+  double P[6];
+  double Hm[36];
+  double red[32 * 21];
+  int ired[32];
+  int flag;
+  int done;
+  int code;
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// 6-DOF first pass.  Dynamic shared memory: npx_max doubles (tempg) + 4
+// npx_max bytes (mask tile, bw_f, bw_g, scratch bitmap).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) icgn6_plain_kernel(IcgnArgs a) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ Shared sh;
+  const int node = blockIdx.x;
+  if (node >= a.N) return;
+  Frame64 fr{(const double*)a.f, (const double*)a.g, a.mask, (const double*)a.dfdx,
+             (const double*)a.dfdy, a.W, a.H};
+  double* tg = (double*)dsm;
+  uint8_t* mtile = (uint8_t*)(tg + a.npx_max);
+  uint8_t* bwf = mtile + a.npx_max;
+  uint8_t* bwg = bwf + a.npx_max;
+  uint8_t* tmp = bwg + a.npx_max;
+
+  const double cx = a.coords[node], cy = a.coords[a.N + node];
+  const long long x0 = llround(cx), y0 = llround(cy);
+  int ws = a.ws_list ? a.ws_list[node] : a.ws_all;
+  const int ws0 = ws;
+  const double tol = a.tol;
+  const double U0x = a.U0[2 * node], U0y = a.U0[2 * node + 1];
+
+  auto finish = [&](int code, bool nan_out, const double* P, const double* Hm) {
+    if (threadIdx.x == 0) {
+      a.conv[node] = code;
+      if (nan_out) {
+        a.U[2 * node] = a.U[2 * node + 1] = nan("");
+        for (int k = 0; k < 4; ++k) a.F[4 * node + k] = nan("");
+      } else {
+        a.U[2 * node] = P[4]; a.U[2 * node + 1] = P[5];
+        for (int k = 0; k < 4; ++k) a.F[4 * node + k] = P[k];
+      }
+      if (a.Hpk) {
+        int q = 0;
+        for (int col = 0; col < 6; ++col)
+          for (int row = col; row < 6; ++row)
+            a.Hpk[(size_t)q++ * a.N + node] = (Hm && !nan_out) ? Hm[row * 6 + col] : 0.0;
+      }
+    }
+  };
+
+  long long x1 = x0 - ws / 2, x3 = x0 + ws / 2, y1 = y0 - ws / 2, y3 = y0 + ws / 2;
+  // markCoordHoleStrain flag of LocalICGNQuadtree.m:112-123 (original window)
+  bool crop_valid = (ws % 2 == 0) && ws <= a.ws_max && mask_crop_ok(fr, x1, x3, y1, y3);
+  int cntf = 0, nanf = 0;
+  if (crop_valid) {
+    const int m = ws + 1;
+    for (int p = threadIdx.x; p < m * m; p += blockDim.x) {
+      const int i = p % m, j = p / m;
+      const double t = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j);
+      if (t != t) nanf = 1;
+      if (t == 0) ++cntf;
+    }
+  }
+  cntf = block_sum_int(cntf, sh.ired);
+  nanf = __syncthreads_or(nanf);
+  if (a.mark && threadIdx.x == 0) a.mark[node] = (!crop_valid || cntf > 0) ? 1 : 0;
+  double P[6] = {0, 0, 0, 0, U0x, U0y};
+  if (!crop_valid || !crop_ok(fr, x1, x3, y1, y3) || nanf) { finish(-1, true, P, nullptr); return; }
+  const double npx0 = (double)((ws + 1) * (ws + 1));
+  if (!((double)cntf < 0.4 * npx0)) { finish(kMaxIter + 2, false, P, nullptr); return; }
+  if ((double)cntf > 0.0 * npx0) {
+    ws = (int)grow_window(npx0, npx0 - (double)cntf, ws);
+    x1 = x0 - ws / 2; x3 = x0 + ws / 2; y1 = y0 - ws / 2; y3 = y0 + ws / 2;
+    if (!mask_crop_ok(fr, x1, x3, y1, y3) || !crop_ok(fr, x1, x3, y1, y3) ||
+        (ws + 1) * (ws + 1) > a.npx_max) {
+      finish(-1, true, P, nullptr);
+      return;
+    }
+  }
+  const int m = ws + 1, npx = m * m;
+  const int c = (ws + 1) / 2;
+  bool has_masked = false;
+  {
+    int z = 0;
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+      const int i = p % m, j = p / m;
+      const uint8_t mk = __ldg(fr.mask + (y1 + j - 1) * fr.W + (x1 + i - 1)) != 0;
+      mtile[p] = mk;
+      if (!mk) z = 1;
+    }
+    has_masked = __syncthreads_or(z) != 0;
+  }
+  if (has_masked) bwselect_block(mtile, bwf, m, m, c, c, 4);
+  else {
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) bwf[p] = 1;
+    __syncthreads();
+  }
+  // tempf (masked) is staged in tg for the statistics, then regenerated on the fly
+  {
+    double h[21];
+#pragma unroll
+    for (int k = 0; k < 21; ++k) h[k] = 0;
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+      const int i = p % m, j = p / m;
+      const double s = (double)bwf[p];
+      const double gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
+      tg[p] = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
+      const double dx = (double)(x1 + i - x0), dy = (double)(y1 + j - y0);
+      const double J[6] = {dx * gx, dx * gy, dy * gx, dy * gy, gx, gy};
+      int q = 0;
+#pragma unroll
+      for (int aa = 0; aa < 6; ++aa)
+#pragma unroll
+        for (int bb = aa; bb < 6; ++bb) h[q++] += J[aa] * J[bb];
+    }
+    block_sum<21>(h, sh.red);
+    if (threadIdx.x == 0) {
+      int q = 0;
+      for (int aa = 0; aa < 6; ++aa)
+        for (int bb = aa; bb < 6; ++bb) { sh.Hm[aa * 6 + bb] = h[q]; sh.Hm[bb * 6 + aa] = h[q]; ++q; }
+    }
+  }
+  double meanf, bottomf;
+  masked_stats(tg, npx, sh.red, &meanf, &bottomf);
+  double sabs;
+  {
+    double v[1] = {0};
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) v[0] += fabs(tg[p]);
+    block_sum<1>(v, sh.red);
+    sabs = v[0];
+  }
+
+  double normNew = 1, normAbs = 1, normInit = 0;
+  int step = 0;
+  int cg = 0;  // sum(tempg_BW2) of the last iteration
+  int code = 0;
+  while (step <= kMaxIter && normNew > tol && normAbs > tol) {
+    ++step;
+    if (step > 1 && (double)cntf > 0.0 * npx0) {
+      const double r = sqrt((double)((ws0 + 1) * (ws0 + 1)) / (double)cg) * ws / 2;
+      if (!isfinite(r)) { code = -1; break; }
+      const int nws = 2 * (int)ceil(r);
+      if (nws != ws) {
+        const long long nx1 = x0 - nws / 2, nx3 = x0 + nws / 2, ny1 = y0 - nws / 2, ny3 = y0 + nws / 2;
+        if (!mask_crop_ok(fr, nx1, nx3, ny1, ny3)) { code = -1; break; }
+        if (any_oob(fr, P, x0, y0, nx1, ny1, nws + 1, nws + 1)) { normNew = 1e6; break; }
+        code = -1;  // tempf and tempg sizes disagree: MATLAB throws
+        break;
+      }
+    }
+    if (any_oob(fr, P, x0, y0, x1, y1, m, m)) { normNew = 1e6; break; }
+    int zg = 0, nang = 0;
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+      const int i = p % m, j = p / m;
+      double u22, v22;
+      warp_exact(P, (double)(x1 + i - x0), (double)(y1 + j - y0), (double)x0, (double)y0, &u22, &v22);
+      const double t = ba_cubic_exact(fr.g, fr.W, fr.H, v22, u22);
+      tg[p] = t;
+      if (t != t) nang = 1;
+      if (t == 0) ++zg;
+    }
+    zg = block_sum_int(zg, sh.ired);
+    if (__syncthreads_or(nang)) { code = -1; break; }
+    if (cntf > 0 || zg > 0) {
+      for (int p = threadIdx.x; p < npx; p += blockDim.x) tmp[p] = tg[p] != 0;
+      __syncthreads();
+      bwselect_block(tmp, bwg, m, m, c, c, 8);
+      int anyzero = 0;
+      for (int p = threadIdx.x; p < npx; p += blockDim.x) anyzero |= !bwg[p];
+      if (!__syncthreads_or(anyzero)) bwselect_block(mtile, bwg, m, m, c, c, 8);
+      int cnt = 0;
+      for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+        tg[p] *= (double)bwg[p];
+        cnt += bwg[p];
+      }
+      cg = block_sum_int(cnt, sh.ired);
+    }
+    double meang, bottomg;
+    masked_stats(tg, npx, sh.red, &meang, &bottomg);
+    double b2[6] = {0, 0, 0, 0, 0, 0};
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+      const int i = p % m, j = p / m;
+      const double s = (double)bwf[p];
+      const double gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
+      const double fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
+      const double dx = (double)(x1 + i - x0), dy = (double)(y1 + j - y0);
+      const double r = (fv - meanf) / bottomf - (tg[p] - meang) / bottomg;
+      b2[0] += dx * gx * r;
+      b2[1] += dx * gy * r;
+      b2[2] += dy * gx * r;
+      b2[3] += dy * gy * r;
+      b2[4] += gx * r;
+      b2[5] += gy * r;
+    }
+    block_sum<6>(b2, sh.red);
+    // control on thread 0, broadcast through shared memory
+    if (threadIdx.x == 0) {
+      double b[6], nb = 0;
+      for (int k = 0; k < 6; ++k) { b[k] = bottomf * b2[k]; nb += b[k] * b[k]; }
+      double nN = sqrt(nb);
+      const double nA = nN;
+      if (step == 1) sh.red[0] = nN;  // normInit
+      const double nI = step == 1 ? nN : normInit;
+      if (nI > tol) nN = nN / nI;
+      else nN = 0;
+      int done = 0;
+      if (nN < tol || nA < tol) done = 1;
+      else {
+        double D[6];
+        small_solve(sh.Hm, b, 6, D);
+        for (int k = 0; k < 6; ++k) D[k] = -D[k];
+        double Pn[6];
+        for (int k = 0; k < 6; ++k) Pn[k] = P[k];
+        if (!compose_update(Pn, D)) done = 2;
+        for (int k = 0; k < 6; ++k) sh.P[k] = Pn[k];
+      }
+      sh.red[1] = nN;
+      sh.red[2] = nA;
+      sh.flag = done;
+      if (done) for (int k = 0; k < 6; ++k) sh.P[k] = P[k];
+    }
+    __syncthreads();
+    if (step == 1) normInit = sh.red[0];
+    normNew = sh.red[1];
+    normAbs = sh.red[2];
+    const int done = sh.flag;
+    for (int k = 0; k < 6; ++k) P[k] = sh.P[k];
+    __syncthreads();
+    if (done) break;
+  }
+  if (code == -1) { finish(-1, true, P, nullptr); return; }
+  int st = step;
+  if (!(normNew < tol || normAbs < tol)) st = kMaxIter + 1;
+  if (isnan(normNew)) st = kMaxIter + 1;
+  if (sabs < 1e-6) st = kMaxIter + 3;
+  finish(st, false, P, sh.Hm);
+}
+
+// ---------------------------------------------------------------------------
+// 2-DOF augmented-Lagrangian Subpb1 (funICGN_Subpb1.m).  Dynamic shared
+// memory as for the 6-DOF kernel plus npx_max doubles for tempf.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) icgn2_plain_kernel(IcgnArgs a) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ Shared sh;
+  const int node = blockIdx.x;
+  if (node >= a.N) return;
+  Frame64 fr{(const double*)a.f, (const double*)a.g, a.mask, (const double*)a.dfdx,
+             (const double*)a.dfdy, a.W, a.H};
+  double* tg = (double*)dsm;
+  double* tf = tg + a.npx_max;
+  uint8_t* mtile = (uint8_t*)(tf + a.npx_max);
+  uint8_t* bwf = mtile + a.npx_max;
+  uint8_t* bwg = bwf + a.npx_max;
+  uint8_t* tmp = bwg + a.npx_max;
+
+  const long long x0 = llround(a.coords[node]), y0 = llround(a.coords[a.N + node]);
+  int wx = a.wsl2[node], wy = a.wsl2[a.N + node];
+  const double tol = a.tol, mu = a.mu;
+  const double UOx = a.UOld[2 * node], UOy = a.UOld[2 * node + 1];
+  const double vdx = a.vdual[2 * node], vdy = a.vdual[2 * node + 1];
+  double P[6] = {a.FOld[4 * node], a.FOld[4 * node + 1], a.FOld[4 * node + 2],
+                 a.FOld[4 * node + 3], UOx, UOy};
+
+  auto finish = [&](int code, bool nan_out) {
+    if (threadIdx.x == 0) {
+      a.conv[node] = code;
+      a.U[2 * node] = nan_out ? nan("") : P[4];
+      a.U[2 * node + 1] = nan_out ? nan("") : P[5];
+    }
+  };
+  long long x1 = x0 - wx / 2, x3 = x0 + wx / 2, y1 = y0 - wy / 2, y3 = y0 + wy / 2;
+  if ((wx & 1) || (wy & 1) || wx < 0 || wy < 0 || !mask_crop_ok(fr, x1, x3, y1, y3) ||
+      !crop_ok(fr, x1, x3, y1, y3) || (wx + 1) * (wy + 1) > a.npx_max) {
+    finish(0, true);
+    return;
+  }
+  int cntf = 0, nanf = 0;
+  {
+    const int mx = wx + 1, npx = (wx + 1) * (wy + 1);
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+      const int i = p % mx, j = p / mx;
+      const double t = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j);
+      if (t != t) nanf = 1;
+      if (t == 0) ++cntf;
+    }
+  }
+  cntf = block_sum_int(cntf, sh.ired);
+  if (__syncthreads_or(nanf)) { finish(0, true); return; }
+  const double npx0 = (double)(wx + 1) * (double)(wy + 1);
+  if (!((double)cntf < 0.4 * npx0)) { finish(kMaxIter + 2, false); return; }
+  if ((double)cntf > 0.0 * npx0) {
+    {
+      const double aa = (double)(wx + 1) * (double)(wy + 1);
+      wx = (int)grow_window(aa, aa - (double)cntf, wx);
+    }
+    {
+      const double aa = (double)(wx + 1) * (double)(wy + 1);
+      wy = (int)grow_window(aa, aa - (double)cntf, wy);
+    }
+    x1 = x0 - wx / 2; x3 = x0 + wx / 2; y1 = y0 - wy / 2; y3 = y0 + wy / 2;
+    if (!mask_crop_ok(fr, x1, x3, y1, y3) || !crop_ok(fr, x1, x3, y1, y3) ||
+        (wx + 1) * (wy + 1) > a.npx_max) {
+      finish(0, true);
+      return;
+    }
+  }
+  const int mx = wx + 1, my = wy + 1, npx = mx * my;
+  const int sc = (wx + 1) / 2, sr = (wy + 1) / 2;  // bwselect(BW, c, r): column, row
+  bool has_masked;
+  {
+    int z = 0;
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+      const int i = p % mx, j = p / mx;
+      const uint8_t mk = __ldg(fr.mask + (y1 + j - 1) * fr.W + (x1 + i - 1)) != 0;
+      mtile[p] = mk;
+      if (!mk) z = 1;
+    }
+    has_masked = __syncthreads_or(z) != 0;
+  }
+  if (has_masked) bwselect_block(mtile, bwf, mx, my, sr, sc, 4);
+  else {
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) bwf[p] = 1;
+    __syncthreads();
+  }
+  // bw points at the selection that currently masks tempf/DfDx/DfDy
+  const uint8_t* bw = bwf;
+  auto f_stats = [&](double* A11, double* A12, double* A22, double* mf, double* bf) {
+    double h[3] = {0, 0, 0};
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+      const int i = p % mx, j = p / mx;
+      const double s = (double)bw[p];
+      const double gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
+      tf[p] = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
+      h[0] += gx * gx; h[1] += gx * gy; h[2] += gy * gy;
+    }
+    block_sum<3>(h, sh.red);
+    masked_stats(tf, npx, sh.red, mf, bf);
+    const double b2 = *bf * *bf;
+    *A11 = h[0] * 2 / b2 + mu;
+    *A12 = h[1] * 2 / b2;
+    *A22 = h[2] * 2 / b2 + mu;
+  };
+  double A11, A12, A22, meanf, bottomf;
+  f_stats(&A11, &A12, &A22, &meanf, &bottomf);
+
+  double normNew = 1, normAbs = 1, normInit = 0;
+  int step = 0;
+  while (step <= 100 && normNew > tol && normAbs > tol) {
+    ++step;
+    if (any_oob(fr, P, x0, y0, x1, y1, mx, my)) { normNew = 1e6; break; }
+    int zg = 0, nang = 0;
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+      const int i = p % mx, j = p / mx;
+      double u22, v22;
+      warp_exact(P, (double)(x1 + i - x0), (double)(y1 + j - y0), (double)x0, (double)y0, &u22, &v22);
+      const double t = ba_cubic_exact(fr.g, fr.W, fr.H, v22, u22);
+      tg[p] = t;
+      if (t != t) nang = 1;
+      if (t == 0) ++zg;
+    }
+    zg = block_sum_int(zg, sh.ired);
+    if (__syncthreads_or(nang)) { step = -1; break; }
+    if (cntf > 0 || zg > 0) {
+      for (int p = threadIdx.x; p < npx; p += blockDim.x) tmp[p] = tg[p] != 0;
+      __syncthreads();
+      bwselect_block(tmp, bwg, mx, my, sr, sc, 4);
+      int anyzero = 0;
+      for (int p = threadIdx.x; p < npx; p += blockDim.x) anyzero |= !bwg[p];
+      if (!__syncthreads_or(anyzero)) bwselect_block(mtile, bwg, mx, my, sr, sc, 8);
+      for (int p = threadIdx.x; p < npx; p += blockDim.x) tg[p] *= (double)bwg[p];
+      __syncthreads();
+      bw = bwg;  // tempf, DfDx, DfDy, H, meanf, bottomf recomputed with tempg_BW2
+      f_stats(&A11, &A12, &A22, &meanf, &bottomf);
+    }
+    double meang, bottomg;
+    masked_stats(tg, npx, sh.red, &meang, &bottomg);
+    double b2[2] = {0, 0};
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+      const int i = p % mx, j = p / mx;
+      const double s = (double)bw[p];
+      const double gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
+      const double r = (tf[p] - meanf) / bottomf - (tg[p] - meang) / bottomg;
+      b2[0] += gx * r;
+      b2[1] += gy * r;
+    }
+    block_sum<2>(b2, sh.red);
+    if (threadIdx.x == 0) {
+      const double b0 = bottomf * b2[0], b1 = bottomf * b2[1];
+      const double tb0 = b0 * 2 / (bottomf * bottomf) + mu * (P[4] - UOx - vdx);
+      const double tb1 = b1 * 2 / (bottomf * bottomf) + mu * (P[5] - UOy - vdy);
+      const double dmax = isnan(A11) ? A22 : (isnan(A22) ? A11 : fmax(A11, A22));
+      const double Hm[4] = {A11 + 1e-3 * dmax, A12, A12, A22 + 1e-3 * dmax};
+      const double rhs[2] = {tb0, tb1};
+      double dP[2];
+      small_solve(Hm, rhs, 2, dP);
+      double nN = sqrt(tb0 * tb0 + tb1 * tb1);
+      const double nA = nN;
+      const double nI = step == 1 ? nN : normInit;
+      if (step == 1) sh.red[0] = nN;
+      if (nI > tol) nN = nN / nI;
+      else nN = 0;
+      int done = 0;
+      double Pn[6];
+      for (int k = 0; k < 6; ++k) Pn[k] = P[k];
+      if (nN < tol || nA < tol) done = 1;
+      else {
+        const double D[6] = {0, 0, 0, 0, -dP[0], -dP[1]};
+        if (!compose_update(Pn, D)) done = 2;
+      }
+      for (int k = 0; k < 6; ++k) sh.P[k] = Pn[k];
+      sh.red[1] = nN;
+      sh.red[2] = nA;
+      sh.flag = done;
+    }
+    __syncthreads();
+    if (step == 1) normInit = sh.red[0];
+    normNew = sh.red[1];
+    normAbs = sh.red[2];
+    const int done = sh.flag;
+    for (int k = 0; k < 6; ++k) P[k] = sh.P[k];
+    __syncthreads();
+    if (done) break;
+  }
+  if (step == -1) { finish(0, true); return; }
+  int st = step;
+  if (!(normNew < tol || normAbs < tol)) st = kMaxIter + 1;
+  if (isnan(normNew)) st = kMaxIter + 1;
+  double v[1] = {0};
+  for (int p = threadIdx.x; p < npx; p += blockDim.x) v[0] += fabs(tf[p]);
+  block_sum<1>(v, sh.red);
+  if (v[0] < 1e-6) st = kMaxIter + 3;
+  finish(st, false);
+}
+
+}  // namespace stdic

@@ -1,0 +1,103 @@
+// Internal kernel interface of libstaqdic (not part of the public C ABI).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace stdic {
+
+// Arguments of the IC-GN kernels (6-DOF first pass and 2-DOF Subpb1).
+struct IcgnArgs {
+  const void* f;
+  const void* g;
+  const uint8_t* mask;
+  const void* dfdx;
+  const void* dfdy;
+  int W, H;
+  int N;
+  const double* coords;  // N x 2 column-major, 1-based
+  // 6-DOF
+  const double* U0;
+  int ws_all;
+  const int32_t* ws_list;  // optional
+  double* F;
+  double* Hpk;      // N x 21, optional
+  uint8_t* mark;    // optional
+  // 2-DOF
+  const double* UOld;
+  const double* FOld;
+  const double* vdual;
+  const int32_t* wsl2;  // N x 2
+  double mu;
+  // common
+  double tol;
+  double* U;
+  int32_t* conv;
+  int ws_max;   // largest requested subset size
+  int npx_max;  // largest tile (pixels) after window growth
+};
+
+// Largest tile after the reference's window growth for a subset size ws.
+inline int grown_tile_pixels(int ws) {
+  // growth factor < sqrt(1/0.6) because fewer than 40 % of the pixels are masked
+  const int wg = 2 * (int)((1.2910 * ws) / 2 + 1) + 2;
+  return (wg + 1) * (wg + 1);
+}
+
+// Batched FP32 queue entry, precomputed per call on the device.
+struct BatchedArgs {
+  IcgnArgs a;
+  const float* f32;
+  const float* g32;
+  const float* dfdx32;
+  const float* dfdy32;
+  const int32_t* order;   // node order of the work queue (largest tiles first)
+  int* queue_head;        // global work counter (scratch)
+  int warps_per_subset;
+  int two_dof;
+  int frames;             // number of frame pairs stacked in g32 (multi-frame)
+  const int32_t* frame_of_node;  // optional
+  long long g_stride;     // elements between stacked deformed frames
+};
+
+cudaError_t launch_interp(const void* F, long long M, long long N, long long P, const void* X,
+                          const void* Y, long long n, void* out, int dtype, cudaStream_t s);
+cudaError_t launch_gradient(const void* img, const uint8_t* mask, int W, int H, void* dfdx,
+                            void* dfdy, int dtype, cudaStream_t s);
+cudaError_t launch_intsearch(const double* f, const double* g, int W, int H, int Sx, int Sy,
+                             double gx0, double gy0, int nx, int ny, int wsx, int wsy, int stepx,
+                             int stepy, double* x, double* y, double* u, double* v, double* cc,
+                             int32_t* peak, cudaStream_t s);
+cudaError_t launch_icgn6_plain(const IcgnArgs& a, cudaStream_t s);
+cudaError_t launch_icgn2_plain(const IcgnArgs& a, cudaStream_t s);
+cudaError_t launch_badpoints(int32_t* conv, int N, double* U, double* F, int two_dof,
+                             int* badnum_dev, cudaStream_t s);
+cudaError_t launch_to_f32(const double* in, float* out, long long n, cudaStream_t s);
+cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int ws_all, int N,
+                               int32_t* order, int* scratch, cudaStream_t s);
+cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, cudaStream_t s);
+
+// Subpb2 (FEM).  All pointers are device pointers.
+struct Subpb2Args {
+  const double* coords;
+  int N;
+  const int32_t* elems;
+  int E;
+  const int32_t* dirichlet;
+  int nd;
+  const double* neumann;
+  int nn;
+  int gauss_order;
+  double beta, mu, alpha, winstepsize;
+  const double* U;
+  const double* F;
+  double tol;
+  int maxit;
+  double* Uhat;
+};
+// workspace: caller-provided device memory of subpb2_workspace_bytes(N, E)
+size_t subpb2_workspace_bytes(int N, int E);
+cudaError_t run_subpb2(const Subpb2Args& a, void* workspace, int* iters_dev, double* resid_dev,
+                       int* status_dev, cudaStream_t s, long long* launches);
+
+}  // namespace stdic

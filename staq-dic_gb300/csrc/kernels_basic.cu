@@ -1,0 +1,437 @@
+// Gather/stencil kernels of the STAQ-DIC hot path and the small helpers the
+// solvers share.
+//   interp_kernel      ba_interp2.cpp:184-234 (bit-identical, see device_common.cuh)
+//   gradient_kernel    func/funImgGradient.m:53-78
+//   intsearch_kernel   func/funIntegerSearch.m:110-170 + func/findpeak.m:27-68 with
+//                      normxcorr2 restated from its published definition
+//   badpoints_kernel   LocalICGNQuadtree.m:153-177 / Subpb1Quadtree.m:173-191
+#include <cfloat>
+
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace stdic {
+
+// ---------------------------------------------------------------------------
+// ba_interp2: one thread per output sample, P layers.
+// ---------------------------------------------------------------------------
+template <class REAL>
+__global__ void interp_kernel(const REAL* __restrict__ F, long long M, long long N, long long P,
+                              const REAL* __restrict__ X, const REAL* __restrict__ Y, long long n,
+                              REAL* __restrict__ out) {
+  const long long LO = M * N;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x) {
+    const REAL x = X[k], y = Y[k];
+    for (long long j = 0; j < P; ++j) {
+      if constexpr (sizeof(REAL) == 8)
+        out[k + j * n] = ba_cubic_exact((const double*)F + j * LO, M, N, x, y);
+      else
+        out[k + j * n] = ba_cubic_exact_f32((const float*)F + j * LO, M, N, x, y);
+    }
+  }
+}
+
+cudaError_t launch_interp(const void* F, long long M, long long N, long long P, const void* X,
+                          const void* Y, long long n, void* out, int dtype, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int threads = 256;
+  long long blocks = (n + threads - 1) / threads;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  if (dtype == 0)
+    interp_kernel<double><<<(int)blocks, threads, 0, s>>>((const double*)F, M, N, P,
+                                                          (const double*)X, (const double*)Y, n,
+                                                          (double*)out);
+  else
+    interp_kernel<float><<<(int)blocks, threads, 0, s>>>((const float*)F, M, N, P, (const float*)X,
+                                                         (const float*)Y, n, (float*)out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// funImgGradient: 7-tap correlation [-1/60 3/20 -3/4 0 3/4 -3/20 1/60] along x
+// and y, crop 3 on each side, times the mask.  A 32 x 8 output tile with its
+// 3-pixel halo is staged in shared memory by coalesced row loads; the sums are
+// rounded in the order of a left-to-right loop over the taps.
+// ---------------------------------------------------------------------------
+template <class REAL>
+__global__ void __launch_bounds__(256) gradient_kernel(const REAL* __restrict__ img,
+                                                       const uint8_t* __restrict__ mask, int W,
+                                                       int H, REAL* __restrict__ dfdx,
+                                                       REAL* __restrict__ dfdy) {
+  constexpr int TX = 32, TY = 8, R = 3;
+  __shared__ REAL t[TY + 2 * R][TX + 2 * R + 1];
+  const int Wo = W - 6, Ho = H - 6;
+  const int bx = blockIdx.x * TX, by = blockIdx.y * TY;  // output tile origin
+  // output (i, j) sits on image pixel (i + 3, j + 3); tile covers image
+  // x in [bx, bx + TX + 6), y in [by, by + TY + 6)
+  for (int q = threadIdx.x; q < (TY + 2 * R) * (TX + 2 * R); q += blockDim.x) {
+    const int ly = q / (TX + 2 * R), lx = q % (TX + 2 * R);
+    const int gx = bx + lx, gy = by + ly;
+    t[ly][lx] = (gx < W && gy < H) ? img[(long long)gy * W + gx] : REAL(0);
+  }
+  __syncthreads();
+  const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
+  const int i = bx + lx, j = by + ly;
+  if (i >= Wo || j >= Ho) return;
+  const REAL h[7] = {REAL(-1.0 / 60), REAL(3.0 / 20), REAL(-3.0 / 4), REAL(0.0),
+                     REAL(3.0 / 4), REAL(-3.0 / 20), REAL(1.0 / 60)};
+  REAL sx = 0, sy = 0;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    if constexpr (sizeof(REAL) == 8) {
+      sx = da(sx, dm(h[k], t[ly + R][lx + k]));
+      sy = da(sy, dm(h[k], t[ly + k][lx + R]));
+    } else {
+      sx = __fadd_rn(sx, __fmul_rn(h[k], t[ly + R][lx + k]));
+      sy = __fadd_rn(sy, __fmul_rn(h[k], t[ly + k][lx + R]));
+    }
+  }
+  const REAL m = (REAL)mask[(long long)(j + 3) * W + (i + 3)];
+  dfdx[(long long)j * Wo + i] = sx * m;
+  dfdy[(long long)j * Wo + i] = sy * m;
+}
+
+cudaError_t launch_gradient(const void* img, const uint8_t* mask, int W, int H, void* dfdx,
+                            void* dfdy, int dtype, cudaStream_t s) {
+  const int Wo = W - 6, Ho = H - 6;
+  if (Wo <= 0 || Ho <= 0) return cudaErrorInvalidValue;
+  dim3 grid((Wo + 31) / 32, (Ho + 7) / 8);
+  if (dtype == 0)
+    gradient_kernel<double><<<grid, 256, 0, s>>>((const double*)img, mask, W, H, (double*)dfdx,
+                                                 (double*)dfdy);
+  else
+    gradient_kernel<float><<<grid, 256, 0, s>>>((const float*)img, mask, W, H, (float*)dfdx,
+                                                (float*)dfdy);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Integer search: one CTA per grid point.  The template C (m x n) and search
+// window D (am x an) are staged in shared memory; each thread owns lags of the
+// cropped (2S+3)^2 normalised cross-correlation map.  normxcorr2's numerics:
+//   num = sum(T.A) - sum(A) sum(T)/mn,  den = sqrt(mn-1) std(T) sqrt(max(sum(A^2)
+//   - sum(A)^2/mn, 0)) over the zero-padded window, C = num/den where
+//   den > sqrt(eps(max den)), and C = 0 where |C| - 1 > sqrt(eps(1)).
+// ---------------------------------------------------------------------------
+STDIC_DEV double eps_of(double x) {
+  x = fabs(x);
+  if (!(x > 0)) return 4.9406564584124654e-324;
+  int e;
+  frexp(x, &e);
+  const int p = e - 53;
+  return p < -1074 ? 4.9406564584124654e-324 : ldexp(1.0, p);
+}
+
+__global__ void __launch_bounds__(256) intsearch_kernel(const double* __restrict__ f,
+                                                        const double* __restrict__ g, int W, int Sx,
+                                                        int Sy, double gx0, double gy0, int nx,
+                                                        int ny, int wsx, int wsy, int stepx,
+                                                        int stepy, double* x, double* y, double* u,
+                                                        double* v, double* cc, int32_t* peak) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ double red[32 * 2];
+  __shared__ int ired[32];
+  __shared__ int best_idx;
+  const int t = blockIdx.x;
+  const int ix = t % nx, iy = t / nx;
+  const long long ii = (long long)gx0 + (long long)ix * stepx;
+  const long long jj = (long long)gy0 + (long long)iy * stepy;
+  const int m = wsx + 1, n = wsy + 1, am = wsx + 1 + 2 * Sx, an = wsy + 1 + 2 * Sy;
+  const int nr = 2 * Sx + 3, nc = 2 * Sy + 3, nl = nr * nc;
+  const double mn = (double)m * (double)n;
+  double* T = (double*)dsm;
+  double* A = T + m * n;
+  double* num = A + am * an;
+  double* den = num + nl;
+  const long long o = iy + (long long)ix * ny;
+  int bad = 0;
+  for (int q = threadIdx.x; q < m * n; q += blockDim.x) {
+    const int a = q % m, b = q / m;
+    const double val = f[(jj - 1 + b) * W + (ii - 1 + a)];
+    T[q] = val;
+    if (!isfinite(val)) bad = 1;
+  }
+  for (int q = threadIdx.x; q < am * an; q += blockDim.x) {
+    const int p = q % am, r = q / am;
+    const double val = g[(jj - 1 - Sy + r) * W + (ii - 1 - Sx + p)];
+    A[q] = val;
+    if (!isfinite(val)) bad = 1;
+  }
+  bad = __syncthreads_or(bad);
+  double s[1] = {0};
+  for (int q = threadIdx.x; q < m * n; q += blockDim.x) s[0] += T[q];
+  block_sum<1>(s, red);
+  const double sumT = s[0];
+  const double meanT = sumT / mn;
+  double q2[1] = {0};
+  for (int q = threadIdx.x; q < m * n; q += blockDim.x) {
+    const double d = T[q] - meanT;
+    q2[0] += d * d;
+  }
+  block_sum<1>(q2, red);
+  const double stdT = sqrt(q2[0] / (mn - 1));
+  if (bad || !(stdT != 0)) {
+    if (threadIdx.x == 0) {
+      u[o] = v[o] = cc[o] = nan("");
+      if (peak) { peak[o] = 0; peak[(long long)nx * ny + o] = 0; }
+      x[o] = (double)(ii + ii + wsx) / 2;
+      y[o] = (double)(jj + jj + wsy) / 2;
+    }
+    return;
+  }
+  const double denomT = sqrt(mn - 1) * stdT;
+  double dmax = 0;
+  for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+    const int dp = k % nr - 1, dq = k / nr - 1;
+    const int a0 = dp < 0 ? -dp : 0, a1 = (am - dp) < m ? (am - dp) : m;
+    const int b0 = dq < 0 ? -dq : 0, b1 = (an - dq) < n ? (an - dq) : n;
+    double xc = 0, sA = 0, sA2 = 0;
+    for (int b = b0; b < b1; ++b) {
+      const double* Tr = T + b * m;
+      const double* Ar = A + (b + dq) * am + dp;
+      for (int a = a0; a < a1; ++a) {
+        const double av = Ar[a];
+        xc = fma(Tr[a], av, xc);
+        sA += av;
+        sA2 = fma(av, av, sA2);
+      }
+    }
+    const double nm = xc - sA * sumT / mn;
+    const double dl = sA2 - (sA * sA) / mn;
+    const double dA = sqrt(dl > 0 ? dl : 0.0);
+    num[k] = nm;
+    den[k] = denomT * dA;
+    dmax = fmax(dmax, fabs(den[k]));
+  }
+  // block max of |den|
+  for (int off = 16; off > 0; off >>= 1) dmax = fmax(dmax, __shfl_down_sync(0xffffffffu, dmax, off));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dmax;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t2 = threadIdx.x < (blockDim.x + 31) / 32 ? red[threadIdx.x] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) t2 = fmax(t2, __shfl_down_sync(0xffffffffu, t2, off));
+    if (threadIdx.x == 0) red[0] = t2;
+  }
+  __syncthreads();
+  const double tolc = sqrt(eps_of(red[0]));
+  const double clip = sqrt(eps_of(1.0));
+  __syncthreads();
+  // C into num[], then first (column-major) argmax
+  double bv = -INFINITY;
+  int bi = 0x7fffffff;
+  for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+    double cv = den[k] > tolc ? num[k] / den[k] : 0.0;
+    if ((fabs(cv) - 1) > clip) cv = 0;
+    num[k] = cv;
+    if (cv > bv) { bv = cv; bi = k; }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const double ov = __shfl_down_sync(0xffffffffu, bv, off);
+    const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+    if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+  }
+  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = bv; ired[threadIdx.x >> 5] = bi; }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nw = (blockDim.x + 31) / 32;
+    double v2 = threadIdx.x < nw ? red[threadIdx.x] : -INFINITY;
+    int i2 = threadIdx.x < nw ? ired[threadIdx.x] : 0x7fffffff;
+    for (int off = 16; off > 0; off >>= 1) {
+      const double ov = __shfl_down_sync(0xffffffffu, v2, off);
+      const int oi = __shfl_down_sync(0xffffffffu, i2, off);
+      if (ov > v2 || (ov == v2 && oi < i2)) { v2 = ov; i2 = oi; }
+    }
+    if (threadIdx.x == 0) best_idx = i2;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const double* C = num;
+  const int imax = best_idx;
+  const double cmax = C[imax];
+  const int yp = imax % nr + 1, xp = imax / nr + 1;
+  double ypeak = yp, xpeak = xp, maxf = cmax;
+  if (!(xp == 1 || xp == nc || yp == 1 || yp == nr)) {
+    double s0 = 0, sx = 0, sy = 0, sxy = 0, sxx = 0, syy = 0;
+    for (int dc = -1; dc <= 1; ++dc)
+      for (int dr = -1; dr <= 1; ++dr) {
+        const double uu = C[(yp - 1 + dr) + (xp - 1 + dc) * nr];
+        s0 += uu; sx += dc * uu; sy += dr * uu; sxy += dc * dr * uu;
+        sxx += dc * dc * uu; syy += dr * dr * uu;
+      }
+    const double A2 = sx / 6, A3 = sy / 6, A4 = sxy / 4;
+    const double Sv = (sxx + syy) / 2 - (2.0 / 3.0) * s0;
+    const double Dd = (sxx - syy) / 2;
+    const double A5 = (Sv + Dd) / 2, A6 = (Sv - Dd) / 2;
+    const double A1 = (s0 - 6 * Sv) / 9;
+    double xo = (-A3 * A4 + 2 * A6 * A2) / (A4 * A4 - 4 * A5 * A6);
+    double yo = -1 / (A4 * A4 - 4 * A5 * A6) * (A4 * A2 - 2 * A5 * A3);
+    if (!(fabs(xo) > 1 || fabs(yo) > 1)) {
+      xo = round(1000 * xo) / 1000;
+      yo = round(1000 * yo) / 1000;
+      xpeak += xo;
+      ypeak += yo;
+      maxf = A1 + xo * A2 + yo * A3 + xo * yo * A4 + xo * xo * A5 + yo * yo * A6;
+    }
+  }
+  u[o] = ypeak - ceil(nr / 2.0);
+  v[o] = xpeak - ceil(nc / 2.0);
+  cc[o] = maxf;
+  if (peak) { peak[o] = yp; peak[(long long)nx * ny + o] = xp; }
+  x[o] = (double)(ii + ii + wsx) / 2;
+  y[o] = (double)(jj + jj + wsy) / 2;
+}
+
+cudaError_t launch_intsearch(const double* f, const double* g, int W, int H, int Sx, int Sy,
+                             double gx0, double gy0, int nx, int ny, int wsx, int wsy, int stepx,
+                             int stepy, double* x, double* y, double* u, double* v, double* cc,
+                             int32_t* peak, cudaStream_t s) {
+  (void)H;
+  if (nx <= 0 || ny <= 0) return cudaSuccess;
+  const size_t m = wsx + 1, n = wsy + 1, am = wsx + 1 + 2 * Sx, an = wsy + 1 + 2 * Sy;
+  const size_t nl = (size_t)(2 * Sx + 3) * (2 * Sy + 3);
+  const size_t smem = sizeof(double) * (m * n + am * an + 2 * nl);
+  if (smem > 200 * 1024) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaFuncSetAttribute(intsearch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  intsearch_kernel<<<nx * ny, 256, smem, s>>>(f, g, W, Sx, Sy, gx0, gy0, nx, ny, wsx, wsy, stepx,
+                                              stepy, x, y, u, v, cc, peak);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// IC-GN plain launchers (kernels in icgn_plain.cu)
+// ---------------------------------------------------------------------------
+__global__ void icgn6_plain_kernel(IcgnArgs a);
+__global__ void icgn2_plain_kernel(IcgnArgs a);
+
+cudaError_t launch_icgn6_plain(const IcgnArgs& a, cudaStream_t s) {
+  if (a.N <= 0) return cudaSuccess;
+  const size_t smem = (size_t)a.npx_max * (sizeof(double) + 4);
+  cudaError_t e = cudaFuncSetAttribute(icgn6_plain_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  icgn6_plain_kernel<<<a.N, 256, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_icgn2_plain(const IcgnArgs& a, cudaStream_t s) {
+  if (a.N <= 0) return cudaSuccess;
+  const size_t smem = (size_t)a.npx_max * (2 * sizeof(double) + 4);
+  cudaError_t e = cudaFuncSetAttribute(icgn2_plain_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  icgn2_plain_kernel<<<a.N, 256, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Bad-subset filter after the per-node loop (one CTA; N is at most a few
+// hundred thousand).  LocalICGNQuadtree: bad = conv<0 | conv>99, then also
+// conv > max(mean+std, 6) of the good codes; Subpb1Quadtree: max(mean+0.25 std,
+// 10).  U (and F for the first pass) become NaN at bad nodes; badnum is
+// #bad - #(conv==102).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) badpoints_kernel(const int32_t* __restrict__ conv, int N,
+                                                         double* U, double* F, int two_dof,
+                                                         int* badnum) {
+  __shared__ double red[32 * 2];
+  __shared__ int ired[32];
+  double v[2] = {0, 0};
+  int nbad = 0, n102 = 0;
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    const int c = conv[k];
+    const bool bad = c < 0 || c > kMaxIter - 1;
+    if (!bad) { v[0] += c; v[1] += 1; }
+    nbad += bad;
+    n102 += (c == kMaxIter + 2);
+  }
+  block_sum<2>(v, red);
+  nbad = block_sum_int(nbad, ired);
+  n102 = block_sum_int(n102, ired);
+  const double ng = v[1];
+  const double mean = v[0] / ng;
+  double q[1] = {0};
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    const int c = conv[k];
+    if (!(c < 0 || c > kMaxIter - 1)) { const double d = c - mean; q[0] += d * d; }
+  }
+  block_sum<1>(q, red);
+  const double sd = ng > 1 ? sqrt(q[0] / (ng - 1)) : (ng == 1 ? 0.0 : nan(""));
+  const double cand = two_dof ? mean + 0.25 * sd : mean + 1.0 * sd;
+  const double floorv = two_dof ? 10.0 : 6.0;
+  const double thr = isnan(cand) ? floorv : fmax(cand, floorv);
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    const int c = conv[k];
+    if (c < 0 || c > kMaxIter - 1 || (double)c > thr) {
+      U[2 * k] = nan("");
+      U[2 * k + 1] = nan("");
+      if (F && !two_dof)
+        for (int a = 0; a < 4; ++a) F[4 * k + a] = nan("");
+    }
+  }
+  if (threadIdx.x == 0 && badnum) *badnum = nbad - n102;
+}
+
+cudaError_t launch_badpoints(int32_t* conv, int N, double* U, double* F, int two_dof,
+                             int* badnum_dev, cudaStream_t s) {
+  if (N <= 0) return cudaSuccess;
+  badpoints_kernel<<<1, 1024, 0, s>>>(conv, N, U, F, two_dof, badnum_dev);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+__global__ void to_f32_kernel(const double* __restrict__ in, float* __restrict__ out, long long n) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x)
+    out[k] = (float)in[k];
+}
+
+cudaError_t launch_to_f32(const double* in, float* out, long long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  to_f32_kernel<<<(int)blocks, 256, 0, s>>>(in, out, n);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Work queue of the batched solver: nodes ordered by decreasing subset size
+// (counting sort over the subset edge length, one CTA).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) build_queue_kernel(const int32_t* __restrict__ ws_list,
+                                                           const int32_t* __restrict__ wsl2,
+                                                           int ws_all, int N, int32_t* order) {
+  __shared__ int hist[256];
+  __shared__ int start[256];
+  for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+  __syncthreads();
+  auto key = [&](int k) {
+    int w = ws_all;
+    if (wsl2) w = max(wsl2[k], wsl2[N + k]);
+    else if (ws_list) w = ws_list[k];
+    return 255 - min(max(w, 0), 255);  // larger subsets first
+  };
+  for (int k = threadIdx.x; k < N; k += blockDim.x) atomicAdd(&hist[key(k)], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int b = 0; b < 256; ++b) { start[b] = acc; acc += hist[b]; }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    const int pos = atomicAdd(&start[key(k)], 1);
+    order[pos] = k;
+  }
+}
+
+cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int ws_all, int N,
+                               int32_t* order, int* scratch, cudaStream_t s) {
+  (void)scratch;
+  if (N <= 0) return cudaSuccess;
+  build_queue_kernel<<<1, 1024, 0, s>>>(ws_list, wsl2, ws_all, N, order);
+  return cudaGetLastError();
+}
+
+}  // namespace stdic

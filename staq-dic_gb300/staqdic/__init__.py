@@ -1,0 +1,11 @@
+"""GB300-native (sm_103a) STAQ-DIC augmented-Lagrangian hot path.
+
+The compute lives in libstaqdic.so (hand-written CUDA behind the C ABI of
+include/staqdic.h); this package is the host-side mirror of the reference's
+MATLAB interface (``staqdic.api``), plus seeded synthetic workloads.
+"""
+from ._lib import Context, StdicError, default_context, load  # noqa: F401
+from .api import (  # noqa: F401
+    LocalICGNQuadtree, Subpb1Quadtree, Subpb2Quadtree, ba_interp2, funICGNQuadtree,
+    funImgGradient, funIntegerSearch, icgn_subsets, subpb1_subsets,
+)

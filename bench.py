@@ -1,0 +1,506 @@
+"""Benchmark of the STAQ-DIC hot path on GB300.
+
+Metric: converged IC-GN subsets per second, counting a subset only when its
+code is 1..100 (and the LocalICGNQuadtree bad-subset filter kept it) and its
+displacement is within 0.01 px of the plain FP64 drop-in on the same inputs.
+
+Step (default workload hole1024): one LocalICGNQuadtree pass — the batched
+FP32 persistent kernel behind stdic_icgn_local — over all nodes of a seeded
+1024^2 plate-with-hole pair (Kirsch field, 1 % strain, quadtree 4..32 px,
+uneven subsets 8..64 px).  Inputs are resident in HBM (`value`); the same call
+with pinned host buffers, copies inside the timed region, gives `e2e`.  The L2
+is flushed (256 MiB write) between timed steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs one replica per GPU (the path has no data-path collective);
+`value` is all ranks' converged subsets over the slowest rank's time.
+--impl reference times the CPU implementation of the path on the host cores
+(the reference is MATLAB, so the oracle's C++ restatement stands in).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "staq-dic_gb300"), ROOT):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "converged IC-GN subsets/s at <=0.01 px vs FP64; batched vs plain on GB300"
+UNIT = "subsets/s"
+TOLPX = 0.01
+WS_MAX = 64
+TOL = 1e-2
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------------------
+def make_workload(name):
+    from staqdic import workloads
+    t = time.time()
+    w = workloads.WORKLOADS[name]()
+    log("workload %s: %d nodes, generated in %.1fs" % (name, w["coordinatesFEM"].shape[0], time.time() - t))
+    return w
+
+
+def flops_per_subset(conv, ws_list):
+    """Algorithmic FLOPs of one IC-GN solve: 70 n_px set-up + 106 n_px per
+    iteration (warp 8, bicubic weights 38, 16-tap sum 35, residual 4, g stats
+    3, b-vector 18), n_px = (ws+1)^2."""
+    npx = (ws_list.astype(np.float64) + 1) ** 2
+    it = np.where((conv >= 1) & (conv <= 101), conv, np.where(conv == 102, 0, 1)).astype(np.float64)
+    return 70.0 * npx + 106.0 * it * npx
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def fp32_peak_tflops(torch):
+    """FP32 CUDA-core throughput: cuBLAS SGEMM with TF32 disabled, 8192^3."""
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        for _ in range(2):
+            torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(5):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del a, b
+        return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
+
+
+def traffic_from_profiles():
+    """DRAM bytes per launch of the batched kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "icgn_batched_hole1024.md")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        if ln.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(ln.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ----------------------------------------------------------------------------
+def run_reference(args, world, rank):
+    """CPU implementation of the path on the host cores (oracle port)."""
+    if rank != 0:
+        return 0
+    from oracle import build as ob
+    ob.build_oracle()
+    from oracle import oracle as orc
+    w = make_workload(args.workload)
+    f = w["f"].astype(np.float64)
+    g = w["g"].astype(np.float64)
+    Df = orc.funImgGradient(f, w["maskf"])
+    coords = w["coordinatesFEM"]
+    N = coords.shape[0]
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    # bounded sample: every k-th node, about 4000 subsets per step
+    k = max(1, N // 4000)
+    idx = np.arange(0, N, k)
+    U0 = w["U0"].reshape(-1, 2)[idx].ravel()
+    cs = coords[idx]
+    wl = w["winsize_list"][idx]
+    for _ in range(args.warmup):
+        orc.icgn6(U0, cs, Df, f, g, wl, TOL)
+    t0 = time.perf_counter()
+    conv_total = 0
+    for _ in range(args.steps):
+        U, F, Hp, conv, mark = orc.icgn6(U0, cs, Df, f, g, wl, TOL)
+        conv_total += int(((conv >= 1) & (conv <= 100)).sum())
+    dt = time.perf_counter() - t0
+    val = conv_total / dt
+    sample = "%d of %d nodes of %s (every %d-th), FP64 IC-GN, %d OpenMP threads" % (
+        idx.size, N, args.workload, k, cores)
+    out = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "impl": "reference",
+           "config": {"workload": args.workload, "nodes": int(N), "sample_nodes": int(idx.size)},
+           "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="hole1024")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import staqdic
+    from staqdic import _lib
+
+    ctx = staqdic.Context(local)
+    # one non-default stream for torch and the library, so the CUDA events of
+    # the timed region bracket the library's kernels
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    L = ctx.L
+    w = make_workload(args.workload)
+    W, H = w["f"].shape
+    N = int(w["coordinatesFEM"].shape[0])
+    ws_list = np.ascontiguousarray(w["winsize_list"], dtype=np.int32)
+
+    def dev(a, dt):
+        return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dt).ravel(order="F"))).cuda()
+
+    f32, g32 = dev(w["f"], np.float32), dev(w["g"], np.float32)
+    mask = dev(w["maskf"], np.uint8)
+    coords = dev(w["coordinatesFEM"], np.float64)
+    U0 = dev(w["U0"], np.float64)
+    wsl = dev(ws_list, np.int32)
+    gx32 = torch.empty((W - 6) * (H - 6), dtype=torch.float32, device="cuda")
+    gy32 = torch.empty_like(gx32)
+    ctx.check(L.stdic_img_gradient(ctx.h, f32.data_ptr(), mask.data_ptr(), W, H, gx32.data_ptr(),
+                                   gy32.data_ptr(), _lib.STDIC_F32), "gradient")
+    f64, g64 = f32.double(), g32.double()
+    gx64 = torch.empty((W - 6) * (H - 6), dtype=torch.float64, device="cuda")
+    gy64 = torch.empty_like(gx64)
+    ctx.check(L.stdic_img_gradient(ctx.h, f64.data_ptr(), mask.data_ptr(), W, H, gx64.data_ptr(),
+                                   gy64.data_ptr(), _lib.STDIC_F64), "gradient64")
+
+    def frame(f, g, gx, gy, dtype):
+        fr = _lib.Frame()
+        fr.f, fr.g, fr.mask, fr.dfdx, fr.dfdy = f.data_ptr(), g.data_ptr(), mask.data_ptr(), gx.data_ptr(), gy.data_ptr()
+        fr.W, fr.H, fr.dtype = W, H, dtype
+        return fr
+
+    fr32 = frame(f32, g32, gx32, gy32, _lib.STDIC_F32)
+    fr64 = frame(f64, g64, gx64, gy64, _lib.STDIC_F64)
+    U = torch.empty(2 * N, dtype=torch.float64, device="cuda")
+    F = torch.empty(4 * N, dtype=torch.float64, device="cuda")
+    Hp = torch.empty(21 * N, dtype=torch.float64, device="cuda")
+    conv = torch.empty(N, dtype=torch.int32, device="cuda")
+    mark = torch.empty(N, dtype=torch.uint8, device="cuda")
+    badnum = torch.zeros(1, dtype=torch.int32, device="cuda")
+    import ctypes
+
+    def solve(fr, prec, outs=(U, F, Hp, conv, mark, badnum)):
+        u, f_, h, c, m, b = outs
+        ctx.check(L.stdic_icgn_local(ctx.h, ctypes.byref(fr), U0.data_ptr(), coords.data_ptr(), N, WS_MAX,
+                                     wsl.data_ptr(), TOL, u.data_ptr(), f_.data_ptr(), h.data_ptr(),
+                                     c.data_ptr(), m.data_ptr(), b.data_ptr(), prec), "icgn_local")
+
+    # ---- plain FP64 drop-in: accuracy reference and the 'plain' throughput
+    solve(fr64, _lib.STDIC_PLAIN_F64)
+    torch.cuda.synchronize()
+    U_plain = U.clone()
+    F_plain = F.clone()
+    conv_plain = conv.clone()
+    plain_ms = []
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        solve(fr64, _lib.STDIC_PLAIN_F64)
+        e1.record()
+        e1.synchronize()
+        plain_ms.append(e0.elapsed_time(e1))
+    plain_conv = int((((conv_plain >= 1) & (conv_plain <= 100)) & ~torch.isnan(U_plain[0::2])).sum())
+    plain_value = plain_conv / (np.mean(plain_ms) * 1e-3)
+
+    # ---- batched FP32: warm-up (the first call autotunes), then K timed steps
+    for _ in range(args.warmup):
+        solve(fr32, _lib.STDIC_BATCHED_F32)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launches
+    sampler = ClockSampler(local)
+    sampler.start()
+    step_ms, solver_ms = [], []
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(float(len(step_ms)))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        solve(fr32, _lib.STDIC_BATCHED_F32)
+        e1.record()
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        solver_ms.append(ctx.last_solver_ms())
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    clocks = sampler.stop()
+    launches = ctx.launches - launches0
+    if dist:
+        dist.barrier()
+
+    # accuracy and the converged count of the last step
+    Uc, cc = U.cpu().numpy(), conv.cpu().numpy()
+    Fc = F.cpu().numpy()
+    Up, cp = U_plain.cpu().numpy(), conv_plain.cpu().numpy()
+    dU = np.abs(Uc - Up).reshape(-1, 2).max(axis=1)
+    ok = (cc >= 1) & (cc <= 100) & ~np.isnan(Uc[0::2]) & ~np.isnan(Up[0::2]) & (dU <= TOLPX)
+    n_conv = int(ok.sum())
+    total_ms = float(np.sum(step_ms))
+    mean_ms = total_ms / len(step_ms)
+    if dist:
+        t = torch.tensor([mean_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        mean_ms = float(t.item())
+        n = torch.tensor([n_conv], device="cuda", dtype=torch.float64)
+        dist.all_reduce(n)
+        n_conv_all = float(n.item())
+    else:
+        n_conv_all = float(n_conv)
+    value = n_conv_all / (mean_ms * 1e-3)
+
+    # ---- end to end through the C ABI with pinned host buffers
+    def pinned(a, dt):
+        t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dt).ravel(order="F"))).pin_memory()
+        return t
+
+    hf, hg, hm = pinned(w["f"], np.float32), pinned(w["g"], np.float32), pinned(w["maskf"], np.uint8)
+    hgx, hgy = gx32.cpu().pin_memory(), gy32.cpu().pin_memory()
+    hU0, hc, hw = pinned(w["U0"], np.float64), pinned(w["coordinatesFEM"], np.float64), pinned(ws_list, np.int32)
+    oU = torch.empty(2 * N, dtype=torch.float64).pin_memory()
+    oF = torch.empty(4 * N, dtype=torch.float64).pin_memory()
+    oH = torch.empty(21 * N, dtype=torch.float64).pin_memory()
+    oc = torch.empty(N, dtype=torch.int32).pin_memory()
+    om = torch.empty(N, dtype=torch.uint8).pin_memory()
+    hb = ctypes.c_int(0)
+    hfr = _lib.Frame()
+    hfr.f, hfr.g, hfr.mask, hfr.dfdx, hfr.dfdy = hf.data_ptr(), hg.data_ptr(), hm.data_ptr(), hgx.data_ptr(), hgy.data_ptr()
+    hfr.W, hfr.H, hfr.dtype = W, H, _lib.STDIC_F32
+    h2d = sum(t.numel() * t.element_size() for t in (hf, hg, hm, hgx, hgy, hU0, hc, hw))
+    d2h = sum(t.numel() * t.element_size() for t in (oU, oF, oH, oc, om)) + 4
+
+    def solve_host():
+        ctx.check(L.stdic_icgn_local(ctx.h, ctypes.byref(hfr), hU0.data_ptr(), hc.data_ptr(), N, WS_MAX,
+                                     hw.data_ptr(), TOL, oU.data_ptr(), oF.data_ptr(), oH.data_ptr(),
+                                     oc.data_ptr(), om.data_ptr(), ctypes.byref(hb), _lib.STDIC_BATCHED_F32),
+                  "icgn_local host")
+
+    for _ in range(2):
+        solve_host()
+    if dist:
+        dist.barrier()
+    e2e_ms = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        solve_host()  # H2D copies, kernels, D2H copies, stream sync
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    oUn, ocn = oU.numpy(), oc.numpy()
+    dUe = np.abs(oUn - Up).reshape(-1, 2).max(axis=1)
+    n_conv_e2e = int(((ocn >= 1) & (ocn <= 100) & ~np.isnan(oUn[0::2]) & ~np.isnan(Up[0::2]) & (dUe <= TOLPX)).sum())
+    e2e_mean = float(np.mean(e2e_ms))
+    if dist:
+        t = torch.tensor([e2e_mean], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_mean = float(t.item())
+        n = torch.tensor([n_conv_e2e], device="cuda", dtype=torch.float64)
+        dist.all_reduce(n)
+        n_conv_e2e = float(n.item())
+    e2e_value = n_conv_e2e / (e2e_mean * 1e-3)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    # ---- roofline of the dominant kernel (the batched persistent IC-GN)
+    peaks, src = measured_peaks()
+    fp32_peak = fp32_peak_tflops(torch)
+    flops = float(flops_per_subset(cc, ws_list).sum())
+    sv = [s for s in solver_ms if s > 0]
+    kern_ms = float(np.mean(sv)) if sv else mean_ms
+    achieved = flops / (kern_ms * 1e-3) / 1e12
+    alg_bytes = (2 * 4 * W * H + W * H + 2 * 4 * (W - 6) * (H - 6) + N * (16 + 16 + 4 + 16 + 32 + 168 + 4 + 1))
+    traffic = traffic_from_profiles()
+    roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak,
+                "traffic": traffic,
+                "peak_source": "cuBLAS SGEMM 8192^3 with TF32 off, measured in this run "
+                               "(MEASURED_PEAKS.json has no FP32 CUDA-core figure)",
+                "flops_per_launch": flops, "kernel_ms": kern_ms}
+    roofline_hbm = {"bound": "hbm", "achieved": alg_bytes / (kern_ms * 1e-3) / 1e9,
+                    "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                    "frac": alg_bytes / (kern_ms * 1e-3) / 1e9 / peaks.get("hbm_gbs"),
+                    "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
+                    "peak_source": src}
+
+    both_conv = (cc >= 1) & (cc <= 100) & (cp >= 1) & (cp <= 100)
+    dF = np.abs(Fc - F_plain.cpu().numpy()).reshape(-1, 4).max(axis=1)
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, args.workload)
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "%s: %dx%d plate with hole, Kirsch 1%% strain, quadtree, %d nodes, "
+                                  "subsets 8..64 px, one LocalICGNQuadtree pass per step" % (args.workload, W, H, N),
+                      "nodes": N, "subset_sizes": {str(k): int(v) for k, v in zip(*np.unique(ws_list, return_counts=True))},
+                      "precision": "batched FP32 (compensated sums, FP64 solves)",
+                      "l2": "flushed between timed steps (256 MiB write)",
+                      "parallelism": "replicas" if world > 1 else "single GPU"},
+           "clocks": clocks,
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                   "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_mean},
+           "gpu_launches": int(launches),
+           "roofline": roofline,
+           "roofline_hbm": roofline_hbm,
+           "plain_fp64": {"value": plain_value, "ms_per_step": float(np.mean(plain_ms)),
+                          "converged": plain_conv},
+           "batched_over_plain": value / plain_value if plain_value > 0 else None,
+           "accuracy": {"converged": n_conv, "nodes": N,
+                        "max_abs_du_px_converged": float(np.nanmax(dU[both_conv])) if both_conv.any() else None,
+                        "max_abs_dF_converged": float(np.nanmax(dF[both_conv])) if both_conv.any() else None,
+                        "codes_equal_frac": float(np.mean(cc == cp))},
+           "wall_s_timed": t_wall}
+    if cpu:
+        out["cpu_baseline"] = cpu
+    print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    ctx.close()
+    return 0
+
+
+def cpu_baseline(w, name):
+    """The oracle (FP64 C++ restatement, OpenMP on all host cores) on a bounded
+    sample of the same workload, about 10-20 s of CPU work."""
+    try:
+        from oracle import build as ob
+        ob.build_oracle()
+        from oracle import oracle as orc
+    except Exception as e:  # pragma: no cover
+        return {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                "sample": "oracle unavailable: %s" % e}
+    f = w["f"].astype(np.float64)
+    g = w["g"].astype(np.float64)
+    Df = orc.funImgGradient(f, w["maskf"])
+    coords = w["coordinatesFEM"]
+    N = coords.shape[0]
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    k = max(1, N // 4000)
+    idx = np.arange(0, N, k)
+    U0 = w["U0"].reshape(-1, 2)[idx].ravel()
+    cs = coords[idx]
+    wl = w["winsize_list"][idx]
+    orc.icgn6(U0, cs, Df, f, g, wl, TOL)
+    t0 = time.perf_counter()
+    nconv, reps = 0, 0
+    while reps < 20 and (time.perf_counter() - t0) < 10.0:
+        U, F, Hp, conv, mark = orc.icgn6(U0, cs, Df, f, g, wl, TOL)
+        nconv += int(((conv >= 1) & (conv <= 100)).sum())
+        reps += 1
+    dt = time.perf_counter() - t0
+    return {"value": nconv / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d of %d nodes of %s (every %d-th) x %d repeats, FP64, OpenMP %d threads" % (
+                idx.size, N, name, k, reps, cores)}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -91,8 +91,13 @@ int stdic_ctx_destroy(stdic_ctx* ctx);
 /* Use an external cudaStream_t (NULL restores the context's own stream). */
 int stdic_ctx_set_stream(stdic_ctx* ctx, void* cuda_stream);
 const char* stdic_last_error(const stdic_ctx* ctx);
-/* Number of kernels this context launched since creation (instrumentation). */
+/* Number of kernels this context launched since creation (instrumentation;
+ * no counterpart in the reference). */
 long long stdic_kernel_launches(const stdic_ctx* ctx);
+/* Device time in ms of the last IC-GN solver kernel (plain or batched), from
+ * CUDA events on the launching stream; -1 if none ran.  Waits for that kernel.
+ * Instrumentation; no counterpart in the reference. */
+double stdic_last_solver_ms(stdic_ctx* ctx);
 
 /* Z = ba_interp2(F, X, Y, 'cubic').  F is M x N x P (P layers), X/Y hold n
  * points (X indexes dim 2, Y dim 1, 1-based); out is n x P.  dtype STDIC_F64 or

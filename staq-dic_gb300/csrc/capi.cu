@@ -12,9 +12,6 @@
 #include "../../include/staqdic.h"
 #include "kernels.h"
 
-namespace stdic {
-int batched_blocks_per_sm(int tw, bool two, int threads, int npx_max);
-}
 
 struct stdic_ctx {
   int device = 0;
@@ -26,6 +23,8 @@ struct stdic_ctx {
   int* scal = nullptr;  // device scalars: [0] queue head, [1] badnum, [2] iters, [3] status
   double* scald = nullptr;  // device double scalars: [0] residual
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t es0 = nullptr, es1 = nullptr;  // around the last IC-GN solver kernel
+  bool solver_timed = false;
   std::string err;
   long long launches = 0;
   // autotuner cache: (N bucket, npx_max, two_dof, frames) -> (warps per subset, threads)
@@ -185,6 +184,8 @@ int stdic_ctx_create(stdic_ctx** out, int device) {
   if (e == cudaSuccess) e = cudaMalloc(&c->scald, 8 * sizeof(double));
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->es0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->es1);
   if (e != cudaSuccess) {
     cudaGetLastError();
     delete c;
@@ -204,6 +205,8 @@ int stdic_ctx_destroy(stdic_ctx* c) {
   if (c->scald) cudaFree(c->scald);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->es0) cudaEventDestroy(c->es0);
+  if (c->es1) cudaEventDestroy(c->es1);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return STDIC_OK;
@@ -218,6 +221,16 @@ int stdic_ctx_set_stream(stdic_ctx* c, void* s) {
 const char* stdic_last_error(const stdic_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
 long long stdic_kernel_launches(const stdic_ctx* c) { return c ? c->launches : 0; }
+
+double stdic_last_solver_ms(stdic_ctx* c) {
+  if (!c || !c->solver_timed) return -1.0;
+  float ms = -1.f;
+  if (cudaEventSynchronize(c->es1) != cudaSuccess || cudaEventElapsedTime(&ms, c->es0, c->es1) != cudaSuccess) {
+    cudaGetLastError();
+    return -1.0;
+  }
+  return (double)ms;
+}
 
 // ---------------------------------------------------------------------------
 int stdic_interp_bicubic(stdic_ctx* c, const void* F, int64_t M, int64_t N, int64_t P, const void* X,
@@ -375,45 +388,81 @@ bool frame_ok(const stdic_frame* fr) {
          (fr->dtype == STDIC_F64 || fr->dtype == STDIC_F32);
 }
 
-// Run the persistent batched kernel with the autotuned (warps per subset,
-// threads per CTA).  On a new problem class every candidate is timed once on
-// the real data (outputs are idempotent) and the fastest is cached.
-int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot) {
-  const bool two = b.two_dof != 0;
-  auto launch = [&](int tw, int threads) -> int {
-    const int per_sm = stdic::batched_blocks_per_sm(tw, two, threads, b.a.npx_max);
-    if (per_sm <= 0) return STDIC_E_UNSUPPORTED;
+// Candidate launch shapes of the persistent batched kernel: (warps per
+// subset, threads per CTA), each with its resident grid, its shared tile slot
+// and the global scratch its teams need.
+struct BatchedCand {
+  int tw, threads, blocks, smem_px;
+  size_t scratch;
+};
+
+std::vector<BatchedCand> batched_candidates(stdic_ctx* c, bool two, int npx_max, int Ntot) {
+  std::vector<BatchedCand> out;
+  const std::pair<int, int> shapes[] = {{1, 128}, {1, 256}, {2, 256}, {4, 256}};
+  for (auto sh : shapes) {
+    const int tw = sh.first, threads = sh.second;
     const int teams_per_block = threads / (32 * tw);
+    // shared slot sized for about 12.5 KB per team (16 resident warps per SM)
+    const int bpp = two ? 12 : 8;
+    int smem_px = (int)((12800 * tw - 512 - 32 * 4 * tw) / bpp);
+    smem_px = std::max(64, std::min(smem_px, npx_max));
+    const int per_sm = stdic::batched_blocks_per_sm(tw, two, threads, smem_px);
+    if (per_sm <= 0) continue;
     int blocks = c->nsm * per_sm;
     blocks = std::max(1, std::min(blocks, (Ntot + teams_per_block - 1) / teams_per_block));
+    const long long teams = (long long)blocks * teams_per_block;
+    out.push_back({tw, threads, blocks, smem_px, stdic::batched_scratch_bytes(npx_max, two, teams)});
+  }
+  return out;
+}
+
+size_t batched_scratch_need(const std::vector<BatchedCand>& cs) {
+  size_t m = 256;
+  for (auto& cd : cs) m = std::max(m, cd.scratch);
+  return m;
+}
+
+// Run the persistent batched kernel with the autotuned launch shape.  On a new
+// problem class every candidate is timed once on the real data (the outputs
+// are idempotent) and the fastest is cached in the context.
+int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector<BatchedCand>& cands) {
+  const bool two = b.two_dof != 0;
+  if (cands.empty()) return fail(c, STDIC_E_UNSUPPORTED, "no launch shape fits this subset size");
+  auto launch = [&](const BatchedCand& cd) -> int {
     cudaError_t e = cudaMemsetAsync(b.queue_head, 0, sizeof(int), c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "queue reset");
-    b.warps_per_subset = tw;
-    return check_launch(c, stdic::launch_icgn_batched(b, blocks, threads, c->stream), "IC-GN batched");
+    b.warps_per_subset = cd.tw;
+    b.smem_px = cd.smem_px;
+    return check_launch(c, stdic::launch_icgn_batched(b, cd.blocks, cd.threads, c->stream), "IC-GN batched");
   };
   const int nb = Ntot <= 0 ? 0 : (int)std::ceil(std::log2((double)Ntot));
   const auto key = std::make_tuple(nb, b.a.npx_max, (int)two, b.frames);
   auto it = c->tune.find(key);
   if (it == c->tune.end()) {
-    std::pair<int, int> best{1, 128};
-    if (c->tuning && Ntot > 0) {
-      const std::pair<int, int> cands[] = {{1, 128}, {1, 256}, {2, 256}, {4, 256}, {8, 256}};
+    std::pair<int, int> best{cands[0].tw, cands[0].threads};
+    if (c->tuning && Ntot > 0 && cands.size() > 1) {
       float bt = 1e30f;
-      for (auto cd : cands) {
+      for (auto& cd : cands) {
         cudaEventRecord(c->ev0, c->stream);
-        const int rc = launch(cd.first, cd.second);
+        const int rc = launch(cd);
         cudaEventRecord(c->ev1, c->stream);
-        if (rc == STDIC_E_UNSUPPORTED) continue;
         if (rc) return rc;
         cudaEventSynchronize(c->ev1);
         float ms = 0;
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-        if (ms < bt) { bt = ms; best = cd; }
+        if (ms < bt) { bt = ms; best = {cd.tw, cd.threads}; }
       }
     }
     it = c->tune.emplace(key, best).first;
   }
-  return launch(it->second.first, it->second.second);
+  const BatchedCand* chosen = &cands[0];
+  for (auto& cd : cands)
+    if (cd.tw == it->second.first && cd.threads == it->second.second) chosen = &cd;
+  cudaEventRecord(c->es0, c->stream);
+  const int rc = launch(*chosen);
+  cudaEventRecord(c->es1, c->stream);
+  c->solver_timed = rc == STDIC_OK;
+  return rc;
 }
 
 }  // namespace
@@ -445,16 +494,26 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
   pl.out_opt(conv, (size_t)N, &a.conv);
   pl.out(mark_hole, (size_t)N, &a.mark);
   int32_t* order = nullptr;
-  if (batched) pl.scratch((size_t)std::max(N, 1), &order);
+  unsigned char* bscr = nullptr;
+  const int npx_max = stdic::grown_tile_pixels(winsize);
+  std::vector<BatchedCand> cands;
+  if (batched) {
+    cands = batched_candidates(c, false, npx_max, N);
+    pl.scratch((size_t)std::max(N, 1), &order);
+    pl.scratch(batched_scratch_need(cands), &bscr);
+  }
   int rc = pl.commit(c);
   if (rc) return rc;
   a.f = d.f; a.g = d.g; a.mask = d.mask; a.dfdx = d.dfdx; a.dfdy = d.dfdy;
   a.W = fr->W; a.H = fr->H; a.N = N;
   a.ws_all = winsize; a.ws_max = winsize; a.tol = tol;
-  a.npx_max = stdic::grown_tile_pixels(winsize);
+  a.npx_max = npx_max;
   if (N > 0) {
     if (!batched) {
+      cudaEventRecord(c->es0, c->stream);
       rc = check_launch(c, stdic::launch_icgn6_plain(a, c->stream), "IC-GN plain");
+      cudaEventRecord(c->es1, c->stream);
+      c->solver_timed = rc == STDIC_OK;
     } else {
       rc = convert_frame(c, fr, &d, 1);
       if (!rc) rc = check_launch(c, stdic::launch_build_queue(a.ws_list, nullptr, winsize, N, order, nullptr, c->stream), "queue");
@@ -463,7 +522,8 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
         b.a = a;
         b.f32 = d.f32; b.g32 = d.g32; b.dfdx32 = d.dfdx32; b.dfdy32 = d.dfdy32;
         b.order = order; b.queue_head = c->scal; b.two_dof = 0; b.frames = 1; b.g_stride = 0;
-        rc = run_batched(c, b, N);
+        b.scratch = bscr;
+        rc = run_batched(c, b, N, cands);
       }
     }
     if (rc) return rc;
@@ -556,15 +616,25 @@ static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, 
   pl.out(U, 2 * (size_t)N, &a.U);
   pl.out_opt(conv, (size_t)N, &a.conv);
   int32_t* order = nullptr;
-  if (batched) pl.scratch((size_t)std::max(N, 1), &order);
+  unsigned char* bscr = nullptr;
+  const int npx_max = stdic::grown_tile_pixels(wmax);
+  std::vector<BatchedCand> cands;
+  if (batched) {
+    cands = batched_candidates(c, true, npx_max, N);
+    pl.scratch((size_t)std::max(N, 1), &order);
+    pl.scratch(batched_scratch_need(cands), &bscr);
+  }
   int rc = pl.commit(c);
   if (rc) return rc;
   a.f = d.f; a.g = d.g; a.mask = d.mask; a.dfdx = d.dfdx; a.dfdy = d.dfdy;
   a.W = fr->W; a.H = fr->H; a.N = N; a.mu = mu; a.tol = tol; a.ws_max = wmax;
-  a.npx_max = stdic::grown_tile_pixels(wmax);
+  a.npx_max = npx_max;
   if (N > 0) {
     if (!batched) {
+      cudaEventRecord(c->es0, c->stream);
       rc = check_launch(c, stdic::launch_icgn2_plain(a, c->stream), "Subpb1 plain");
+      cudaEventRecord(c->es1, c->stream);
+      c->solver_timed = rc == STDIC_OK;
     } else {
       rc = convert_frame(c, fr, &d, 1);
       if (!rc) rc = check_launch(c, stdic::launch_build_queue(nullptr, a.wsl2, 0, N, order, nullptr, c->stream), "queue");
@@ -573,7 +643,8 @@ static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, 
         b.a = a;
         b.f32 = d.f32; b.g32 = d.g32; b.dfdx32 = d.dfdx32; b.dfdy32 = d.dfdy32;
         b.order = order; b.queue_head = c->scal; b.two_dof = 1; b.frames = 1; b.g_stride = 0;
-        rc = run_batched(c, b, N);
+        b.scratch = bscr;
+        rc = run_batched(c, b, N, cands);
       }
     }
     if (rc) return rc;

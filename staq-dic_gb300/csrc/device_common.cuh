@@ -273,6 +273,36 @@ STDIC_DEV void small_solve(const double* Ain, const double* b, int n, double* x)
   }
 }
 
+// x = A \ b for a symmetric 2x2 A = [a11 a12; a12 a22] in registers, with the
+// branch structure of small_solve (Cholesky when it succeeds, else LU with
+// partial pivoting).
+STDIC_DEV void solve2(double a11, double a12, double a22, double b0, double b1, double* x0,
+                      double* x1) {
+  if (a11 > 0 && a22 > 0) {
+    const double l11 = sqrt(a11);
+    const double l21 = a12 / l11;
+    const double d = a22 - l21 * l21;
+    if (d > 0) {
+      const double l22 = sqrt(d);
+      const double y0 = b0 / l11, y1 = (b1 - l21 * y0) / l22;
+      *x1 = y1 / l22;
+      *x0 = (y0 - l21 * *x1) / l11;
+      return;
+    }
+  }
+  double r00 = a11, r01 = a12, r10 = a12, r11 = a22, c0 = b0, c1 = b1;
+  if (fabs(r10) > fabs(r00)) {
+    double t = r00; r00 = r10; r10 = t;
+    t = r01; r01 = r11; r11 = t;
+    t = c0; c0 = c1; c1 = t;
+  }
+  const double f = r10 / r00;
+  r11 -= f * r01;
+  c1 -= f * c0;
+  *x1 = c1 / r11;
+  *x0 = (c0 - r01 * *x1) / r00;
+}
+
 // Inverse-compositional update of P by DeltaP (funICGNQuadtree.m:393-411).
 // Returns false when det(DeltaP) == 0 (the reference then leaves the loop).
 STDIC_DEV bool compose_update(double P[6], const double D[6]) {

@@ -1,15 +1,23 @@
 // Batched IC-GN (6-DOF first pass and 2-DOF Subpb1) as one persistent kernel.
 //
-// Each CTA holds several teams of TW warps; a team pulls the next subset from a
-// global work queue (nodes ordered by decreasing subset size, so the longest
-// jobs start first) and solves it with the same control flow, mask logic and
-// result codes as the plain FP64 kernels (funICGNQuadtree.m / funICGN_Subpb1.m).
+// A team of TW warps (one warp by default) pulls the next subset from a global
+// work queue ordered by decreasing subset size, so the longest solves start
+// first, and runs it with the control flow, mask logic and result codes of the
+// plain FP64 kernels (funICGNQuadtree.m / funICGN_Subpb1.m).
 //
-// Precision: warped positions are formed as integer + FP32 offset, bicubic
-// weights, interpolation and residuals are FP32; the b-vector and the g
-// statistics are accumulated per lane with Kahan compensation, the Hessian
-// with plain FP32 (it only scales the step, never the converged point); lane
-// partials are reduced in FP64 and the 6x6 / 2x2 solves are FP64.
+// Per-subset scratch (interpolated g tile, tempf for the 2-DOF form, four
+// flood-fill bitmaps) lives in shared memory when the tile fits the team's
+// shared slot and otherwise in a per-team slice of a global scratch buffer, so
+// occupancy is set by registers, not by the largest subset of the batch.
+//
+// Precision: warped positions are an integer base plus an FP32 offset;
+// bicubic weights, interpolation and residuals are FP32.  Per-lane sums are
+// Kahan-compensated FP32 (b-vector and g statistics; the g variance is a
+// one-pass shifted sum around meanf), reduced across lanes in FP32 together
+// with their compensations; the Hessian is accumulated in plain FP32 (it only
+// scales the step, never the converged point).  Team totals, the Cholesky
+// factor of the 6x6 Hessian (once per subset), the triangular solves of every
+// iteration and the warp-parameter update are FP64.
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -18,59 +26,66 @@ namespace {
 
 template <int TW>
 struct Team {
-  int id;    // team index in the CTA
-  int tl;    // thread index in the team
+  int id;  // team index in the CTA
+  int tl;  // thread index in the team
   static constexpr int TT = TW * 32;
   STDIC_DEV void sync() const {
     if constexpr (TW == 1) __syncwarp();
     else asm volatile("bar.sync %0, %1;" ::"r"(id + 1), "r"(TT) : "memory");
   }
-  STDIC_DEV int any(int v, int* scratch) const {
-    if constexpr (TW == 1) return __any_sync(0xffffffffu, v);
-    const int w = tl >> 5;
+  STDIC_DEV int any(int v, int* scr) const {
     const int r = __any_sync(0xffffffffu, v);
+    if constexpr (TW == 1) return r;
     sync();
-    if ((tl & 31) == 0) scratch[w] = r;
+    if ((tl & 31) == 0) scr[tl >> 5] = r;
     sync();
     int o = 0;
 #pragma unroll
-    for (int k = 0; k < TW; ++k) o |= scratch[k];
+    for (int k = 0; k < TW; ++k) o |= scr[k];
     sync();
     return o;
   }
-  STDIC_DEV int sum_int(int v, int* scratch) const {
+  STDIC_DEV int sum_int(int v, int* scr) const {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if constexpr (TW == 1) return v;
     sync();
-    if ((tl & 31) == 0) scratch[tl >> 5] = v;
+    if ((tl & 31) == 0) scr[tl >> 5] = v;
     sync();
     int s = 0;
 #pragma unroll
-    for (int k = 0; k < TW; ++k) s += scratch[k];
+    for (int k = 0; k < TW; ++k) s += scr[k];
     sync();
     return s;
   }
+  // team sum of K FP32 values, returned to every thread as double
   template <int K>
-  STDIC_DEV void sum(double (&v)[K], double* scratch) const {
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-    if constexpr (TW == 1) return;
-    sync();
-    if ((tl & 31) == 0)
-#pragma unroll
-      for (int k = 0; k < K; ++k) scratch[k * TW + (tl >> 5)] = v[k];
-    sync();
+  STDIC_DEV void sumf(const float (&v)[K], double (&out)[K], float* scr) const {
+    float t[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      double s = 0;
+      t[k] = v[k];
 #pragma unroll
-      for (int w = 0; w < TW; ++w) s += scratch[k * TW + w];
-      v[k] = s;
+      for (int o = 16; o > 0; o >>= 1) t[k] += __shfl_xor_sync(0xffffffffu, t[k], o);
     }
-    sync();
+    if constexpr (TW == 1) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) out[k] = t[k];
+    } else {
+      sync();
+      if ((tl & 31) == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) scr[k * TW + (tl >> 5)] = t[k];
+      sync();
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        double s = 0;
+#pragma unroll
+        for (int w = 0; w < TW; ++w) s += (double)scr[k * TW + w];
+        out[k] = s;
+      }
+      sync();
+    }
   }
 };
 
@@ -82,7 +97,6 @@ struct Kahan {
     c = (t - s) - y;
     s = t;
   }
-  STDIC_DEV double value() const { return (double)s - (double)c; }
 };
 
 // flood fill of bwselect restricted to a team (see bwselect_block)
@@ -185,18 +199,14 @@ STDIC_DEV float cubic32(const float* __restrict__ g, int W, int H, int iu, float
   const float wy0 = 0.5f * (-dy + 2.f * dy2 - dy3), wy1 = 0.5f * (2.f - 5.f * dy2 + 3.f * dy3);
   const float wy2 = 0.5f * (dy + 4.f * dy2 - 3.f * dy3), wy3 = 0.5f * (-dy2 + dy3);
   const float* r = g + (long long)yb * W + xb;
-  float acc;
-  {
-    const float s0 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
-    r += W;
-    const float s1 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
-    r += W;
-    const float s2 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
-    r += W;
-    const float s3 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
-    acc = wy0 * s0 + wy1 * s1 + wy2 * s2 + wy3 * s3;
-  }
-  return acc;
+  const float s0 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
+  r += W;
+  const float s1 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
+  r += W;
+  const float s2 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
+  r += W;
+  const float s3 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
+  return wy0 * s0 + wy1 * s1 + wy2 * s2 + wy3 * s3;
 }
 
 // (i, j) of tile pixel p = i + j*mx, advanced by a fixed stride without division
@@ -211,6 +221,51 @@ struct PixIter {
   }
 };
 
+// Packed lower-triangular Cholesky of a 6x6 SPD matrix in registers.
+struct Chol6 {
+  double l[21];  // row-major packed: l[r*(r+1)/2 + c], c <= r
+  bool ok;
+};
+
+STDIC_DEV void chol6_factor(const double H[21], Chol6& C) {
+  C.ok = true;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    double d = H[j * (j + 1) / 2 + j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) d -= C.l[j * (j + 1) / 2 + k] * C.l[j * (j + 1) / 2 + k];
+    C.ok = C.ok && (d > 0);
+    const double ljj = sqrt(d > 0 ? d : 1.0);
+    C.l[j * (j + 1) / 2 + j] = ljj;
+    const double inv = 1.0 / ljj;
+#pragma unroll
+    for (int i = j + 1; i < 6; ++i) {
+      double s = H[i * (i + 1) / 2 + j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) s -= C.l[i * (i + 1) / 2 + k] * C.l[j * (j + 1) / 2 + k];
+      C.l[i * (i + 1) / 2 + j] = s * inv;
+    }
+  }
+}
+
+STDIC_DEV void chol6_solve(const Chol6& C, const double b[6], double x[6]) {
+  double y[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double s = b[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) s -= C.l[i * (i + 1) / 2 + k] * y[k];
+    y[i] = s / C.l[i * (i + 1) / 2 + i];
+  }
+#pragma unroll
+  for (int i = 5; i >= 0; --i) {
+    double s = y[i];
+#pragma unroll
+    for (int k = i + 1; k < 6; ++k) s -= C.l[k * (k + 1) / 2 + i] * x[k];
+    x[i] = s / C.l[i * (i + 1) / 2 + i];
+  }
+}
+
 struct TeamCtl {
   double P[6];
   double Hm[36];
@@ -221,8 +276,18 @@ struct TeamCtl {
 
 }  // namespace
 
-// Dynamic shared memory per team: npx_max floats (tempg) + npx_max floats
-// (tempf, 2-DOF only) + 4 npx_max bytes + reduction scratch.
+size_t batched_team_bytes(int sm_px, bool two, int tw) {
+  return ((size_t)sm_px * (two ? 8 : 4) + 4 * (size_t)sm_px + 15) / 16 * 16 + sizeof(TeamCtl) +
+         sizeof(float) * 32 * tw + 16 * tw + 64;
+}
+
+size_t batched_scratch_bytes(int npx_max, bool two, long long teams) {
+  return ((size_t)npx_max * (two ? 8 : 4) + 4 * (size_t)npx_max) * (size_t)teams + 256;
+}
+
+// Shared memory per team: smem_px floats (tempg) [+ smem_px floats (tempf,
+// 2-DOF)] + 4 smem_px bytes of bitmaps, then the control block and reduction
+// scratch.  Global scratch per team: the same layout for npx_max pixels.
 template <int TW, bool TWO>
 __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
   extern __shared__ __align__(16) unsigned char dsm[];
@@ -230,20 +295,17 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
   Team<TW> tm;
   tm.id = threadIdx.x / Team<TW>::TT;
   tm.tl = threadIdx.x % Team<TW>::TT;
-  const int npxm = a.npx_max;
-  const size_t team_bytes =
-      ((size_t)npxm * (TWO ? 8 : 4) + 4 * (size_t)npxm + 15) / 16 * 16 + sizeof(TeamCtl) +
-      sizeof(double) * 24 * TW + 16 * TW + 64;
-  unsigned char* base = dsm + team_bytes * tm.id;
-  float* tg = (float*)base;
-  float* tf = tg + npxm;  // 2-DOF only
-  uint8_t* mtile = (uint8_t*)(tg + (TWO ? 2 : 1) * npxm);
-  uint8_t* bwf = mtile + npxm;
-  uint8_t* bwg = bwf + npxm;
-  uint8_t* tmp = bwg + npxm;
-  TeamCtl* ctl = (TeamCtl*)(base + ((size_t)npxm * (TWO ? 8 : 4) + 4 * (size_t)npxm + 15) / 16 * 16);
-  double* dscr = (double*)(ctl + 1);
-  int* iscr = (int*)(dscr + 24 * TW);
+  const int teams_per_block = blockDim.x / Team<TW>::TT;
+  const long long gteam = (long long)blockIdx.x * teams_per_block + tm.id;
+  const int smpx = B.smem_px;
+  const size_t tiles_b = ((size_t)smpx * (TWO ? 8 : 4) + 4 * (size_t)smpx + 15) / 16 * 16;
+  const size_t tb = tiles_b + sizeof(TeamCtl) + sizeof(float) * 32 * TW + 16 * TW + 64;
+  unsigned char* base = dsm + tb * tm.id;
+  TeamCtl* ctl = (TeamCtl*)(base + tiles_b);
+  float* fscr = (float*)(ctl + 1);
+  int* iscr = (int*)(fscr + 32 * TW);
+  const size_t gstride = (size_t)a.npx_max * (TWO ? 8 : 4) + 4 * (size_t)a.npx_max;
+  unsigned char* gbase = B.scratch + gstride * gteam;
 
   const int Ntot = a.N * (B.frames > 0 ? B.frames : 1);
   const double tol = a.tol;
@@ -277,18 +339,18 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
     }
     const int ws0 = wx;
     long long x1 = x0 - wx / 2, x3 = x0 + wx / 2, y1 = y0 - wy / 2, y3 = y0 + wy / 2;
-    int code = 0;       // final code
+    int code = 0;
     bool nan_out = false;
-    bool hdone = false;  // Hm valid for the packed output
+    bool hdone = false;
     const int err_code = TWO ? 0 : -1;  // value the reference leaves on a run-time error
-    bool crop_valid = !((wx & 1) || (wy & 1)) && wx >= 0 && wy >= 0 && wx <= a.ws_max &&
-                      wy <= a.ws_max && mask_crop_ok32(fr, x1, x3, y1, y3);
+    const bool crop_valid = !((wx & 1) || (wy & 1)) && wx >= 0 && wy >= 0 && wx <= a.ws_max &&
+                            wy <= a.ws_max && mask_crop_ok32(fr, x1, x3, y1, y3);
     int cntf = 0, nanf = 0;
     if (crop_valid) {
-      const int mx = wx + 1, npx = (wx + 1) * (wy + 1);
-      for (int p = tm.tl; p < npx; p += tm.TT) {
-        const int i = p % mx, j = p / mx;
-        const float t = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j);
+      const int mx0 = wx + 1, np0 = (wx + 1) * (wy + 1);
+      PixIter it(tm.tl, tm.TT, mx0);
+      for (int p = tm.tl; p < np0; p += tm.TT, it.next()) {
+        const float t = fr.F(x1 + it.i, y1 + it.j) * fr.M(x1 + it.i, y1 + it.j);
         if (t != t) nanf = 1;
         if (t == 0.f) ++cntf;
       }
@@ -301,11 +363,14 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
     const double npx0 = (double)(wx + 1) * (double)(wy + 1);
     double meanf = 0, bottomf = 0, A11 = 0, A12 = 0, A22 = 0, sabs = 0;
     int mx = 0, my = 0, npx = 0, sc = 0, sr = 0;
+    float* tg = nullptr;
+    float* tf = nullptr;
+    uint8_t *mtile = nullptr, *bwf = nullptr, *bwg = nullptr, *tmp = nullptr;
+    bool has_masked = false;
     if (!crop_valid || !crop_ok32(fr, x1, x3, y1, y3) || nanf) {
       code = err_code; nan_out = true;
     } else if (!((double)cntf < 0.4 * npx0)) {
       code = kMaxIter + 2;
-      if constexpr (!TWO) { P[0] = P[1] = P[2] = P[3] = 0; }
     } else {
       if ((double)cntf > 0.0 * npx0) {
         if constexpr (TWO) {
@@ -322,48 +387,53 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
         }
         x1 = x0 - wx / 2; x3 = x0 + wx / 2; y1 = y0 - wy / 2; y3 = y0 + wy / 2;
         if (!mask_crop_ok32(fr, x1, x3, y1, y3) || !crop_ok32(fr, x1, x3, y1, y3) ||
-            (wx + 1) * (wy + 1) > npxm) {
+            (wx + 1) * (wy + 1) > a.npx_max) {
           code = err_code; nan_out = true;
         }
       }
       if (!nan_out) {
         mx = wx + 1; my = wy + 1; npx = mx * my;
         sc = (wx + 1) / 2; sr = (wy + 1) / 2;
+        // tile storage: the team's shared slot when it fits, else its global slice
+        const bool in_smem = npx <= smpx;
+        const int cap = in_smem ? smpx : a.npx_max;
+        unsigned char* st = in_smem ? base : gbase;
+        tg = (float*)st;
+        tf = tg + cap;
+        mtile = (uint8_t*)(tg + (TWO ? 2 : 1) * cap);
+        bwf = mtile + cap;
+        bwg = bwf + cap;
+        tmp = bwg + cap;
         int z = 0;
-        for (int p = tm.tl; p < npx; p += tm.TT) {
-          const int i = p % mx, j = p / mx;
-          const uint8_t mk = __ldg(fr.mask + (y1 + j - 1) * fr.W + (x1 + i - 1)) != 0;
+        PixIter it(tm.tl, tm.TT, mx);
+        for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+          const uint8_t mk = __ldg(fr.mask + (y1 + it.j - 1) * fr.W + (x1 + it.i - 1)) != 0;
           mtile[p] = mk;
           if (!mk) z = 1;
         }
-        if (tm.any(z, iscr)) bwselect_team(tm, mtile, bwf, mx, my, sr, sc, 4, iscr);
-        else {
-          for (int p = tm.tl; p < npx; p += tm.TT) bwf[p] = 1;
-          tm.sync();
-        }
+        has_masked = tm.any(z, iscr) != 0;
+        if (has_masked) bwselect_team(tm, mtile, bwf, mx, my, sr, sc, 4, iscr);
+        tm.sync();
       }
     }
 
-    const uint8_t* bw = bwf;
+    const uint8_t* bw = has_masked ? bwf : nullptr;  // nullptr: every pixel selected
     // f-side statistics: Hessian (6x6 or 2x2), meanf, bottomf, sum |tempf|
     auto f_side = [&]() {
-      double h[21];
-#pragma unroll
-      for (int k = 0; k < 21; ++k) h[k] = 0;
       float hs[21];
 #pragma unroll
       for (int k = 0; k < 21; ++k) hs[k] = 0.f;
-      Kahan sf, nf;
-      float sa = 0.f;
+      Kahan sf;
+      float nf = 0.f, sa = 0.f;
       PixIter it(tm.tl, tm.TT, mx);
       for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
         const int i = it.i, j = it.j;
-        const float s = (float)bw[p];
+        const float s = bw ? (float)bw[p] : 1.f;
         const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
         const float fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
         if constexpr (TWO) tf[p] = fv;
         sa += fabsf(fv);
-        if (fabsf(fv) > 1e-10f) { sf.add(fv); nf.add(1.f); }
+        if (fabsf(fv) > 1e-10f) { sf.add(fv); nf += 1.f; }
         if constexpr (TWO) {
           hs[0] += gx * gx; hs[1] += gx * gy; hs[2] += gy * gy;
         } else {
@@ -376,28 +446,29 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
             for (int bb = aa; bb < 6; ++bb) hs[q++] += J[aa] * J[bb];
         }
       }
-#pragma unroll
-      for (int k = 0; k < 21; ++k) h[k] = hs[k];
-      tm.template sum<21>(h, dscr);
-      double st[3] = {sf.value(), nf.value(), (double)sa};
-      tm.template sum<3>(st, dscr);
-      const double cnt = st[1];
-      const double mean = st[0] / cnt;
+      double h[21];
+      tm.template sumf<21>(hs, h, fscr);
+      const float st3[4] = {sf.s, -sf.c, nf, sa};
+      double st[4];
+      tm.template sumf<4>(st3, st, fscr);
+      const double cnt = st[2];
+      const double mean = (st[0] + st[1]) / cnt;
       Kahan q;
+      const float meanf32 = (float)mean;
       PixIter it2(tm.tl, tm.TT, mx);
       for (int p = tm.tl; p < npx; p += tm.TT, it2.next()) {
-        const int i = it2.i, j = it2.j;
         float fv;
         if constexpr (TWO) fv = tf[p];
-        else fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * (float)bw[p];
-        if (fabsf(fv) > 1e-10f) { const float d = fv - (float)mean; q.add(d * d); }
+        else fv = fr.F(x1 + it2.i, y1 + it2.j) * fr.M(x1 + it2.i, y1 + it2.j) * (bw ? (float)bw[p] : 1.f);
+        if (fabsf(fv) > 1e-10f) { const float d = fv - meanf32; q.add(d * d); }
       }
-      double qq[1] = {q.value()};
-      tm.template sum<1>(qq, dscr);
-      const double var = cnt == 0 ? nan("") : (cnt == 1 ? 0.0 : qq[0] / (cnt - 1));
+      const float qq3[2] = {q.s, -q.c};
+      double qq[2];
+      tm.template sumf<2>(qq3, qq, fscr);
+      const double var = cnt == 0 ? nan("") : (cnt == 1 ? 0.0 : (qq[0] + qq[1]) / (cnt - 1));
       meanf = mean;
       bottomf = sqrt((cnt - 1) * var);
-      sabs = st[2];
+      sabs = st[3];
       if constexpr (TWO) {
         const double b2 = bottomf * bottomf;
         A11 = h[0] * 2 / b2 + a.mu;
@@ -411,8 +482,23 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
       tm.sync();
     };
 
-    bool run = (code == 0 && !nan_out);
-    if (run) { f_side(); hdone = true; }
+    const bool run = (code == 0 && !nan_out);
+    Chol6 ch;
+    ch.ok = false;
+    if (run) {
+      f_side();
+      hdone = true;
+      if constexpr (!TWO) {
+        if (tm.tl == 0) {
+          double Hp[21];
+#pragma unroll
+          for (int r = 0; r < 6; ++r)
+#pragma unroll
+            for (int c2 = 0; c2 <= r; ++c2) Hp[r * (r + 1) / 2 + c2] = ctl->Hm[r * 6 + c2];
+          chol6_factor(Hp, ch);
+        }
+      }
+    }
     double normNew = 1, normAbs = 1, normInit = 0;
     int step = 0, cg = 0;
     bool err = false;
@@ -439,17 +525,27 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
       const float fu = (float)(bu - iu), fv0 = (float)(bv - iv);
       const float p0 = (float)(1 + P[0]), p1 = (float)P[1], p2 = (float)P[2], p3 = (float)(1 + P[3]);
       const float dx0 = (float)(x1 - x0), dy0 = (float)(y1 - y0);
+      const float shift = (float)meanf;  // one-pass variance around meanf
       int zg = 0, nang = 0;
-      PixIter it(tm.tl, tm.TT, mx);
-      for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
-        const int i = it.i, j = it.j;
-        const float dx = dx0 + (float)i, dy = dy0 + (float)j;
-        const float su = fu + p0 * dx + p2 * dy;
-        const float sv = fv0 + p1 * dx + p3 * dy;
-        const float t = cubic32(fr.g, fr.W, fr.H, iu, su, iv, sv);
-        tg[p] = t;
-        if (t != t) nang = 1;
-        if (t == 0.f) ++zg;
+      Kahan sg, qg;
+      float ng = 0.f;
+      {
+        PixIter it(tm.tl, tm.TT, mx);
+        for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+          const float dx = dx0 + (float)it.i, dy = dy0 + (float)it.j;
+          const float su = fu + p0 * dx + p2 * dy;
+          const float sv = fv0 + p1 * dx + p3 * dy;
+          const float t = cubic32(fr.g, fr.W, fr.H, iu, su, iv, sv);
+          tg[p] = t;
+          if (t != t) nang = 1;
+          if (t == 0.f) ++zg;
+          if (fabsf(t) > 1e-10f) {
+            const float d = t - shift;
+            sg.add(d);
+            qg.add(d * d);
+            ng += 1.f;
+          }
+        }
       }
       zg = tm.sum_int(zg, iscr);
       if (tm.any(nang, iscr)) { err = true; break; }
@@ -461,9 +557,17 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
         for (int p = tm.tl; p < npx; p += tm.TT) anyzero |= !bwg[p];
         if (!tm.any(anyzero, iscr)) bwselect_team(tm, mtile, bwg, mx, my, sr, sc, 8, iscr);
         int cnt = 0;
+        sg = Kahan(); qg = Kahan(); ng = 0.f;
         for (int p = tm.tl; p < npx; p += tm.TT) {
-          tg[p] *= (float)bwg[p];
+          const float t = tg[p] * (float)bwg[p];
+          tg[p] = t;
           cnt += bwg[p];
+          if (fabsf(t) > 1e-10f) {
+            const float d = t - shift;
+            sg.add(d);
+            qg.add(d * d);
+            ng += 1.f;
+          }
         }
         cg = tm.sum_int(cnt, iscr);
         if constexpr (TWO) {
@@ -471,24 +575,14 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
           f_side();
         }
       }
-      // g statistics
-      Kahan sg, ng;
-      for (int p = tm.tl; p < npx; p += tm.TT) {
-        const float t = tg[p];
-        if (fabsf(t) > 1e-10f) { sg.add(t); ng.add(1.f); }
-      }
-      double st[2] = {sg.value(), ng.value()};
-      tm.template sum<2>(st, dscr);
-      const double meang = st[0] / st[1];
-      Kahan qg;
-      for (int p = tm.tl; p < npx; p += tm.TT) {
-        const float t = tg[p];
-        if (fabsf(t) > 1e-10f) { const float d = t - (float)meang; qg.add(d * d); }
-      }
-      double qq[1] = {qg.value()};
-      tm.template sum<1>(qq, dscr);
-      const double cntg = st[1];
-      const double varg = cntg == 0 ? nan("") : (cntg == 1 ? 0.0 : qq[0] / (cntg - 1));
+      // g statistics: mean and sqrt((n-1) var) from the shifted one-pass sums
+      const float gs[5] = {sg.s, -sg.c, qg.s, -qg.c, ng};
+      double gt[5];
+      tm.template sumf<5>(gs, gt, fscr);
+      const double cntg = gt[4];
+      const double s1 = gt[0] + gt[1], s2 = gt[2] + gt[3];
+      const double meang = (double)shift + s1 / cntg;
+      const double varg = cntg == 0 ? nan("") : (cntg == 1 ? 0.0 : fmax(s2 - s1 * s1 / cntg, 0.0) / (cntg - 1));
       const double bottomg = sqrt((cntg - 1) * varg);
       const float mf = (float)meanf, ibf = (float)(1.0 / bottomf);
       const float mg = (float)meang, ibg = (float)(1.0 / bottomg);
@@ -497,23 +591,23 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
         Kahan k0, k1;
         PixIter it3(tm.tl, tm.TT, mx);
         for (int p = tm.tl; p < npx; p += tm.TT, it3.next()) {
-          const int i = it3.i, j = it3.j;
-          const float s = (float)bw[p];
-          const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
+          const float s = bw ? (float)bw[p] : 1.f;
+          const float gx = fr.GX(x1 + it3.i, y1 + it3.j) * s, gy = fr.GY(x1 + it3.i, y1 + it3.j) * s;
           const float r = (tf[p] - mf) * ibf - (tg[p] - mg) * ibg;
           k0.add(gx * r);
           k1.add(gy * r);
         }
-        b2[0] = k0.value(); b2[1] = k1.value();
-        double t2[2] = {b2[0], b2[1]};
-        tm.template sum<2>(t2, dscr);
-        b2[0] = t2[0]; b2[1] = t2[1];
+        const float kk[4] = {k0.s, -k0.c, k1.s, -k1.c};
+        double t4[4];
+        tm.template sumf<4>(kk, t4, fscr);
+        b2[0] = t4[0] + t4[1];
+        b2[1] = t4[2] + t4[3];
       } else {
         Kahan k[6];
         PixIter it3(tm.tl, tm.TT, mx);
         for (int p = tm.tl; p < npx; p += tm.TT, it3.next()) {
           const int i = it3.i, j = it3.j;
-          const float s = (float)bw[p];
+          const float s = bw ? (float)bw[p] : 1.f;
           const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
           const float fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
           const float dx = dx0 + (float)i, dy = dy0 + (float)j;
@@ -522,9 +616,12 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
           k[0].add(dx * gxr); k[1].add(dx * gyr); k[2].add(dy * gxr); k[3].add(dy * gyr);
           k[4].add(gxr); k[5].add(gyr);
         }
+        const float kk[12] = {k[0].s, -k[0].c, k[1].s, -k[1].c, k[2].s, -k[2].c,
+                              k[3].s, -k[3].c, k[4].s, -k[4].c, k[5].s, -k[5].c};
+        double t12[12];
+        tm.template sumf<12>(kk, t12, fscr);
 #pragma unroll
-        for (int q = 0; q < 6; ++q) b2[q] = k[q].value();
-        tm.template sum<6>(b2, dscr);
+        for (int q = 0; q < 6; ++q) b2[q] = t12[2 * q] + t12[2 * q + 1];
       }
       if (tm.tl == 0) {
         int done = 0;
@@ -536,10 +633,8 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
           const double tb0 = b0 * 2 / (bottomf * bottomf) + a.mu * (P[4] - a.UOld[2 * item] - a.vdual[2 * item]);
           const double tb1 = b1 * 2 / (bottomf * bottomf) + a.mu * (P[5] - a.UOld[2 * item + 1] - a.vdual[2 * item + 1]);
           const double dmax = isnan(A11) ? A22 : (isnan(A22) ? A11 : fmax(A11, A22));
-          const double Hm[4] = {A11 + 1e-3 * dmax, A12, A12, A22 + 1e-3 * dmax};
-          const double rhs[2] = {tb0, tb1};
           double dP[2];
-          small_solve(Hm, rhs, 2, dP);
+          solve2(A11 + 1e-3 * dmax, A12, A22 + 1e-3 * dmax, tb0, tb1, &dP[0], &dP[1]);
           nN = sqrt(tb0 * tb0 + tb1 * tb1);
           nA = nN;
           const double nI = step == 1 ? nN : normInit;
@@ -561,7 +656,8 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
           if (nN < tol || nA < tol) done = 1;
           else {
             double D[6];
-            small_solve(ctl->Hm, b, 6, D);
+            if (ch.ok) chol6_solve(ch, b, D);
+            else small_solve(ctl->Hm, b, 6, D);
             for (int k = 0; k < 6; ++k) D[k] = -D[k];
             if (!compose_update(Pn, D)) done = 2;
           }
@@ -587,10 +683,12 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
         if (!(normNew < tol || normAbs < tol)) code = kMaxIter + 1;
         if (isnan(normNew)) code = kMaxIter + 1;
         if constexpr (TWO) {
-          double v[1] = {0};
-          for (int p = tm.tl; p < npx; p += tm.TT) v[0] += fabsf(tf[p]);
-          tm.template sum<1>(v, dscr);
-          sabs = v[0];
+          float v = 0.f;
+          for (int p = tm.tl; p < npx; p += tm.TT) v += fabsf(tf[p]);
+          const float vv[1] = {v};
+          double sv[1];
+          tm.template sumf<1>(vv, sv, fscr);
+          sabs = sv[0];
         }
         if (sabs < 1e-6) code = kMaxIter + 3;
       }
@@ -614,15 +712,10 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
   }
 }
 
-size_t batched_team_bytes(int npx_max, bool two, int tw) {
-  return ((size_t)npx_max * (two ? 8 : 4) + 4 * (size_t)npx_max + 15) / 16 * 16 + sizeof(TeamCtl) +
-         sizeof(double) * 24 * tw + 16 * tw + 64;
-}
-
 template <int TW, bool TWO>
 static cudaError_t launch_tw(const BatchedArgs& b, int blocks, int threads, cudaStream_t s) {
   const int teams = threads / (TW * 32);
-  const size_t smem = batched_team_bytes(b.a.npx_max, TWO, TW) * teams;
+  const size_t smem = batched_team_bytes(b.smem_px, TWO, TW) * teams;
   if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
   cudaError_t e = cudaFuncSetAttribute(icgn_batched_kernel<TW, TWO>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -637,15 +730,15 @@ cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, c
     case 1: return two ? launch_tw<1, true>(b, blocks, threads, s) : launch_tw<1, false>(b, blocks, threads, s);
     case 2: return two ? launch_tw<2, true>(b, blocks, threads, s) : launch_tw<2, false>(b, blocks, threads, s);
     case 4: return two ? launch_tw<4, true>(b, blocks, threads, s) : launch_tw<4, false>(b, blocks, threads, s);
-    case 8: return two ? launch_tw<8, true>(b, blocks, threads, s) : launch_tw<8, false>(b, blocks, threads, s);
   }
   return cudaErrorInvalidValue;
 }
 
-// Occupancy of one configuration (blocks per SM), for the autotuner.
-int batched_blocks_per_sm(int tw, bool two, int threads, int npx_max) {
+// Resident blocks per SM of one configuration (for grid sizing and the autotuner).
+int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px) {
   const int teams = threads / (tw * 32);
-  const size_t smem = batched_team_bytes(npx_max, two, tw) * teams;
+  const size_t smem = batched_team_bytes(smem_px, two, tw) * teams;
+  if (smem > 227 * 1024) return 0;
   int nb = 0;
   cudaError_t e = cudaSuccess;
 #define STDIC_OCC(TWv, TWOv)                                                                 \
@@ -658,11 +751,9 @@ int batched_blocks_per_sm(int tw, bool two, int threads, int npx_max) {
     case 1: if (two) { STDIC_OCC(1, true) } else { STDIC_OCC(1, false) } break;
     case 2: if (two) { STDIC_OCC(2, true) } else { STDIC_OCC(2, false) } break;
     case 4: if (two) { STDIC_OCC(4, true) } else { STDIC_OCC(4, false) } break;
-    case 8: if (two) { STDIC_OCC(8, true) } else { STDIC_OCC(8, false) } break;
     default: return 0;
   }
 #undef STDIC_OCC
-  if (smem > 227 * 1024) return 0;
   return e == cudaSuccess ? nb : 0;
 }
 

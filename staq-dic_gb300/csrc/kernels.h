@@ -56,9 +56,15 @@ struct BatchedArgs {
   int warps_per_subset;
   int two_dof;
   int frames;             // number of frame pairs stacked in g32 (multi-frame)
-  const int32_t* frame_of_node;  // optional
   long long g_stride;     // elements between stacked deformed frames
+  unsigned char* scratch; // per-team global slices for tiles that exceed the shared slot
+  int smem_px;            // tile pixels each team keeps in shared memory
 };
+
+// Size of one team's shared slot / global slice of the batched kernel.
+size_t batched_team_bytes(int sm_px, bool two, int tw);
+size_t batched_scratch_bytes(int npx_max, bool two, long long teams);
+int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px);
 
 cudaError_t launch_interp(const void* F, long long M, long long N, long long P, const void* X,
                           const void* Y, long long n, void* out, int dtype, cudaStream_t s);

@@ -28,7 +28,7 @@ STDIC_BATCHED_F32 = 1
 
 EXPORTS = [
     "stdic_ctx_create", "stdic_ctx_destroy", "stdic_ctx_set_stream", "stdic_last_error",
-    "stdic_kernel_launches", "stdic_interp_bicubic", "stdic_img_gradient",
+    "stdic_kernel_launches", "stdic_last_solver_ms", "stdic_interp_bicubic", "stdic_img_gradient",
     "stdic_integer_search_grid", "stdic_integer_search", "stdic_icgn_subsets", "stdic_icgn_local",
     "stdic_subpb1_subsets", "stdic_subpb1", "stdic_subpb2",
 ]
@@ -70,6 +70,8 @@ def load(build_if_missing=True):
     L.stdic_last_error.restype = _c.c_char_p
     L.stdic_kernel_launches.argtypes = [_vp]
     L.stdic_kernel_launches.restype = _c.c_longlong
+    L.stdic_last_solver_ms.argtypes = [_vp]
+    L.stdic_last_solver_ms.restype = _c.c_double
     L.stdic_interp_bicubic.argtypes = [_vp, _vp, _c.c_int64, _c.c_int64, _c.c_int64, _vp, _vp,
                                        _c.c_int64, _vp, _c.c_int]
     L.stdic_img_gradient.argtypes = [_vp, _vp, _vp, _c.c_int, _c.c_int, _vp, _vp, _c.c_int]
@@ -89,7 +91,7 @@ def load(build_if_missing=True):
                                _c.c_int, _c.c_double, _c.c_double, _vp, _vp, _c.c_double,
                                _c.c_double, _c.c_double, _c.c_int, _vp, _vp]
     for name in EXPORTS:
-        if name not in ("stdic_last_error", "stdic_kernel_launches"):
+        if name not in ("stdic_last_error", "stdic_kernel_launches", "stdic_last_solver_ms"):
             getattr(L, name).restype = _c.c_int
     _lib = L
     return L
@@ -114,6 +116,10 @@ class Context:
 
     def set_stream(self, stream_ptr):
         self.check(self.L.stdic_ctx_set_stream(self.h, _vp(stream_ptr or 0)), "set_stream")
+
+    def last_solver_ms(self):
+        """Device time (ms) of the last IC-GN solver kernel (CUDA events)."""
+        return float(self.L.stdic_last_solver_ms(self.h))
 
     @property
     def launches(self):

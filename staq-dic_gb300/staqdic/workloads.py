@@ -82,9 +82,9 @@ def _hole_case(name, seed, W, a, eps, scale_sizes=1.0):
         d = abs(math.hypot(x - centre[0], y - centre[1]) - a)
         if d < 40 * s:
             return 4.0
-        if d < 0.35 * W:
+        if d < 0.3 * W:
             return 8.0
-        if d < 0.5 * W:
+        if d < 0.4 * W:
             return 16.0
         return 32.0
 

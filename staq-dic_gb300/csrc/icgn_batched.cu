@@ -58,36 +58,91 @@ struct Team {
     sync();
     return s;
   }
-  // team sum of K FP32 values, returned to every thread as double
+  // in-place team sum of K FP32 values (every thread receives the totals)
   template <int K>
-  STDIC_DEV void sumf(const float (&v)[K], double (&out)[K], float* scr) const {
-    float t[K];
+  STDIC_DEV void sumf(float (&v)[K], float* scr) const {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      t[k] = v[k];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t[k] += __shfl_xor_sync(0xffffffffu, t[k], o);
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
     }
-    if constexpr (TW == 1) {
-#pragma unroll
-      for (int k = 0; k < K; ++k) out[k] = t[k];
-    } else {
+    if constexpr (TW > 1) {
       sync();
       if ((tl & 31) == 0)
 #pragma unroll
-        for (int k = 0; k < K; ++k) scr[k * TW + (tl >> 5)] = t[k];
+        for (int k = 0; k < K; ++k) scr[k * TW + (tl >> 5)] = v[k];
       sync();
 #pragma unroll
       for (int k = 0; k < K; ++k) {
-        double s = 0;
+        float s = 0.f;
 #pragma unroll
-        for (int w = 0; w < TW; ++w) s += (double)scr[k * TW + w];
-        out[k] = s;
+        for (int w = 0; w < TW; ++w) s += scr[k * TW + w];
+        v[k] = s;
       }
       sync();
     }
   }
 };
+
+// Warp-parallel FP64 Gauss-Newton update.  Lane k < 6 holds row k of H^-1
+// (6x6 form) and produces DeltaP_k; the inverse-compositional update of P and
+// the image-bounds test of the next warp are also split over lanes, so the
+// narrow FP64 pipe sees a few dozen instructions per iteration.
+STDIC_DEV double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+// P <- P o DeltaP^-1 (funICGNQuadtree.m:393-411) with D known on every lane.
+// Returns false (P unchanged) when det(DeltaP) == 0.
+STDIC_DEV bool compose_warp(double P[6], const double D[6], int lane) {
+  const double det = (1 + D[0]) * (1 + D[3]) - D[1] * D[2];
+  if (!(det != 0)) return false;
+  const double inv = 1.0 / det;
+  // lane k < 6 forms tempP_(k+1)
+  double t = 0;
+  switch (lane) {
+    case 0: t = (-D[0] - D[0] * D[3] + D[1] * D[2]) * inv; break;
+    case 1: t = -D[1] * inv; break;
+    case 2: t = -D[2] * inv; break;
+    case 3: t = (-D[3] - D[0] * D[3] + D[1] * D[2]) * inv; break;
+    case 4: t = (-D[4] - D[3] * D[4] + D[2] * D[5]) * inv; break;
+    case 5: t = (-D[5] - D[0] * D[5] + D[1] * D[4]) * inv; break;
+  }
+  double T[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) T[k] = shfl_d(t, k);
+  // lane k < 6 forms the new P_(k+1)
+  double pn = 0;
+  switch (lane) {
+    case 0: pn = (1 + P[0]) * (1 + T[0]) + P[2] * T[1] - 1; break;
+    case 1: pn = P[1] * (1 + T[0]) + (1 + P[3]) * T[1]; break;
+    case 2: pn = (1 + P[0]) * T[2] + P[2] * (1 + T[3]); break;
+    case 3: pn = P[1] * T[2] + (1 + P[3]) * (1 + T[3]) - 1; break;
+    case 4: pn = (1 + P[0]) * T[4] + P[2] * T[5] + P[4]; break;
+    case 5: pn = P[1] * T[4] + (1 + P[3]) * T[5] + P[5]; break;
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) P[k] = shfl_d(pn, k);
+  return true;
+}
+
+// Bounds test of the warp P over the tile [x1, x1+mx-1] x [y1, y1+my-1]: lanes
+// 0..7 evaluate one coordinate of one corner each (the warp is affine).
+STDIC_DEV bool corners_oob_warp(const double P[6], long long x0, long long y0, long long x1,
+                                long long y1, int mx, int my, int W, int H, int lane) {
+  bool bad = false;
+  if (lane < 8) {
+    const int cn = lane >> 1;
+    const double dx = (double)((cn & 1 ? x1 + mx - 1 : x1) - x0);
+    const double dy = (double)((cn & 2 ? y1 + my - 1 : y1) - y0);
+    if ((lane & 1) == 0) {
+      const double u22 = (1 + P[0]) * dx + P[2] * dy + ((double)x0 + P[4]);
+      bad = u22 < 3 || u22 > (double)W - 2;
+    } else {
+      const double v22 = P[1] * dx + (1 + P[3]) * dy + ((double)y0 + P[5]);
+      bad = v22 < 3 || v22 > (double)H - 2;
+    }
+  }
+  return __any_sync(0xffffffffu, bad);
+}
 
 struct Kahan {
   float s = 0.f, c = 0.f;
@@ -288,13 +343,18 @@ size_t batched_scratch_bytes(int npx_max, bool two, long long teams) {
 // Shared memory per team: smem_px floats (tempg) [+ smem_px floats (tempf,
 // 2-DOF)] + 4 smem_px bytes of bitmaps, then the control block and reduction
 // scratch.  Global scratch per team: the same layout for npx_max pixels.
+//
+// Every warp of a team holds the team totals after each reduction and runs the
+// same FP64 update on them, so all warps carry bit-identical P without a
+// shared-memory broadcast.
 template <int TW, bool TWO>
-__global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
+__global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
   extern __shared__ __align__(16) unsigned char dsm[];
   const IcgnArgs& a = B.a;
   Team<TW> tm;
   tm.id = threadIdx.x / Team<TW>::TT;
   tm.tl = threadIdx.x % Team<TW>::TT;
+  const int lane = threadIdx.x & 31;
   const int teams_per_block = blockDim.x / Team<TW>::TT;
   const long long gteam = (long long)blockIdx.x * teams_per_block + tm.id;
   const int smpx = B.smem_px;
@@ -308,7 +368,7 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
   unsigned char* gbase = B.scratch + gstride * gteam;
 
   const int Ntot = a.N * (B.frames > 0 ? B.frames : 1);
-  const double tol = a.tol;
+  const float tolf = (float)a.tol;
   for (;;) {
     if (tm.tl == 0) {
       // frames interleaved so that every frame's largest subsets start first
@@ -330,6 +390,7 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
     double P[6];
     if constexpr (TWO) {
       wx = a.wsl2[node]; wy = a.wsl2[a.N + node];
+#pragma unroll
       for (int k = 0; k < 4; ++k) P[k] = a.FOld[4 * item + k];
       P[4] = a.UOld[2 * item]; P[5] = a.UOld[2 * item + 1];
     } else {
@@ -361,7 +422,8 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
       if (a.mark && tm.tl == 0) a.mark[item] = (!crop_valid || cntf > 0) ? 1 : 0;
     }
     const double npx0 = (double)(wx + 1) * (double)(wy + 1);
-    double meanf = 0, bottomf = 0, A11 = 0, A12 = 0, A22 = 0, sabs = 0;
+    float meanf = 0.f, bottomf = 0.f, sabs = 0.f;
+    double A11 = 0, A12 = 0, A22 = 0;
     int mx = 0, my = 0, npx = 0, sc = 0, sr = 0;
     float* tg = nullptr;
     float* tf = nullptr;
@@ -418,6 +480,9 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
     }
 
     const uint8_t* bw = has_masked ? bwf : nullptr;  // nullptr: every pixel selected
+    double hinv[6];  // lane k < 6: row k of the inverse Hessian (6-DOF)
+    bool hok = false;
+    double i00 = 0, i01 = 0, i10 = 0, i11 = 0;  // inverse of the 2x2 system (2-DOF)
     // f-side statistics: Hessian (6x6 or 2x2), meanf, bottomf, sum |tempf|
     auto f_side = [&]() {
       float hs[21];
@@ -437,7 +502,7 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
         if constexpr (TWO) {
           hs[0] += gx * gx; hs[1] += gx * gy; hs[2] += gy * gy;
         } else {
-          const float dx = (float)(x1 + i - x0), dy = (float)(y1 + j - y0);
+          const float dx = (float)(int)(x1 + i - x0), dy = (float)(int)(y1 + j - y0);
           const float J[6] = {dx * gx, dx * gy, dy * gx, dy * gy, gx, gy};
           int q = 0;
 #pragma unroll
@@ -446,63 +511,80 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
             for (int bb = aa; bb < 6; ++bb) hs[q++] += J[aa] * J[bb];
         }
       }
-      double h[21];
-      tm.template sumf<21>(hs, h, fscr);
-      const float st3[4] = {sf.s, -sf.c, nf, sa};
-      double st[4];
-      tm.template sumf<4>(st3, st, fscr);
-      const double cnt = st[2];
-      const double mean = (st[0] + st[1]) / cnt;
+      float st4[4] = {sf.s, -sf.c, nf, sa};
+      tm.template sumf<4>(st4, fscr);
+      const float cnt = st4[2];
+      const float mean = (st4[0] + st4[1]) / cnt;
       Kahan q;
-      const float meanf32 = (float)mean;
       PixIter it2(tm.tl, tm.TT, mx);
       for (int p = tm.tl; p < npx; p += tm.TT, it2.next()) {
         float fv;
         if constexpr (TWO) fv = tf[p];
         else fv = fr.F(x1 + it2.i, y1 + it2.j) * fr.M(x1 + it2.i, y1 + it2.j) * (bw ? (float)bw[p] : 1.f);
-        if (fabsf(fv) > 1e-10f) { const float d = fv - meanf32; q.add(d * d); }
+        if (fabsf(fv) > 1e-10f) { const float d = fv - mean; q.add(d * d); }
       }
-      const float qq3[2] = {q.s, -q.c};
-      double qq[2];
-      tm.template sumf<2>(qq3, qq, fscr);
-      const double var = cnt == 0 ? nan("") : (cnt == 1 ? 0.0 : (qq[0] + qq[1]) / (cnt - 1));
+      float qq[2] = {q.s, -q.c};
+      tm.template sumf<2>(qq, fscr);
+      const float var = cnt == 0.f ? __int_as_float(0x7fc00000) : (cnt == 1.f ? 0.f : (qq[0] + qq[1]) / (cnt - 1.f));
       meanf = mean;
-      bottomf = sqrt((cnt - 1) * var);
-      sabs = st[3];
+      bottomf = sqrtf((cnt - 1.f) * var);
+      sabs = st4[3];
       if constexpr (TWO) {
-        const double b2 = bottomf * bottomf;
-        A11 = h[0] * 2 / b2 + a.mu;
-        A12 = h[1] * 2 / b2;
-        A22 = h[2] * 2 / b2 + a.mu;
-      } else if (tm.tl == 0) {
-        int q2 = 0;
-        for (int aa = 0; aa < 6; ++aa)
-          for (int bb = aa; bb < 6; ++bb) { ctl->Hm[aa * 6 + bb] = h[q2]; ctl->Hm[bb * 6 + aa] = h[q2]; ++q2; }
+        tm.template sumf<3>(*reinterpret_cast<float(*)[3]>(hs), fscr);
+        const double b2 = (double)bottomf * (double)bottomf;
+        A11 = (double)hs[0] * 2 / b2 + a.mu;
+        A12 = (double)hs[1] * 2 / b2;
+        A22 = (double)hs[2] * 2 / b2 + a.mu;
+        // H2 + 1e-3 max(diag H2) I of funICGN_Subpb1.m:391-394, inverted once per change
+        const double dmax = isnan(A11) ? A22 : (isnan(A22) ? A11 : fmax(A11, A22));
+        solve2(A11 + 1e-3 * dmax, A12, A22 + 1e-3 * dmax, 1.0, 0.0, &i00, &i10);
+        solve2(A11 + 1e-3 * dmax, A12, A22 + 1e-3 * dmax, 0.0, 1.0, &i01, &i11);
+      } else {
+        tm.template sumf<21>(hs, fscr);
+        // Cholesky of H (every lane, FP64), then lane k < 6 solves for column k
+        // of H^-1 (= row k by symmetry)
+        double Hp[21];
+#pragma unroll
+        for (int k = 0; k < 21; ++k) Hp[k] = 0;
+        {
+          int q2 = 0;
+#pragma unroll
+          for (int aa = 0; aa < 6; ++aa)
+#pragma unroll
+            for (int bb = aa; bb < 6; ++bb) {
+              // hs is (row aa, col bb >= aa); packed lower storage wants (bb, aa)
+              Hp[bb * (bb + 1) / 2 + aa] = (double)hs[q2];
+              ++q2;
+            }
+        }
+        if (tm.tl == 0) {
+          int q3 = 0;
+          for (int aa = 0; aa < 6; ++aa)
+            for (int bb = aa; bb < 6; ++bb) {
+              ctl->Hm[aa * 6 + bb] = (double)hs[q3]; ctl->Hm[bb * 6 + aa] = (double)hs[q3]; ++q3;
+            }
+        }
+        Chol6 ch;
+        chol6_factor(Hp, ch);
+        hok = ch.ok;
+        double e[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) e[k] = (lane == k) ? 1.0 : 0.0;
+        chol6_solve(ch, e, hinv);
       }
       tm.sync();
     };
 
     const bool run = (code == 0 && !nan_out);
-    Chol6 ch;
-    ch.ok = false;
     if (run) {
       f_side();
       hdone = true;
-      if constexpr (!TWO) {
-        if (tm.tl == 0) {
-          double Hp[21];
-#pragma unroll
-          for (int r = 0; r < 6; ++r)
-#pragma unroll
-            for (int c2 = 0; c2 <= r; ++c2) Hp[r * (r + 1) / 2 + c2] = ctl->Hm[r * 6 + c2];
-          chol6_factor(Hp, ch);
-        }
-      }
     }
-    double normNew = 1, normAbs = 1, normInit = 0;
+    float normNew = 1.f, normAbs = 1.f, normInit = 0.f;
     int step = 0, cg = 0;
     bool err = false;
-    while (run && step <= kMaxIter && normNew > tol && normAbs > tol) {
+    bool oob = run ? corners_oob_warp(P, x0, y0, x1, y1, mx, my, a.W, a.H, lane) : false;
+    while (run && step <= kMaxIter && normNew > tolf && normAbs > tolf) {
       ++step;
       if constexpr (!TWO) {
         if (step > 1 && (double)cntf > 0.0 * npx0) {
@@ -512,20 +594,20 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
           if (nws != wx) {
             const long long nx1 = x0 - nws / 2, nx3 = x0 + nws / 2, ny1 = y0 - nws / 2, ny3 = y0 + nws / 2;
             if (!mask_crop_ok32(fr, nx1, nx3, ny1, ny3)) { err = true; break; }
-            if (corners_oob(fr, P, x0, y0, nx1, ny1, nws + 1, nws + 1)) { normNew = 1e6; break; }
+            if (corners_oob_warp(P, x0, y0, nx1, ny1, nws + 1, nws + 1, a.W, a.H, lane)) { normNew = 1e6f; break; }
             err = true;
             break;
           }
         }
       }
-      if (corners_oob(fr, P, x0, y0, x1, y1, mx, my)) { normNew = 1e6; break; }
+      if (oob) { normNew = 1e6f; break; }
       // integer base + FP32 offsets of the warp
       const double bu = (double)x0 + P[4], bv = (double)y0 + P[5];
       const int iu = (int)floor(bu), iv = (int)floor(bv);
       const float fu = (float)(bu - iu), fv0 = (float)(bv - iv);
       const float p0 = (float)(1 + P[0]), p1 = (float)P[1], p2 = (float)P[2], p3 = (float)(1 + P[3]);
-      const float dx0 = (float)(x1 - x0), dy0 = (float)(y1 - y0);
-      const float shift = (float)meanf;  // one-pass variance around meanf
+      const float dx0 = (float)(int)(x1 - x0), dy0 = (float)(int)(y1 - y0);
+      const float shift = meanf;  // one-pass variance around meanf
       int zg = 0, nang = 0;
       Kahan sg, qg;
       float ng = 0.f;
@@ -576,17 +658,17 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
         }
       }
       // g statistics: mean and sqrt((n-1) var) from the shifted one-pass sums
-      const float gs[5] = {sg.s, -sg.c, qg.s, -qg.c, ng};
-      double gt[5];
-      tm.template sumf<5>(gs, gt, fscr);
-      const double cntg = gt[4];
-      const double s1 = gt[0] + gt[1], s2 = gt[2] + gt[3];
-      const double meang = (double)shift + s1 / cntg;
-      const double varg = cntg == 0 ? nan("") : (cntg == 1 ? 0.0 : fmax(s2 - s1 * s1 / cntg, 0.0) / (cntg - 1));
-      const double bottomg = sqrt((cntg - 1) * varg);
-      const float mf = (float)meanf, ibf = (float)(1.0 / bottomf);
-      const float mg = (float)meang, ibg = (float)(1.0 / bottomg);
-      double b2[6];
+      float gs[5] = {sg.s, -sg.c, qg.s, -qg.c, ng};
+      tm.template sumf<5>(gs, fscr);
+      const float cntg = gs[4];
+      const float s1 = gs[0] + gs[1], s2 = gs[2] + gs[3];
+      const float meang = shift + s1 / cntg;
+      const float varg = cntg == 0.f ? __int_as_float(0x7fc00000)
+                                     : (cntg == 1.f ? 0.f : fmaxf(s2 - s1 * s1 / cntg, 0.f) / (cntg - 1.f));
+      const float bottomg = sqrtf((cntg - 1.f) * varg);
+      const float mf = meanf, ibf = 1.f / bottomf;
+      const float mg = meang, ibg = 1.f / bottomg;
+      float bsum[TWO ? 4 : 12];
       if constexpr (TWO) {
         Kahan k0, k1;
         PixIter it3(tm.tl, tm.TT, mx);
@@ -597,11 +679,8 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
           k0.add(gx * r);
           k1.add(gy * r);
         }
-        const float kk[4] = {k0.s, -k0.c, k1.s, -k1.c};
-        double t4[4];
-        tm.template sumf<4>(kk, t4, fscr);
-        b2[0] = t4[0] + t4[1];
-        b2[1] = t4[2] + t4[3];
+        bsum[0] = k0.s; bsum[1] = -k0.c; bsum[2] = k1.s; bsum[3] = -k1.c;
+        tm.template sumf<4>(bsum, fscr);
       } else {
         Kahan k[6];
         PixIter it3(tm.tl, tm.TT, mx);
@@ -616,81 +695,65 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
           k[0].add(dx * gxr); k[1].add(dx * gyr); k[2].add(dy * gxr); k[3].add(dy * gyr);
           k[4].add(gxr); k[5].add(gyr);
         }
-        const float kk[12] = {k[0].s, -k[0].c, k[1].s, -k[1].c, k[2].s, -k[2].c,
-                              k[3].s, -k[3].c, k[4].s, -k[4].c, k[5].s, -k[5].c};
-        double t12[12];
-        tm.template sumf<12>(kk, t12, fscr);
 #pragma unroll
-        for (int q = 0; q < 6; ++q) b2[q] = t12[2 * q] + t12[2 * q + 1];
+        for (int q = 0; q < 6; ++q) { bsum[2 * q] = k[q].s; bsum[2 * q + 1] = -k[q].c; }
+        tm.template sumf<12>(bsum, fscr);
       }
-      if (tm.tl == 0) {
-        int done = 0;
-        double Pn[6];
-        for (int k = 0; k < 6; ++k) Pn[k] = P[k];
-        double nN, nA;
-        if constexpr (TWO) {
-          const double b0 = bottomf * b2[0], b1 = bottomf * b2[1];
-          const double tb0 = b0 * 2 / (bottomf * bottomf) + a.mu * (P[4] - a.UOld[2 * item] - a.vdual[2 * item]);
-          const double tb1 = b1 * 2 / (bottomf * bottomf) + a.mu * (P[5] - a.UOld[2 * item + 1] - a.vdual[2 * item + 1]);
-          const double dmax = isnan(A11) ? A22 : (isnan(A22) ? A11 : fmax(A11, A22));
-          double dP[2];
-          solve2(A11 + 1e-3 * dmax, A12, A22 + 1e-3 * dmax, tb0, tb1, &dP[0], &dP[1]);
-          nN = sqrt(tb0 * tb0 + tb1 * tb1);
-          nA = nN;
-          const double nI = step == 1 ? nN : normInit;
-          ctl->nI = nI;
-          nN = nI > tol ? nN / nI : 0;
-          if (nN < tol || nA < tol) done = 1;
-          else {
-            const double D[6] = {0, 0, 0, 0, -dP[0], -dP[1]};
-            if (!compose_update(Pn, D)) done = 2;
-          }
+      // convergence test (FP32) and the FP64 update, identical on every warp
+      int done = 0;
+      float nb = 0.f;
+      double D[6] = {0, 0, 0, 0, 0, 0};
+      if constexpr (TWO) {
+        const float b0 = bottomf * (bsum[0] + bsum[1]), b1 = bottomf * (bsum[2] + bsum[3]);
+        const float sc2 = 2.f / (bottomf * bottomf);
+        const float tb0 = b0 * sc2 + (float)(a.mu * (P[4] - a.UOld[2 * item] - a.vdual[2 * item]));
+        const float tb1 = b1 * sc2 + (float)(a.mu * (P[5] - a.UOld[2 * item + 1] - a.vdual[2 * item + 1]));
+        nb = tb0 * tb0 + tb1 * tb1;
+        D[4] = -(i00 * (double)tb0 + i01 * (double)tb1);
+        D[5] = -(i10 * (double)tb0 + i11 * (double)tb1);
+      } else {
+        float b[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) { b[q] = bottomf * (bsum[2 * q] + bsum[2 * q + 1]); nb += b[q] * b[q]; }
+        if (hok) {
+          double dk = 0;
+#pragma unroll
+          for (int q = 0; q < 6; ++q) dk += hinv[q] * (double)b[q];
+#pragma unroll
+          for (int q = 0; q < 6; ++q) D[q] = -shfl_d(dk, q);
         } else {
-          double b[6], nb = 0;
-          for (int k = 0; k < 6; ++k) { b[k] = bottomf * b2[k]; nb += b[k] * b[k]; }
-          nN = sqrt(nb);
-          nA = nN;
-          const double nI = step == 1 ? nN : normInit;
-          ctl->nI = nI;
-          nN = nI > tol ? nN / nI : 0;
-          if (nN < tol || nA < tol) done = 1;
-          else {
-            double D[6];
-            if (ch.ok) chol6_solve(ch, b, D);
-            else small_solve(ctl->Hm, b, 6, D);
-            for (int k = 0; k < 6; ++k) D[k] = -D[k];
-            if (!compose_update(Pn, D)) done = 2;
-          }
+          double bd[6];
+#pragma unroll
+          for (int q = 0; q < 6; ++q) bd[q] = (double)b[q];
+          small_solve(ctl->Hm, bd, 6, D);
+#pragma unroll
+          for (int q = 0; q < 6; ++q) D[q] = -D[q];
         }
-        for (int k = 0; k < 6; ++k) ctl->P[k] = Pn[k];
-        ctl->nN = nN;
-        ctl->nA = nA;
-        ctl->flag = done;
       }
-      tm.sync();
-      normInit = ctl->nI;
-      normNew = ctl->nN;
-      normAbs = ctl->nA;
-      const int done = ctl->flag;
-      for (int k = 0; k < 6; ++k) P[k] = ctl->P[k];
-      tm.sync();
+      float nN = sqrtf(nb);
+      const float nA = nN;
+      if (step == 1) normInit = nN;
+      nN = normInit > tolf ? nN / normInit : 0.f;
+      normNew = nN;
+      normAbs = nA;
+      if (nN < tolf || nA < tolf) done = 1;
+      else if (!compose_warp(P, D, lane)) done = 2;
       if (done) break;
+      oob = corners_oob_warp(P, x0, y0, x1, y1, mx, my, a.W, a.H, lane);
     }
     if (run) {
       if (err) { code = err_code; nan_out = true; }
       else {
         code = step;
-        if (!(normNew < tol || normAbs < tol)) code = kMaxIter + 1;
+        if (!(normNew < tolf || normAbs < tolf)) code = kMaxIter + 1;
         if (isnan(normNew)) code = kMaxIter + 1;
         if constexpr (TWO) {
-          float v = 0.f;
-          for (int p = tm.tl; p < npx; p += tm.TT) v += fabsf(tf[p]);
-          const float vv[1] = {v};
-          double sv[1];
-          tm.template sumf<1>(vv, sv, fscr);
-          sabs = sv[0];
+          float v[1] = {0.f};
+          for (int p = tm.tl; p < npx; p += tm.TT) v[0] += fabsf(tf[p]);
+          tm.template sumf<1>(v, fscr);
+          sabs = v[0];
         }
-        if (sabs < 1e-6) code = kMaxIter + 3;
+        if (sabs < 1e-6f) code = kMaxIter + 3;
       }
     }
     if (tm.tl == 0) {
@@ -698,6 +761,7 @@ __global__ void __launch_bounds__(256) icgn_batched_kernel(BatchedArgs B) {
       a.U[2 * item] = nan_out ? nan("") : P[4];
       a.U[2 * item + 1] = nan_out ? nan("") : P[5];
       if constexpr (!TWO) {
+#pragma unroll
         for (int k = 0; k < 4; ++k) a.F[4 * item + k] = nan_out ? nan("") : P[k];
         if (a.Hpk) {
           int q = 0;

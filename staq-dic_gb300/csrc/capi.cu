@@ -429,11 +429,23 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
   const bool two = b.two_dof != 0;
   if (cands.empty()) return fail(c, STDIC_E_UNSUPPORTED, "no launch shape fits this subset size");
   auto launch = [&](const BatchedCand& cd) -> int {
-    cudaError_t e = cudaMemsetAsync(b.queue_head, 0, sizeof(int), c->stream);
-    if (e != cudaSuccess) return cuda_fail(c, e, "queue reset");
     b.warps_per_subset = cd.tw;
     b.smem_px = cd.smem_px;
-    return check_launch(c, stdic::launch_icgn_batched(b, cd.blocks, cd.threads, c->stream), "IC-GN batched");
+    // 2-DOF: one fused pass; 6-DOF: set-up, FP64 factorisation, iterations
+    const int stages[2] = {two ? 0 : 1, 2};
+    for (int k = 0; k < (two ? 1 : 2); ++k) {
+      cudaError_t e = cudaMemsetAsync(b.queue_head, 0, sizeof(int), c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "queue reset");
+      b.stage = stages[k];
+      int rc = check_launch(c, stdic::launch_icgn_batched(b, cd.blocks, cd.threads, c->stream), "IC-GN batched");
+      if (rc) return rc;
+      if (!two && k == 0) {
+        rc = check_launch(c, stdic::launch_factor6((const stdic::SubsetState6*)b.st6, b.H6, b.Hinv6, Ntot, c->stream),
+                          "Hessian factorisation");
+        if (rc) return rc;
+      }
+    }
+    return STDIC_OK;
   };
   const int nb = Ntot <= 0 ? 0 : (int)std::ceil(std::log2((double)Ntot));
   const auto key = std::make_tuple(nb, b.a.npx_max, (int)two, b.frames);
@@ -497,10 +509,15 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
   unsigned char* bscr = nullptr;
   const int npx_max = stdic::grown_tile_pixels(winsize);
   std::vector<BatchedCand> cands;
+  stdic::SubsetState6* st6 = nullptr;
+  double *H6 = nullptr, *Hinv6 = nullptr;
   if (batched) {
     cands = batched_candidates(c, false, npx_max, N);
     pl.scratch((size_t)std::max(N, 1), &order);
     pl.scratch(batched_scratch_need(cands), &bscr);
+    pl.scratch((size_t)std::max(N, 1), &st6);
+    pl.scratch(21 * (size_t)std::max(N, 1), &H6);
+    pl.scratch(36 * (size_t)std::max(N, 1), &Hinv6);
   }
   int rc = pl.commit(c);
   if (rc) return rc;
@@ -516,13 +533,14 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
       c->solver_timed = rc == STDIC_OK;
     } else {
       rc = convert_frame(c, fr, &d, 1);
-      if (!rc) rc = check_launch(c, stdic::launch_build_queue(a.ws_list, nullptr, winsize, N, order, nullptr, c->stream), "queue");
+      if (!rc) rc = check_launch(c, stdic::launch_build_queue(a.ws_list, nullptr, winsize, N, order, nullptr, c->stream, 1), "queue");
       if (!rc) {
         stdic::BatchedArgs b{};
         b.a = a;
         b.f32 = d.f32; b.g32 = d.g32; b.dfdx32 = d.dfdx32; b.dfdy32 = d.dfdy32;
         b.order = order; b.queue_head = c->scal; b.two_dof = 0; b.frames = 1; b.g_stride = 0;
         b.scratch = bscr;
+        b.st6 = st6; b.H6 = H6; b.Hinv6 = Hinv6;
         rc = run_batched(c, b, N, cands);
       }
     }
@@ -637,7 +655,7 @@ static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, 
       c->solver_timed = rc == STDIC_OK;
     } else {
       rc = convert_frame(c, fr, &d, 1);
-      if (!rc) rc = check_launch(c, stdic::launch_build_queue(nullptr, a.wsl2, 0, N, order, nullptr, c->stream), "queue");
+      if (!rc) rc = check_launch(c, stdic::launch_build_queue(nullptr, a.wsl2, 0, N, order, nullptr, c->stream, 1), "queue");
       if (!rc) {
         stdic::BatchedArgs b{};
         b.a = a;

@@ -90,14 +90,14 @@ struct Team {
 // narrow FP64 pipe sees a few dozen instructions per iteration.
 STDIC_DEV double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
-// P <- P o DeltaP^-1 (funICGNQuadtree.m:393-411) with D known on every lane.
-// Returns false (P unchanged) when det(DeltaP) == 0.
-STDIC_DEV bool compose_warp(double P[6], const double D[6], int lane) {
-  const double det = (1 + D[0]) * (1 + D[3]) - D[1] * D[2];
-  if (!(det != 0)) return false;
-  const double inv = 1.0 / det;
-  // lane k < 6 forms tempP_(k+1)
-  double t = 0;
+// P <- P o DeltaP^-1 (funICGNQuadtree.m:393-411), warp-parallel in FP32:
+// lane k < 6 forms tempP_(k+1), then the new P_(k+1); D is known on every
+// lane.  Returns false (P unchanged) when det(DeltaP) == 0.
+STDIC_DEV bool compose_warp(float P[6], const float D[6], int lane) {
+  const float det = (1.f + D[0]) * (1.f + D[3]) - D[1] * D[2];
+  if (!(det != 0.f)) return false;
+  const float inv = 1.f / det;
+  float t = 0.f;
   switch (lane) {
     case 0: t = (-D[0] - D[0] * D[3] + D[1] * D[2]) * inv; break;
     case 1: t = -D[1] * inv; break;
@@ -106,39 +106,39 @@ STDIC_DEV bool compose_warp(double P[6], const double D[6], int lane) {
     case 4: t = (-D[4] - D[3] * D[4] + D[2] * D[5]) * inv; break;
     case 5: t = (-D[5] - D[0] * D[5] + D[1] * D[4]) * inv; break;
   }
-  double T[6];
+  float T[6];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) T[k] = shfl_d(t, k);
-  // lane k < 6 forms the new P_(k+1)
-  double pn = 0;
+  for (int k = 0; k < 6; ++k) T[k] = __shfl_sync(0xffffffffu, t, k);
+  float pn = 0.f;
   switch (lane) {
-    case 0: pn = (1 + P[0]) * (1 + T[0]) + P[2] * T[1] - 1; break;
-    case 1: pn = P[1] * (1 + T[0]) + (1 + P[3]) * T[1]; break;
-    case 2: pn = (1 + P[0]) * T[2] + P[2] * (1 + T[3]); break;
-    case 3: pn = P[1] * T[2] + (1 + P[3]) * (1 + T[3]) - 1; break;
-    case 4: pn = (1 + P[0]) * T[4] + P[2] * T[5] + P[4]; break;
-    case 5: pn = P[1] * T[4] + (1 + P[3]) * T[5] + P[5]; break;
+    case 0: pn = P[0] + ((1.f + P[0]) * T[0] + P[2] * T[1]); break;
+    case 1: pn = P[1] * (1.f + T[0]) + (1.f + P[3]) * T[1]; break;
+    case 2: pn = (1.f + P[0]) * T[2] + P[2] * (1.f + T[3]); break;
+    case 3: pn = P[3] + (P[1] * T[2] + (1.f + P[3]) * T[3]); break;
+    case 4: pn = P[4] + ((1.f + P[0]) * T[4] + P[2] * T[5]); break;
+    case 5: pn = P[5] + (P[1] * T[4] + (1.f + P[3]) * T[5]); break;
   }
 #pragma unroll
-  for (int k = 0; k < 6; ++k) P[k] = shfl_d(pn, k);
+  for (int k = 0; k < 6; ++k) P[k] = __shfl_sync(0xffffffffu, pn, k);
   return true;
 }
 
 // Bounds test of the warp P over the tile [x1, x1+mx-1] x [y1, y1+my-1]: lanes
-// 0..7 evaluate one coordinate of one corner each (the warp is affine).
-STDIC_DEV bool corners_oob_warp(const double P[6], long long x0, long long y0, long long x1,
-                                long long y1, int mx, int my, int W, int H, int lane) {
+// 0..7 evaluate one coordinate of one corner each (the warp is affine); the
+// integer node position is kept apart from the FP32 offset.
+STDIC_DEV bool corners_oob_warp(const float P[6], int x0, int y0, int x1, int y1, int mx, int my,
+                                int W, int H, int lane) {
   bool bad = false;
   if (lane < 8) {
     const int cn = lane >> 1;
-    const double dx = (double)((cn & 1 ? x1 + mx - 1 : x1) - x0);
-    const double dy = (double)((cn & 2 ? y1 + my - 1 : y1) - y0);
+    const float dx = (float)((cn & 1 ? x1 + mx - 1 : x1) - x0);
+    const float dy = (float)((cn & 2 ? y1 + my - 1 : y1) - y0);
     if ((lane & 1) == 0) {
-      const double u22 = (1 + P[0]) * dx + P[2] * dy + ((double)x0 + P[4]);
-      bad = u22 < 3 || u22 > (double)W - 2;
+      const float o = (1.f + P[0]) * dx + P[2] * dy + P[4];
+      bad = o < (float)(3 - x0) || o > (float)(W - 2 - x0);
     } else {
-      const double v22 = P[1] * dx + (1 + P[3]) * dy + ((double)y0 + P[5]);
-      bad = v22 < 3 || v22 > (double)H - 2;
+      const float o = P[1] * dx + (1.f + P[3]) * dy + P[5];
+      bad = o < (float)(3 - y0) || o > (float)(H - 2 - y0);
     }
   }
   return __any_sync(0xffffffffu, bad);
@@ -154,10 +154,82 @@ struct Kahan {
   }
 };
 
+// Runs of the set bits of A that contain a bit of S (S subset of A): adding S
+// to A carries through each seeded run and clears it, so ((A + S) ^ A) & A
+// marks every bit from the seed to the top of its run; the bit-reversed form
+// gives the part below the seed.
+STDIC_DEV uint64_t run_fill(uint64_t A, uint64_t S) {
+  const uint64_t up = ((A + S) ^ A) & A;
+  const uint64_t Ar = __brevll(A), Sr = __brevll(S);
+  const uint64_t dn = __brevll(((Ar + Sr) ^ Ar) & Ar);
+  return up | dn | S;
+}
+
+// bwselect on an m x n tile (m <= 64, n <= 96) by one warp with bitmaps: lane
+// l owns the tile columns l, l+32, l+64 (fixed dim-2 index), each a 64-bit
+// mask over dim 1.  Every round fills the seeded runs of each column and then
+// lets each column take the pixels of its neighbour columns' selection
+// (shifted by one for 8-connectivity); rounds repeat until no column changes,
+// at most m*n rounds since each productive round adds a pixel.
+STDIC_DEV void bwselect_warp_bits(const uint8_t* allow, uint8_t* sel, int m, int n, int r1, int c1,
+                                  int conn) {
+  const int lane = threadIdx.x & 31;
+  uint64_t A[3], S[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int j = lane + 32 * c;
+    uint64_t a = 0;
+    if (j < n)
+      for (int i = 0; i < m; ++i) a |= (uint64_t)(allow[i + j * m] != 0) << i;
+    A[c] = a;
+    S[c] = 0;
+    if (r1 >= 1 && r1 <= m && c1 >= 1 && c1 <= n && j == c1 - 1) S[c] = a & (1ull << (r1 - 1));
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) S[c] = run_fill(A[c], S[c]);
+  for (;;) {
+    uint64_t L[3], R[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const uint64_t up = __shfl_up_sync(0xffffffffu, S[c], 1);
+      const uint64_t dn = __shfl_down_sync(0xffffffffu, S[c], 1);
+      const uint64_t wrapL = c > 0 ? __shfl_sync(0xffffffffu, S[c > 0 ? c - 1 : 0], 31) : 0ull;
+      const uint64_t wrapR = c < 2 ? __shfl_sync(0xffffffffu, S[c < 2 ? c + 1 : 2], 0) : 0ull;
+      L[c] = lane == 0 ? wrapL : up;
+      R[c] = lane == 31 ? wrapR : dn;
+    }
+    bool changed = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      uint64_t nb = L[c] | R[c];
+      if (conn == 8) nb |= (L[c] << 1) | (L[c] >> 1) | (R[c] << 1) | (R[c] >> 1);
+      const uint64_t t = S[c] | (nb & A[c]);
+      const uint64_t f = t != S[c] ? run_fill(A[c], t) : t;
+      changed |= f != S[c];
+      S[c] = f;
+    }
+    if (!__any_sync(0xffffffffu, changed)) break;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int j = lane + 32 * c;
+    if (j < n)
+      for (int i = 0; i < m; ++i) sel[i + j * m] = (uint8_t)((S[c] >> i) & 1);
+  }
+  __syncwarp();
+}
+
 // flood fill of bwselect restricted to a team (see bwselect_block)
 template <int TW>
 STDIC_DEV void bwselect_team(const Team<TW>& tm, const uint8_t* allow, uint8_t* sel_, int m, int n,
                              int r1, int c1, int conn, int* iscr) {
+  if constexpr (TW == 1) {
+    if (m <= 64 && n <= 96) {
+      __syncwarp();
+      bwselect_warp_bits(allow, sel_, m, n, r1, c1, conn);
+      return;
+    }
+  }
   volatile uint8_t* sel = sel_;
   const int npx = m * n;
   for (int p = tm.tl; p < npx; p += tm.TT) sel[p] = 0;
@@ -222,23 +294,6 @@ STDIC_DEV bool mask_crop_ok32(const Frame32& fr, long long x1, long long x3, lon
   return x1 >= 1 && x3 <= fr.W && y1 >= 1 && y3 <= fr.H;
 }
 
-// Affine warp is linear in (dx, dy): the tile's extreme positions are at its corners.
-STDIC_DEV bool corners_oob(const Frame32& fr, const double P[6], long long x0, long long y0,
-                           long long x1, long long y1, int mx, int my) {
-  const double dxs[2] = {(double)(x1 - x0), (double)(x1 + mx - 1 - x0)};
-  const double dys[2] = {(double)(y1 - y0), (double)(y1 + my - 1 - y0)};
-  bool bad = false;
-#pragma unroll
-  for (int a = 0; a < 2; ++a)
-#pragma unroll
-    for (int b = 0; b < 2; ++b) {
-      const double u22 = (1 + P[0]) * dxs[a] + P[2] * dys[b] + ((double)x0 + P[4]);
-      const double v22 = P[1] * dxs[a] + (1 + P[3]) * dys[b] + ((double)y0 + P[5]);
-      bad |= (u22 < 3 || u22 > (double)fr.W - 2 || v22 < 3 || v22 > (double)fr.H - 2);
-    }
-  return bad;
-}
-
 // Bicubic sample of g at (iu + su, iv + sv): integer base + FP32 offset.
 STDIC_DEV float cubic32(const float* __restrict__ g, int W, int H, int iu, float su, int iv,
                         float sv) {
@@ -270,6 +325,7 @@ struct PixIter {
   STDIC_DEV PixIter(int p0, int stride, int mx_) : mx(mx_) {
     i = p0 % mx_; j = p0 / mx_; di = stride % mx_; dj = stride / mx_;
   }
+  STDIC_DEV PixIter(const int4& start, int mx_) : i(start.x), j(start.y), di(start.z), dj(start.w), mx(mx_) {}
   STDIC_DEV void next() {
     i += di; j += dj;
     if (i >= mx) { i -= mx; ++j; }
@@ -321,12 +377,26 @@ STDIC_DEV void chol6_solve(const Chol6& C, const double b[6], double x[6]) {
   }
 }
 
+// DeltaP = -H \ b by LU with partial pivoting for a Hessian whose Cholesky
+// factorisation failed (MATLAB's mldivide falls back the same way); kept out
+// of line so its local arrays exist only on this rare path.
+__device__ __noinline__ void singular_solve6(const double* __restrict__ H, const float b[6], float D[6]) {
+  double Hm[36], bd[6], Dd[6];
+  for (int r = 0; r < 6; ++r)
+    for (int c2 = 0; c2 <= r; ++c2) {
+      Hm[r * 6 + c2] = H[r * (r + 1) / 2 + c2];
+      Hm[c2 * 6 + r] = H[r * (r + 1) / 2 + c2];
+    }
+  for (int q = 0; q < 6; ++q) bd[q] = (double)b[q];
+  small_solve(Hm, bd, 6, Dd);
+  for (int q = 0; q < 6; ++q) D[q] = (float)(-Dd[q]);
+}
+
 struct TeamCtl {
-  double P[6];
-  double Hm[36];
-  double nN, nA, nI;
-  int flag;
+  double Hm[36];    // inverse Hessian of the team's current subset (6-DOF)
+  float jf[6], j1[6];
   int item;
+  int pad[3];
 };
 
 }  // namespace
@@ -344,10 +414,13 @@ size_t batched_scratch_bytes(int npx_max, bool two, long long teams) {
 // 2-DOF)] + 4 smem_px bytes of bitmaps, then the control block and reduction
 // scratch.  Global scratch per team: the same layout for npx_max pixels.
 //
-// Every warp of a team holds the team totals after each reduction and runs the
-// same FP64 update on them, so all warps carry bit-identical P without a
-// shared-memory broadcast.
-template <int TW, bool TWO>
+// Stages (B.stage): 0 runs the 2-DOF form fused; for the 6-DOF form stage 1
+// does the per-subset set-up (window, masks, f statistics, FP32 Hessian) and
+// stage 2 the iterations with the inverse Hessian the factor kernel produced
+// in FP64 between them.  Every warp of a team holds the team totals after each
+// reduction and runs the same FP64 update on them, so all warps carry
+// bit-identical P without a shared-memory broadcast.
+template <int TW, bool TWO, int STAGE>
 __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
   extern __shared__ __align__(16) unsigned char dsm[];
   const IcgnArgs& a = B.a;
@@ -355,6 +428,7 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
   tm.id = threadIdx.x / Team<TW>::TT;
   tm.tl = threadIdx.x % Team<TW>::TT;
   const int lane = threadIdx.x & 31;
+  constexpr int stage = STAGE;
   const int teams_per_block = blockDim.x / Team<TW>::TT;
   const long long gteam = (long long)blockIdx.x * teams_per_block + tm.id;
   const int smpx = B.smem_px;
@@ -366,6 +440,7 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
   int* iscr = (int*)(fscr + 32 * TW);
   const size_t gstride = (size_t)a.npx_max * (TWO ? 8 : 4) + 4 * (size_t)a.npx_max;
   unsigned char* gbase = B.scratch + gstride * gteam;
+  SubsetState6* st6 = (SubsetState6*)B.st6;
 
   const int Ntot = a.N * (B.frames > 0 ? B.frames : 1);
   const float tolf = (float)a.tol;
@@ -387,54 +462,73 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
 
     // ---------------- per-subset set-up ----------------
     int wx, wy;
-    double P[6];
+    float P[6];  // warp parameters [F11 F21 F12 F22 u v] in FP32
     if constexpr (TWO) {
       wx = a.wsl2[node]; wy = a.wsl2[a.N + node];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) P[k] = a.FOld[4 * item + k];
-      P[4] = a.UOld[2 * item]; P[5] = a.UOld[2 * item + 1];
+      for (int k = 0; k < 4; ++k) P[k] = (float)a.FOld[4 * item + k];
+      P[4] = (float)a.UOld[2 * item]; P[5] = (float)a.UOld[2 * item + 1];
     } else {
       wx = wy = a.ws_list ? a.ws_list[node] : a.ws_all;
-      P[0] = P[1] = P[2] = P[3] = 0;
-      P[4] = a.U0[2 * item]; P[5] = a.U0[2 * item + 1];
+      P[0] = P[1] = P[2] = P[3] = 0.f;
+      P[4] = (float)a.U0[2 * item]; P[5] = (float)a.U0[2 * item + 1];
     }
     const int ws0 = wx;
+    float uold0 = 0.f, uold1 = 0.f, vd0 = 0.f, vd1 = 0.f;
+    if constexpr (TWO) {
+      uold0 = P[4]; uold1 = P[5];
+      vd0 = (float)a.vdual[2 * item]; vd1 = (float)a.vdual[2 * item + 1];
+    }
     long long x1 = x0 - wx / 2, x3 = x0 + wx / 2, y1 = y0 - wy / 2, y3 = y0 + wy / 2;
     int code = 0;
     bool nan_out = false;
-    bool hdone = false;
     const int err_code = TWO ? 0 : -1;  // value the reference leaves on a run-time error
-    const bool crop_valid = !((wx & 1) || (wy & 1)) && wx >= 0 && wy >= 0 && wx <= a.ws_max &&
-                            wy <= a.ws_max && mask_crop_ok32(fr, x1, x3, y1, y3);
-    int cntf = 0, nanf = 0;
-    if (crop_valid) {
-      const int mx0 = wx + 1, np0 = (wx + 1) * (wy + 1);
-      PixIter it(tm.tl, tm.TT, mx0);
-      for (int p = tm.tl; p < np0; p += tm.TT, it.next()) {
-        const float t = fr.F(x1 + it.i, y1 + it.j) * fr.M(x1 + it.i, y1 + it.j);
-        if (t != t) nanf = 1;
-        if (t == 0.f) ++cntf;
-      }
-    }
-    cntf = tm.sum_int(cntf, iscr);
-    nanf = tm.any(nanf, iscr);
-    if constexpr (!TWO) {
-      if (a.mark && tm.tl == 0) a.mark[item] = (!crop_valid || cntf > 0) ? 1 : 0;
-    }
-    const double npx0 = (double)(wx + 1) * (double)(wy + 1);
+    int cntf = 0;
     float meanf = 0.f, bottomf = 0.f, sabs = 0.f;
     double A11 = 0, A12 = 0, A22 = 0;
     int mx = 0, my = 0, npx = 0, sc = 0, sr = 0;
+    int4 pstart = make_int4(0, 0, 0, 0);  // PixIter start of this thread for the tile
     float* tg = nullptr;
     float* tf = nullptr;
     uint8_t *mtile = nullptr, *bwf = nullptr, *bwg = nullptr, *tmp = nullptr;
     bool has_masked = false;
-    if (!crop_valid || !crop_ok32(fr, x1, x3, y1, y3) || nanf) {
-      code = err_code; nan_out = true;
-    } else if (!((double)cntf < 0.4 * npx0)) {
-      code = kMaxIter + 2;
+    bool decided = false;  // outputs of this subset already written by the set-up stage
+    const double npx0 = (double)(wx + 1) * (double)(wy + 1);
+
+    if (stage == 2) {
+      const SubsetState6 s6 = st6[item];
+      if (s6.code != 0) {
+        decided = true;
+      } else {
+        wx = wy = s6.ws;
+        x1 = x0 - wx / 2; x3 = x0 + wx / 2; y1 = y0 - wy / 2; y3 = y0 + wy / 2;
+        cntf = s6.cntf;
+        has_masked = s6.masked != 0;
+        meanf = s6.meanf; bottomf = s6.bottomf; sabs = s6.sabs;
+      }
     } else {
-      if ((double)cntf > 0.0 * npx0) {
+      const bool crop_valid = !((wx & 1) || (wy & 1)) && wx >= 0 && wy >= 0 && wx <= a.ws_max &&
+                              wy <= a.ws_max && mask_crop_ok32(fr, x1, x3, y1, y3);
+      int nanf = 0;
+      if (crop_valid) {
+        const int mx0 = wx + 1, np0 = (wx + 1) * (wy + 1);
+        PixIter it(tm.tl, tm.TT, mx0);
+        for (int p = tm.tl; p < np0; p += tm.TT, it.next()) {
+          const float t = fr.F(x1 + it.i, y1 + it.j) * fr.M(x1 + it.i, y1 + it.j);
+          if (t != t) nanf = 1;
+          if (t == 0.f) ++cntf;
+        }
+      }
+      cntf = tm.sum_int(cntf, iscr);
+      nanf = tm.any(nanf, iscr);
+      if constexpr (!TWO) {
+        if (a.mark && tm.tl == 0) a.mark[item] = (!crop_valid || cntf > 0) ? 1 : 0;
+      }
+      if (!crop_valid || !crop_ok32(fr, x1, x3, y1, y3) || nanf) {
+        code = err_code; nan_out = true;
+      } else if (!((double)cntf < 0.4 * npx0)) {
+        code = kMaxIter + 2;
+      } else if ((double)cntf > 0.0 * npx0) {
         if constexpr (TWO) {
           {
             const double aa = (double)(wx + 1) * (double)(wy + 1);
@@ -453,78 +547,105 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
           code = err_code; nan_out = true;
         }
       }
-      if (!nan_out) {
-        mx = wx + 1; my = wy + 1; npx = mx * my;
-        sc = (wx + 1) / 2; sr = (wy + 1) / 2;
-        // tile storage: the team's shared slot when it fits, else its global slice
-        const bool in_smem = npx <= smpx;
-        const int cap = in_smem ? smpx : a.npx_max;
-        unsigned char* st = in_smem ? base : gbase;
-        tg = (float*)st;
-        tf = tg + cap;
-        mtile = (uint8_t*)(tg + (TWO ? 2 : 1) * cap);
-        bwf = mtile + cap;
-        bwg = bwf + cap;
-        tmp = bwg + cap;
-        int z = 0;
-        PixIter it(tm.tl, tm.TT, mx);
-        for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
-          const uint8_t mk = __ldg(fr.mask + (y1 + it.j - 1) * fr.W + (x1 + it.i - 1)) != 0;
-          mtile[p] = mk;
-          if (!mk) z = 1;
-        }
-        has_masked = tm.any(z, iscr) != 0;
-        if (has_masked) bwselect_team(tm, mtile, bwf, mx, my, sr, sc, 4, iscr);
-        tm.sync();
+    }
+    // tile storage, mask tile and the 4-connected f selection
+    if (!decided && code == 0 && !nan_out) {
+      mx = wx + 1; my = wy + 1; npx = mx * my;
+      sc = (wx + 1) / 2; sr = (wy + 1) / 2;
+      pstart = make_int4(tm.tl % mx, tm.tl / mx, tm.TT % mx, tm.TT / mx);
+      const bool in_smem = npx <= smpx;
+      const int cap = in_smem ? smpx : a.npx_max;
+      unsigned char* stp = in_smem ? base : gbase;
+      tg = (float*)stp;
+      tf = tg + cap;
+      mtile = (uint8_t*)(tg + (TWO ? 2 : 1) * cap);
+      bwf = mtile + cap;
+      bwg = bwf + cap;
+      tmp = bwg + cap;
+      int z = 0;
+      PixIter it(pstart, mx);
+      for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+        const uint8_t mk = __ldg(fr.mask + (y1 + it.j - 1) * fr.W + (x1 + it.i - 1)) != 0;
+        mtile[p] = mk;
+        if (!mk) z = 1;
       }
+      if (stage != 2) has_masked = tm.any(z, iscr) != 0;
+      if (has_masked) bwselect_team(tm, mtile, bwf, mx, my, sr, sc, 4, iscr);
+      tm.sync();
     }
 
     const uint8_t* bw = has_masked ? bwf : nullptr;  // nullptr: every pixel selected
+    constexpr int NQ = TWO ? 2 : 6;  // parameters of the b-vector
     double hinv[6];  // lane k < 6: row k of the inverse Hessian (6-DOF)
     bool hok = false;
     double i00 = 0, i01 = 0, i10 = 0, i11 = 0;  // inverse of the 2x2 system (2-DOF)
-    // f-side statistics: Hessian (6x6 or 2x2), meanf, bottomf, sum |tempf|
+    // f-side parts of b: jf = sum J (tempf - meanf), j1 = sum J
+    float jf[NQ], j1[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) { jf[q] = 0.f; j1[q] = 0.f; }
+    // steepest-descent images J of pixel (i, j): [dx gx, dx gy, dy gx, dy gy, gx, gy]
+    // (6-DOF) or [gx, gy] (2-DOF), gx/gy masked by the current selection
+    auto jac = [&](int i, int j, float s, float (&J)[NQ]) {
+      const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
+      if constexpr (TWO) {
+        J[0] = gx; J[1] = gy;
+      } else {
+        const float dx = (float)(int)(x1 + i - x0), dy = (float)(int)(y1 + j - y0);
+        J[0] = dx * gx; J[1] = dx * gy; J[2] = dy * gx; J[3] = dy * gy; J[4] = gx; J[5] = gy;
+      }
+    };
+    // f-side statistics: Hessian (6x6 or 2x2), meanf, bottomf, sum |tempf|, jf, j1.
+    // The 6-DOF set-up stage stores them; the 2-DOF form recomputes them when
+    // the g selection changes (funICGN_Subpb1.m:171-190).
     auto f_side = [&]() {
       float hs[21];
 #pragma unroll
       for (int k = 0; k < 21; ++k) hs[k] = 0.f;
       Kahan sf;
       float nf = 0.f, sa = 0.f;
-      PixIter it(tm.tl, tm.TT, mx);
+      PixIter it(pstart, mx);
       for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
         const int i = it.i, j = it.j;
         const float s = bw ? (float)bw[p] : 1.f;
-        const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
         const float fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
         if constexpr (TWO) tf[p] = fv;
         sa += fabsf(fv);
         if (fabsf(fv) > 1e-10f) { sf.add(fv); nf += 1.f; }
-        if constexpr (TWO) {
-          hs[0] += gx * gx; hs[1] += gx * gy; hs[2] += gy * gy;
-        } else {
-          const float dx = (float)(int)(x1 + i - x0), dy = (float)(int)(y1 + j - y0);
-          const float J[6] = {dx * gx, dx * gy, dy * gx, dy * gy, gx, gy};
-          int q = 0;
+        float J[NQ];
+        jac(i, j, s, J);
+        int q = 0;
 #pragma unroll
-          for (int aa = 0; aa < 6; ++aa)
+        for (int aa = 0; aa < NQ; ++aa)
 #pragma unroll
-            for (int bb = aa; bb < 6; ++bb) hs[q++] += J[aa] * J[bb];
-        }
+          for (int bb = aa; bb < NQ; ++bb) hs[q++] += J[aa] * J[bb];
       }
       float st4[4] = {sf.s, -sf.c, nf, sa};
       tm.template sumf<4>(st4, fscr);
       const float cnt = st4[2];
       const float mean = (st4[0] + st4[1]) / cnt;
-      Kahan q;
-      PixIter it2(tm.tl, tm.TT, mx);
+      Kahan q, kjf[NQ], kj1[NQ];
+      PixIter it2(pstart, mx);
       for (int p = tm.tl; p < npx; p += tm.TT, it2.next()) {
+        const float s = bw ? (float)bw[p] : 1.f;
         float fv;
         if constexpr (TWO) fv = tf[p];
-        else fv = fr.F(x1 + it2.i, y1 + it2.j) * fr.M(x1 + it2.i, y1 + it2.j) * (bw ? (float)bw[p] : 1.f);
+        else fv = fr.F(x1 + it2.i, y1 + it2.j) * fr.M(x1 + it2.i, y1 + it2.j) * s;
         if (fabsf(fv) > 1e-10f) { const float d = fv - mean; q.add(d * d); }
+        float J[NQ];
+        jac(it2.i, it2.j, s, J);
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) { kjf[k].add(J[k] * (fv - mean)); kj1[k].add(J[k]); }
       }
-      float qq[2] = {q.s, -q.c};
-      tm.template sumf<2>(qq, fscr);
+      float qq[2 + 4 * NQ];
+      qq[0] = q.s; qq[1] = -q.c;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        qq[2 + 4 * k] = kjf[k].s; qq[3 + 4 * k] = -kjf[k].c;
+        qq[4 + 4 * k] = kj1[k].s; qq[5 + 4 * k] = -kj1[k].c;
+      }
+      tm.template sumf<2 + 4 * NQ>(qq, fscr);
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) { jf[k] = qq[2 + 4 * k] + qq[3 + 4 * k]; j1[k] = qq[4 + 4 * k] + qq[5 + 4 * k]; }
       const float var = cnt == 0.f ? __int_as_float(0x7fc00000) : (cnt == 1.f ? 0.f : (qq[0] + qq[1]) / (cnt - 1.f));
       meanf = mean;
       bottomf = sqrtf((cnt - 1.f) * var);
@@ -541,60 +662,84 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
         solve2(A11 + 1e-3 * dmax, A12, A22 + 1e-3 * dmax, 0.0, 1.0, &i01, &i11);
       } else {
         tm.template sumf<21>(hs, fscr);
-        // Cholesky of H (every lane, FP64), then lane k < 6 solves for column k
-        // of H^-1 (= row k by symmetry)
-        double Hp[21];
+        // packed lower (row-major) Hessian for the factor kernel and the output
+        if (tm.tl < 21) {
+          float v = 0.f;
 #pragma unroll
-        for (int k = 0; k < 21; ++k) Hp[k] = 0;
-        {
-          int q2 = 0;
-#pragma unroll
-          for (int aa = 0; aa < 6; ++aa)
-#pragma unroll
-            for (int bb = aa; bb < 6; ++bb) {
-              // hs is (row aa, col bb >= aa); packed lower storage wants (bb, aa)
-              Hp[bb * (bb + 1) / 2 + aa] = (double)hs[q2];
-              ++q2;
-            }
+          for (int k = 0; k < 21; ++k)
+            if (k == tm.tl) v = hs[k];
+          // hs index of (row aa, col bb >= aa) -> packed lower (bb, aa)
+          int aa = 0, rem = tm.tl;
+          while (rem >= 6 - aa) { rem -= 6 - aa; ++aa; }
+          const int bb = aa + rem;
+          B.H6[(size_t)item * 21 + bb * (bb + 1) / 2 + aa] = (double)v;
+          // HGlobal = [H(1:6) H(8:12) ...]: column aa, rows aa..5 in the order of hs
+          if (a.Hpk) a.Hpk[(size_t)tm.tl * Ntot + item] = (double)v;
         }
-        if (tm.tl == 0) {
-          int q3 = 0;
-          for (int aa = 0; aa < 6; ++aa)
-            for (int bb = aa; bb < 6; ++bb) {
-              ctl->Hm[aa * 6 + bb] = (double)hs[q3]; ctl->Hm[bb * 6 + aa] = (double)hs[q3]; ++q3;
-            }
-        }
-        Chol6 ch;
-        chol6_factor(Hp, ch);
-        hok = ch.ok;
-        double e[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) e[k] = (lane == k) ? 1.0 : 0.0;
-        chol6_solve(ch, e, hinv);
       }
       tm.sync();
     };
 
-    const bool run = (code == 0 && !nan_out);
-    if (run) {
-      f_side();
-      hdone = true;
+    if (stage != 2 && !decided && code == 0 && !nan_out) f_side();
+
+    if (stage == 1) {
+      // hand the subset to the factor kernel and the iteration stage
+      if (tm.tl == 0) {
+        SubsetState6 s6;
+        s6.code = nan_out ? -1 : code;
+        s6.ws = wx; s6.cntf = cntf; s6.masked = has_masked ? 1 : 0;
+        s6.meanf = meanf; s6.bottomf = bottomf; s6.sabs = sabs; s6.pad = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) { s6.Jf[k] = jf[k < NQ ? k : 0]; s6.J1[k] = j1[k < NQ ? k : 0]; }
+        st6[item] = s6;
+        if (code != 0 || nan_out) {
+          a.conv[item] = code;
+          // decided in the set-up: P is still the initial guess, passed through in FP64
+          a.U[2 * item] = nan_out ? nan("") : a.U0[2 * item];
+          a.U[2 * item + 1] = nan_out ? nan("") : a.U0[2 * item + 1];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) a.F[4 * item + k] = nan_out ? nan("") : 0.0;
+          if (a.Hpk)
+            for (int q = 0; q < 21; ++q) a.Hpk[(size_t)q * Ntot + item] = 0.0;
+        }
+      }
+      tm.sync();
+      continue;
     }
+    if (decided) {
+      tm.sync();
+      continue;
+    }
+    if constexpr (!TWO) {
+      // the subset's inverse Hessian and f-side sums, once, into the team's control block
+      for (int k = tm.tl; k < 36; k += tm.TT) ctl->Hm[k] = B.Hinv6[(size_t)item * 36 + k];
+      if (tm.tl < 6) { ctl->jf[tm.tl] = st6[item].Jf[tm.tl]; ctl->j1[tm.tl] = st6[item].J1[tm.tl]; }
+      tm.sync();
+      hok = !isnan(ctl->Hm[0]);
+    }
+    const bool run = (code == 0 && !nan_out);
     float normNew = 1.f, normAbs = 1.f, normInit = 0.f;
-    int step = 0, cg = 0;
+    int step = 0, cg = 0, nupd = 0, last_cg = -1, last_nws = wx;
     bool err = false;
-    bool oob = run ? corners_oob_warp(P, x0, y0, x1, y1, mx, my, a.W, a.H, lane) : false;
+    bool oob = run ? corners_oob_warp(P, (int)x0, (int)y0, (int)x1, (int)y1, mx, my, a.W, a.H, lane) : false;
     while (run && step <= kMaxIter && normNew > tolf && normAbs > tolf) {
       ++step;
       if constexpr (!TWO) {
         if (step > 1 && (double)cntf > 0.0 * npx0) {
-          const double r = sqrt((double)((ws0 + 1) * (ws0 + 1)) / (double)cg) * wx / 2;
-          if (!isfinite(r)) { err = true; break; }
-          const int nws = 2 * (int)ceil(r);
+          // window growth test of funICGNQuadtree.m:140 (FP64, recomputed only
+          // when the count of selected g pixels changes)
+          int nws = last_nws;
+          if (cg != last_cg) {
+            const double r = sqrt((double)((ws0 + 1) * (ws0 + 1)) / (double)cg) * wx / 2;
+            if (!isfinite(r)) { err = true; break; }
+            nws = 2 * (int)ceil(r);
+            last_cg = cg;
+            last_nws = nws;
+          }
           if (nws != wx) {
             const long long nx1 = x0 - nws / 2, nx3 = x0 + nws / 2, ny1 = y0 - nws / 2, ny3 = y0 + nws / 2;
             if (!mask_crop_ok32(fr, nx1, nx3, ny1, ny3)) { err = true; break; }
-            if (corners_oob_warp(P, x0, y0, nx1, ny1, nws + 1, nws + 1, a.W, a.H, lane)) { normNew = 1e6f; break; }
+            if (corners_oob_warp(P, (int)x0, (int)y0, (int)nx1, (int)ny1, nws + 1, nws + 1, a.W, a.H, lane)) { normNew = 1e6f; break; }
             err = true;
             break;
           }
@@ -602,22 +747,21 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
       }
       if (oob) { normNew = 1e6f; break; }
       // integer base + FP32 offsets of the warp
-      const double bu = (double)x0 + P[4], bv = (double)y0 + P[5];
-      const int iu = (int)floor(bu), iv = (int)floor(bv);
-      const float fu = (float)(bu - iu), fv0 = (float)(bv - iv);
-      const float p0 = (float)(1 + P[0]), p1 = (float)P[1], p2 = (float)P[2], p3 = (float)(1 + P[3]);
+      const float flu = floorf(P[4]), flv = floorf(P[5]);
+      const int iu = (int)x0 + (int)flu, iv = (int)y0 + (int)flv;
+      const float fu = P[4] - flu, fv0 = P[5] - flv;
+      const float p0 = 1.f + P[0], p1 = P[1], p2 = P[2], p3 = 1.f + P[3];
       const float dx0 = (float)(int)(x1 - x0), dy0 = (float)(int)(y1 - y0);
       const float shift = meanf;  // one-pass variance around meanf
-      int zg = 0, nang = 0;
-      Kahan sg, qg;
-      float ng = 0.f;
+      // one pass: interpolation, zero/NaN counts, g statistics and sum J g
+      constexpr int NR = 7 + 2 * NQ;
+      float red[NR];
       {
-        PixIter it(tm.tl, tm.TT, mx);
-        for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
-          const float dx = dx0 + (float)it.i, dy = dy0 + (float)it.j;
-          const float su = fu + p0 * dx + p2 * dy;
-          const float sv = fv0 + p1 * dx + p3 * dy;
-          const float t = cubic32(fr.g, fr.W, fr.H, iu, su, iv, sv);
+        int zg = 0, nang = 0;
+        Kahan sg, qg, kg[NQ];
+        float ng = 0.f;
+        PixIter it(pstart, mx);
+        auto one = [&](int p, int i, int j, float t) {
           tg[p] = t;
           if (t != t) nang = 1;
           if (t == 0.f) ++zg;
@@ -627,20 +771,54 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
             qg.add(d * d);
             ng += 1.f;
           }
+          float J[NQ];
+          jac(i, j, bw ? (float)bw[p] : 1.f, J);
+#pragma unroll
+          for (int k = 0; k < NQ; ++k) kg[k].add(J[k] * t);
+        };
+        int p = tm.tl;
+        // two pixels per trip so that both pixels' 16 taps are in flight together
+        for (; p + tm.TT < npx; p += 2 * tm.TT) {
+          const int ia = it.i, ja = it.j;
+          it.next();
+          const int ib = it.i, jb = it.j;
+          it.next();
+          const float dxa = dx0 + (float)ia, dya = dy0 + (float)ja;
+          const float dxb = dx0 + (float)ib, dyb = dy0 + (float)jb;
+          const float ta = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dxa + p2 * dya, iv, fv0 + p1 * dxa + p3 * dya);
+          const float tb2 = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dxb + p2 * dyb, iv, fv0 + p1 * dxb + p3 * dyb);
+          one(p, ia, ja, ta);
+          one(p + tm.TT, ib, jb, tb2);
         }
+        if (p < npx) {
+          const float dx = dx0 + (float)it.i, dy = dy0 + (float)it.j;
+          const float t = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dx + p2 * dy, iv, fv0 + p1 * dx + p3 * dy);
+          one(p, it.i, it.j, t);
+        }
+        red[0] = (float)zg; red[1] = (float)nang;
+        red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) { red[7 + 2 * k] = kg[k].s; red[8 + 2 * k] = -kg[k].c; }
       }
-      zg = tm.sum_int(zg, iscr);
-      if (tm.any(nang, iscr)) { err = true; break; }
-      if (cntf > 0 || zg > 0) {
+      tm.template sumf<NR>(red, fscr);
+      if (red[1] > 0.f) { err = true; break; }
+      if (cntf > 0 || red[0] > 0.f) {
         for (int p = tm.tl; p < npx; p += tm.TT) tmp[p] = tg[p] != 0.f;
         tm.sync();
         bwselect_team(tm, tmp, bwg, mx, my, sr, sc, TWO ? 4 : 8, iscr);
         int anyzero = 0;
         for (int p = tm.tl; p < npx; p += tm.TT) anyzero |= !bwg[p];
         if (!tm.any(anyzero, iscr)) bwselect_team(tm, mtile, bwg, mx, my, sr, sc, 8, iscr);
+        if constexpr (TWO) {
+          bw = bwg;
+          f_side();
+        }
+        // the g tile restricted to its selection, and its sums again
         int cnt = 0;
-        sg = Kahan(); qg = Kahan(); ng = 0.f;
-        for (int p = tm.tl; p < npx; p += tm.TT) {
+        Kahan sg, qg, kg[NQ];
+        float ng = 0.f;
+        PixIter it(pstart, mx);
+        for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
           const float t = tg[p] * (float)bwg[p];
           tg[p] = t;
           cnt += bwg[p];
@@ -650,84 +828,82 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
             qg.add(d * d);
             ng += 1.f;
           }
+          float J[NQ];
+          jac(it.i, it.j, bw ? (float)bw[p] : 1.f, J);
+#pragma unroll
+          for (int k = 0; k < NQ; ++k) kg[k].add(J[k] * t);
         }
-        cg = tm.sum_int(cnt, iscr);
-        if constexpr (TWO) {
-          bw = bwg;
-          f_side();
-        }
+        red[0] = (float)cnt; red[1] = 0.f;
+        red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) { red[7 + 2 * k] = kg[k].s; red[8 + 2 * k] = -kg[k].c; }
+        tm.template sumf<NR>(red, fscr);
+        cg = (int)red[0];
       }
       // g statistics: mean and sqrt((n-1) var) from the shifted one-pass sums
-      float gs[5] = {sg.s, -sg.c, qg.s, -qg.c, ng};
-      tm.template sumf<5>(gs, fscr);
-      const float cntg = gs[4];
-      const float s1 = gs[0] + gs[1], s2 = gs[2] + gs[3];
+      const float cntg = red[6];
+      const float s1 = red[2] + red[3], s2 = red[4] + red[5];
       const float meang = shift + s1 / cntg;
       const float varg = cntg == 0.f ? __int_as_float(0x7fc00000)
                                      : (cntg == 1.f ? 0.f : fmaxf(s2 - s1 * s1 / cntg, 0.f) / (cntg - 1.f));
       const float bottomg = sqrtf((cntg - 1.f) * varg);
-      const float mf = meanf, ibf = 1.f / bottomf;
-      const float mg = meang, ibg = 1.f / bottomg;
-      float bsum[TWO ? 4 : 12];
-      if constexpr (TWO) {
-        Kahan k0, k1;
-        PixIter it3(tm.tl, tm.TT, mx);
-        for (int p = tm.tl; p < npx; p += tm.TT, it3.next()) {
-          const float s = bw ? (float)bw[p] : 1.f;
-          const float gx = fr.GX(x1 + it3.i, y1 + it3.j) * s, gy = fr.GY(x1 + it3.i, y1 + it3.j) * s;
-          const float r = (tf[p] - mf) * ibf - (tg[p] - mg) * ibg;
-          k0.add(gx * r);
-          k1.add(gy * r);
-        }
-        bsum[0] = k0.s; bsum[1] = -k0.c; bsum[2] = k1.s; bsum[3] = -k1.c;
-        tm.template sumf<4>(bsum, fscr);
-      } else {
-        Kahan k[6];
-        PixIter it3(tm.tl, tm.TT, mx);
-        for (int p = tm.tl; p < npx; p += tm.TT, it3.next()) {
-          const int i = it3.i, j = it3.j;
-          const float s = bw ? (float)bw[p] : 1.f;
-          const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
-          const float fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
-          const float dx = dx0 + (float)i, dy = dy0 + (float)j;
-          const float r = (fv - mf) * ibf - (tg[p] - mg) * ibg;
-          const float gxr = gx * r, gyr = gy * r;
-          k[0].add(dx * gxr); k[1].add(dx * gyr); k[2].add(dy * gxr); k[3].add(dy * gyr);
-          k[4].add(gxr); k[5].add(gyr);
-        }
+      const float ibf = 1.f / bottomf, ibg = 1.f / bottomg;
+      // b2 = sum J [(tempf - meanf)/bottomf - (tempg - meang)/bottomg]; the
+      // 6-DOF f-side sums come from the set-up stage (read here, not held
+      // in registers across the pixel pass)
+      if constexpr (!TWO) {
 #pragma unroll
-        for (int q = 0; q < 6; ++q) { bsum[2 * q] = k[q].s; bsum[2 * q + 1] = -k[q].c; }
-        tm.template sumf<12>(bsum, fscr);
+        for (int k = 0; k < NQ; ++k) { jf[k] = ctl->jf[k]; j1[k] = ctl->j1[k]; }
+      }
+      float b2[NQ];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        const float jg = red[7 + 2 * k] + red[8 + 2 * k];
+        b2[k] = jf[k] * ibf - (jg - meang * j1[k]) * ibg;
       }
       // convergence test (FP32) and the FP64 update, identical on every warp
       int done = 0;
       float nb = 0.f;
-      double D[6] = {0, 0, 0, 0, 0, 0};
+      float D[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       if constexpr (TWO) {
-        const float b0 = bottomf * (bsum[0] + bsum[1]), b1 = bottomf * (bsum[2] + bsum[3]);
+        const float b0 = bottomf * b2[0], b1 = bottomf * b2[1];
         const float sc2 = 2.f / (bottomf * bottomf);
-        const float tb0 = b0 * sc2 + (float)(a.mu * (P[4] - a.UOld[2 * item] - a.vdual[2 * item]));
-        const float tb1 = b1 * sc2 + (float)(a.mu * (P[5] - a.UOld[2 * item + 1] - a.vdual[2 * item + 1]));
+        const float tb0 = b0 * sc2 + (float)a.mu * (P[4] - uold0 - vd0);
+        const float tb1 = b1 * sc2 + (float)a.mu * (P[5] - uold1 - vd1);
         nb = tb0 * tb0 + tb1 * tb1;
-        D[4] = -(i00 * (double)tb0 + i01 * (double)tb1);
-        D[5] = -(i10 * (double)tb0 + i11 * (double)tb1);
+        // FP64 2x2 solve: lane 0 forms DeltaP_5, lane 1 DeltaP_6
+        const double t0 = (double)tb0, t1 = (double)tb1;
+        const double dk = lane == 0 ? -(i00 * t0 + i01 * t1) : -(i10 * t0 + i11 * t1);
+        const float dkf = (float)dk;
+        D[4] = __shfl_sync(0xffffffffu, dkf, 0);
+        D[5] = __shfl_sync(0xffffffffu, dkf, 1);
       } else {
         float b[6];
 #pragma unroll
-        for (int q = 0; q < 6; ++q) { b[q] = bottomf * (bsum[2 * q] + bsum[2 * q + 1]); nb += b[q] * b[q]; }
+        for (int q = 0; q < 6; ++q) { b[q] = bottomf * b2[q < NQ ? q : 0]; nb += b[q] * b[q]; }
         if (hok) {
-          double dk = 0;
+          // FP64 solve DeltaP = -H^-1 b: lane q converts b_q, lane k forms row k
+          const double* hr = ctl->Hm + (lane < 6 ? lane : 0) * 6;
 #pragma unroll
-          for (int q = 0; q < 6; ++q) dk += hinv[q] * (double)b[q];
+          for (int k = 0; k < 6; ++k) hinv[k] = hr[k];
+          float bl = 0.f;
 #pragma unroll
-          for (int q = 0; q < 6; ++q) D[q] = -shfl_d(dk, q);
+          for (int q = 0; q < 6; ++q)
+            if (lane == q) bl = b[q];
+          const double bd = (double)bl;
+          double bb[6];
+#pragma unroll
+          for (int q = 0; q < 6; ++q) bb[q] = shfl_d(bd, q);
+          // depth-3 tree for the row dot product
+          const double d01 = fma(hinv[1], bb[1], hinv[0] * bb[0]);
+          const double d23 = fma(hinv[3], bb[3], hinv[2] * bb[2]);
+          const double d45 = fma(hinv[5], bb[5], hinv[4] * bb[4]);
+          const double dk = (d01 + d23) + d45;
+          const float dkf = (float)(-dk);
+#pragma unroll
+          for (int q = 0; q < 6; ++q) D[q] = __shfl_sync(0xffffffffu, dkf, q);
         } else {
-          double bd[6];
-#pragma unroll
-          for (int q = 0; q < 6; ++q) bd[q] = (double)b[q];
-          small_solve(ctl->Hm, bd, 6, D);
-#pragma unroll
-          for (int q = 0; q < 6; ++q) D[q] = -D[q];
+          singular_solve6(B.H6 + (size_t)item * 21, b, D);
         }
       }
       float nN = sqrtf(nb);
@@ -738,8 +914,9 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
       normAbs = nA;
       if (nN < tolf || nA < tolf) done = 1;
       else if (!compose_warp(P, D, lane)) done = 2;
+      else ++nupd;
       if (done) break;
-      oob = corners_oob_warp(P, x0, y0, x1, y1, mx, my, a.W, a.H, lane);
+      oob = corners_oob_warp(P, (int)x0, (int)y0, (int)x1, (int)y1, mx, my, a.W, a.H, lane);
     }
     if (run) {
       if (err) { code = err_code; nan_out = true; }
@@ -758,63 +935,109 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
     }
     if (tm.tl == 0) {
       a.conv[item] = code;
-      a.U[2 * item] = nan_out ? nan("") : P[4];
-      a.U[2 * item + 1] = nan_out ? nan("") : P[5];
+      // a subset that never updated P returns its initial guess bit-exactly
+      const bool moved = nupd > 0;
+      if constexpr (TWO) {
+        a.U[2 * item] = nan_out ? nan("") : (moved ? (double)P[4] : a.UOld[2 * item]);
+        a.U[2 * item + 1] = nan_out ? nan("") : (moved ? (double)P[5] : a.UOld[2 * item + 1]);
+      } else {
+        a.U[2 * item] = nan_out ? nan("") : (moved ? (double)P[4] : a.U0[2 * item]);
+        a.U[2 * item + 1] = nan_out ? nan("") : (moved ? (double)P[5] : a.U0[2 * item + 1]);
+      }
       if constexpr (!TWO) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) a.F[4 * item + k] = nan_out ? nan("") : P[k];
-        if (a.Hpk) {
-          int q = 0;
-          const bool hv = hdone && !nan_out && code != kMaxIter + 2;
-          for (int col = 0; col < 6; ++col)
-            for (int row = col; row < 6; ++row)
-              a.Hpk[(size_t)q++ * Ntot + item] = hv ? ctl->Hm[row * 6 + col] : 0.0;
-        }
+        for (int k = 0; k < 4; ++k) a.F[4 * item + k] = nan_out ? nan("") : (double)P[k];
+        if (a.Hpk && nan_out)
+          for (int q = 0; q < 21; ++q) a.Hpk[(size_t)q * Ntot + item] = 0.0;
       }
     }
     tm.sync();
   }
 }
 
-template <int TW, bool TWO>
+// FP64 Cholesky factorisation and inverse of each subset's 6x6 Hessian, one
+// thread per subset (between the set-up and iteration stages).  A matrix whose
+// factorisation fails gets Hinv6[0] = NaN; the iteration stage then solves
+// with LU and pivoting as MATLAB's mldivide does for such a matrix.
+__global__ void __launch_bounds__(128) factor6_kernel(const SubsetState6* __restrict__ st,
+                                                      const double* __restrict__ H6,
+                                                      double* __restrict__ Hinv6, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n || st[t].code != 0) return;
+  double H[21];
+#pragma unroll
+  for (int k = 0; k < 21; ++k) H[k] = H6[(size_t)t * 21 + k];
+  Chol6 C;
+  chol6_factor(H, C);
+  double* out = Hinv6 + (size_t)t * 36;
+  if (!C.ok) {
+    out[0] = nan("");
+    return;
+  }
+#pragma unroll
+  for (int col = 0; col < 6; ++col) {
+    double e[6], x[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) e[k] = k == col ? 1.0 : 0.0;
+    chol6_solve(C, e, x);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) out[r * 6 + col] = x[r];
+  }
+}
+
+cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hinv6, int n,
+                           cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  factor6_kernel<<<(n + 127) / 128, 128, 0, s>>>(st, H6, Hinv6, n);
+  return cudaGetLastError();
+}
+
+template <int TW, bool TWO, int STAGE>
 static cudaError_t launch_tw(const BatchedArgs& b, int blocks, int threads, cudaStream_t s) {
   const int teams = threads / (TW * 32);
   const size_t smem = batched_team_bytes(b.smem_px, TWO, TW) * teams;
   if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
-  cudaError_t e = cudaFuncSetAttribute(icgn_batched_kernel<TW, TWO>,
+  cudaError_t e = cudaFuncSetAttribute(icgn_batched_kernel<TW, TWO, STAGE>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  icgn_batched_kernel<TW, TWO><<<blocks, threads, smem, s>>>(b);
+  icgn_batched_kernel<TW, TWO, STAGE><<<blocks, threads, smem, s>>>(b);
   return cudaGetLastError();
 }
 
+template <int TW>
+static cudaError_t launch_stage(const BatchedArgs& b, int blocks, int threads, cudaStream_t s) {
+  if (b.two_dof) return launch_tw<TW, true, 0>(b, blocks, threads, s);
+  return b.stage == 1 ? launch_tw<TW, false, 1>(b, blocks, threads, s)
+                      : launch_tw<TW, false, 2>(b, blocks, threads, s);
+}
+
 cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, cudaStream_t s) {
-  const bool two = b.two_dof != 0;
   switch (b.warps_per_subset) {
-    case 1: return two ? launch_tw<1, true>(b, blocks, threads, s) : launch_tw<1, false>(b, blocks, threads, s);
-    case 2: return two ? launch_tw<2, true>(b, blocks, threads, s) : launch_tw<2, false>(b, blocks, threads, s);
-    case 4: return two ? launch_tw<4, true>(b, blocks, threads, s) : launch_tw<4, false>(b, blocks, threads, s);
+    case 1: return launch_stage<1>(b, blocks, threads, s);
+    case 2: return launch_stage<2>(b, blocks, threads, s);
+    case 4: return launch_stage<4>(b, blocks, threads, s);
   }
   return cudaErrorInvalidValue;
 }
 
-// Resident blocks per SM of one configuration (for grid sizing and the autotuner).
+// Resident blocks per SM of one configuration (for grid sizing and the
+// autotuner); the iteration stage (or the fused 2-DOF form) is the reference.
 int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px) {
   const int teams = threads / (tw * 32);
   const size_t smem = batched_team_bytes(smem_px, two, tw) * teams;
   if (smem > 227 * 1024) return 0;
   int nb = 0;
   cudaError_t e = cudaSuccess;
-#define STDIC_OCC(TWv, TWOv)                                                                 \
-  e = cudaFuncSetAttribute(icgn_batched_kernel<TWv, TWOv>,                                   \
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);          \
-  if (e == cudaSuccess)                                                                      \
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, icgn_batched_kernel<TWv, TWOv>,   \
+#define STDIC_OCC(TWv, TWOv, STv)                                                                \
+  e = cudaFuncSetAttribute(icgn_batched_kernel<TWv, TWOv, STv>,                                  \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);              \
+  if (e == cudaSuccess)                                                                          \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, icgn_batched_kernel<TWv, TWOv, STv>,  \
                                                       threads, smem);
   switch (tw) {
-    case 1: if (two) { STDIC_OCC(1, true) } else { STDIC_OCC(1, false) } break;
-    case 2: if (two) { STDIC_OCC(2, true) } else { STDIC_OCC(2, false) } break;
-    case 4: if (two) { STDIC_OCC(4, true) } else { STDIC_OCC(4, false) } break;
+    case 1: if (two) { STDIC_OCC(1, true, 0) } else { STDIC_OCC(1, false, 2) } break;
+    case 2: if (two) { STDIC_OCC(2, true, 0) } else { STDIC_OCC(2, false, 2) } break;
+    case 4: if (two) { STDIC_OCC(4, true, 0) } else { STDIC_OCC(4, false, 2) } break;
     default: return 0;
   }
 #undef STDIC_OCC

@@ -59,7 +59,28 @@ struct BatchedArgs {
   long long g_stride;     // elements between stacked deformed frames
   unsigned char* scratch; // per-team global slices for tiles that exceed the shared slot
   int smem_px;            // tile pixels each team keeps in shared memory
+  // 6-DOF split: stage 1 = per-subset set-up (writes st6, H6), stage 2 =
+  // iterations (reads st6, Hinv6); the 2-DOF form runs fused (stage 0)
+  int stage;
+  void* st6;              // SubsetState6 per item
+  double* H6;             // 21 per item: packed lower Hessian (row-major)
+  double* Hinv6;          // 36 per item: inverse Hessian (row-major), Hinv6[0] = NaN if singular
 };
+
+// Per-subset state handed from the 6-DOF set-up stage to the iterations.
+struct SubsetState6 {
+  int code;      // 0: iterate; otherwise the final ConvItPerEle (outputs already written)
+  int ws;        // subset size after window growth
+  int cntf;      // zero pixels of tempf in the original window
+  int masked;    // 1 when the mask tile has a zero (tempf/DfDx/DfDy use the 4-conn selection)
+  float meanf, bottomf, sabs, pad;
+  // f-side parts of the b-vector, constant over the iterations:
+  // Jf = sum J (tempf - meanf), J1 = sum J, with J the steepest-descent images
+  float Jf[6], J1[6];
+};
+
+cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hinv6, int n,
+                           cudaStream_t s);
 
 // Size of one team's shared slot / global slice of the batched kernel.
 size_t batched_team_bytes(int sm_px, bool two, int tw);
@@ -80,7 +101,7 @@ cudaError_t launch_badpoints(int32_t* conv, int N, double* U, double* F, int two
                              int* badnum_dev, cudaStream_t s);
 cudaError_t launch_to_f32(const double* in, float* out, long long n, cudaStream_t s);
 cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int ws_all, int N,
-                               int32_t* order, int* scratch, cudaStream_t s);
+                               int32_t* order, int* scratch, cudaStream_t s, int ascending = 0);
 cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, cudaStream_t s);
 
 // Subpb2 (FEM).  All pointers are device pointers.

@@ -402,7 +402,8 @@ cudaError_t launch_to_f32(const double* in, float* out, long long n, cudaStream_
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) build_queue_kernel(const int32_t* __restrict__ ws_list,
                                                            const int32_t* __restrict__ wsl2,
-                                                           int ws_all, int N, int32_t* order) {
+                                                           int ws_all, int N, int32_t* order,
+                                                           int ascending) {
   __shared__ int hist[256];
   __shared__ int start[256];
   for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
@@ -411,7 +412,8 @@ __global__ void __launch_bounds__(1024) build_queue_kernel(const int32_t* __rest
     int w = ws_all;
     if (wsl2) w = max(wsl2[k], wsl2[N + k]);
     else if (ws_list) w = ws_list[k];
-    return 255 - min(max(w, 0), 255);  // larger subsets first
+    const int b = min(max(w, 0), 255);
+    return ascending ? b : 255 - b;  // larger subsets first unless ascending
   };
   for (int k = threadIdx.x; k < N; k += blockDim.x) atomicAdd(&hist[key(k)], 1);
   __syncthreads();
@@ -427,10 +429,10 @@ __global__ void __launch_bounds__(1024) build_queue_kernel(const int32_t* __rest
 }
 
 cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int ws_all, int N,
-                               int32_t* order, int* scratch, cudaStream_t s) {
+                               int32_t* order, int* scratch, cudaStream_t s, int ascending) {
   (void)scratch;
   if (N <= 0) return cudaSuccess;
-  build_queue_kernel<<<1, 1024, 0, s>>>(ws_list, wsl2, ws_all, N, order);
+  build_queue_kernel<<<1, 1024, 0, s>>>(ws_list, wsl2, ws_all, N, order, ascending);
   return cudaGetLastError();
 }
 

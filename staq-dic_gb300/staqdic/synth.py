@@ -324,10 +324,12 @@ def quadtree_mesh(W, H, winsize, winstepsize, size_fn, min_size, hole_fn=None):
 
 
 def node_sizes(coords, elems, sizes):
-    """Smallest incident element size per node (nodes of dropped elements get
-    the size of the smallest element touching them, or the largest size)."""
+    """Smallest incident element size per node; nodes that no element touches
+    (inside a hole) get the smallest element size of the mesh."""
     N = coords.shape[0]
-    out = np.full(N, sizes.max() if sizes.size else 0.0)
+    big = sizes.max() if sizes.size else 0.0
+    out = np.full(N, np.inf)
     for k in range(4):
         np.minimum.at(out, elems[:, k] - 1, sizes)
+    out[~np.isfinite(out)] = sizes.min() if sizes.size else big
     return out

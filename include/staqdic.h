@@ -182,6 +182,26 @@ int stdic_subpb2(stdic_ctx* ctx, const double* coords, int N, const int32_t* ele
                  double alpha, double winstepsize, double tol, int maxit, double* Uhat,
                  int* iters);
 
+/* No reference counterpart.  stdic_subpb2 without a context and without any
+ * device allocation, for callers that cannot allocate when the global step
+ * runs (a caching allocator holding nearly all of HBM, a loop that must not
+ * take cudaFree's synchronisation, a host that reserves memory once).  The
+ * scratch is a 16 MiB __device__ array in the library (per device, once its
+ * module is loaded); a mesh needing more returns STDIC_E_NOMEM.  Every array
+ * must be device memory of the current device; the call runs on cuda_stream
+ * (NULL: the default stream) and returns after that stream has finished it.
+ * iters (host, may be NULL) receives the PCG count; err (may be NULL) receives
+ * a message of at most err_len bytes.  Two calls in flight on one device at
+ * once race on the shared array: serialise them.  The first call on each
+ * device looks the array up (cudaGetSymbolAddress): make it before any stream
+ * capture begins. */
+int stdic_subpb2_noalloc(const double* coords, int N, const int32_t* elems, int E,
+                         const int32_t* dirichlet, int nd, const double* neumann, int nn,
+                         int gauss_order, double beta, double mu, const double* U,
+                         const double* F, double alpha, double winstepsize, double tol,
+                         int maxit, double* Uhat, int* iters, void* cuda_stream, char* err,
+                         int err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,7 +30,7 @@ EXPORTS = [
     "stdic_ctx_create", "stdic_ctx_destroy", "stdic_ctx_set_stream", "stdic_last_error",
     "stdic_kernel_launches", "stdic_last_solver_ms", "stdic_interp_bicubic", "stdic_img_gradient",
     "stdic_integer_search_grid", "stdic_integer_search", "stdic_icgn_subsets", "stdic_icgn_local",
-    "stdic_subpb1_subsets", "stdic_subpb1", "stdic_subpb2",
+    "stdic_subpb1_subsets", "stdic_subpb1", "stdic_subpb2", "stdic_subpb2_noalloc",
 ]
 
 
@@ -90,6 +90,10 @@ def load(build_if_missing=True):
     L.stdic_subpb2.argtypes = [_vp, _vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int,
                                _c.c_int, _c.c_double, _c.c_double, _vp, _vp, _c.c_double,
                                _c.c_double, _c.c_double, _c.c_int, _vp, _vp]
+    L.stdic_subpb2_noalloc.argtypes = [_vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int,
+                                       _c.c_int, _c.c_double, _c.c_double, _vp, _vp, _c.c_double,
+                                       _c.c_double, _c.c_double, _c.c_int, _vp, _vp, _vp, _c.c_char_p,
+                                       _c.c_int]
     for name in EXPORTS:
         if name not in ("stdic_last_error", "stdic_kernel_launches", "stdic_last_solver_ms"):
             getattr(L, name).restype = _c.c_int

@@ -210,6 +210,33 @@ def icgn2(UOld, FOld, vdual, coords, Df, ImgRef, ImgDef, winsize_list, mu, tol):
     return U, conv
 
 
+def icgn_adjoint(ImgRef, ImgDef, mask, coords, winsize, U, F, want_dg=True):
+    """Subset ZNSSD costs and their gradients (FP64; no reference counterpart).
+
+    Returns cost (N), dU (2N), dF (4N) and dg (W x H, None unless want_dg)."""
+    W, H = ImgRef.shape
+    coords = _F(coords)
+    N = coords.shape[0]
+    f, g = _F(ImgRef), _F(ImgDef)
+    msk = None if mask is None else _F(mask, np.uint8)
+    wsa = np.atleast_1d(np.asarray(winsize))
+    if wsa.size == 1:
+        wl, ws0 = None, int(wsa[0])
+    else:
+        wl, ws0 = np.ascontiguousarray(wsa, dtype=np.int32), 0
+    c = lambda a: np.ascontiguousarray(a, dtype=np.float64).ravel()
+    U, F = c(U), c(F)
+    cost = np.empty(N)
+    dU = np.empty(2 * N)
+    dF = np.empty(4 * N)
+    dg = np.zeros((W, H), order="F") if want_dg else None
+    lib().orc_adjoint(_p(f, _d), _p(g, _d), _p(msk, _u8) if msk is not None else None, _L(W), _L(H),
+                      _p(coords, _d), _L(N), int(ws0), (_p(wl, _i32) if wl is not None else None),
+                      _p(U, _d), _p(F, _d), _p(cost, _d), _p(dU, _d), _p(dF, _d),
+                      _p(dg, _d) if want_dg else None)
+    return cost, dU, dF, dg
+
+
 def bad_points_local(conv, maxIterNum=100):
     """LocalICGNQuadtree.m:153-169 -> (bad index array, LocalICGNBadPtNum)."""
     conv = np.asarray(conv)

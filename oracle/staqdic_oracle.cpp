@@ -15,6 +15,8 @@
 //                         func_quadtree/LocalICGNQuadtree.m:67-147
 //   orc_icgn2             func/funICGN_Subpb1.m:34-471 driven as in
 //                         func_quadtree/Subpb1Quadtree.m:75-169
+//   orc_adjoint           no counterpart: gradient of the ZNSSD subset cost of
+//                         funICGNQuadtree.m:151-165 (pinned by finite differences)
 //   orc_subpb2_assemble   func_quadtree/Subpb2Quadtree.m:30-336 (element loop,
 //                         sparse triplets, Dirichlet lift); the linear solve of
 //                         :339 is done by the Python side with a direct solver.
@@ -1012,6 +1014,136 @@ extern "C" void orc_integer_search(const double* f, const double* g, long W, lon
     peak_rc[npt + o] = pc;
     x[o] = (double)(ii + ii + wsx) / 2;
     y[o] = (double)(jj + jj + wsy) / 2;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint of the subset ZNSSD cost (no counterpart in the reference).  The cost
+// is the criterion funICGNQuadtree.m minimises, taken on the square window:
+//   C_n = sum_i (a_i - b_i)^2,   a = (f - fbar) / |f - fbar|,
+//   b = (t - tbar) / |t - tbar|,  t_i = ba_interp2 cubic of ImgDef at the warp
+//   of funICGNQuadtree.m:151-152 with P = [F11 F21 F12 F22 u v] of the node.
+// Window pixels with mask 0 or outside the image are left out.  With
+// rho = sum a b, C = 2 - 2 rho and dC/dt_i = -2 (a_i - rho b_i) / |t - tbar|;
+// the chain through the Keys weights (ba_interp2.cpp:184-234, clamped taps)
+// gives dC/dP and dC/dg.  A subset with fewer than 2 pixels or a constant f or
+// t window has cost NaN and no gradient.
+// ---------------------------------------------------------------------------
+static inline void keys_weights(double d, double w[4], double dw[4]) {
+  const double dd = d * d, ddd = dd * d;
+  w[0] = 0.5 * (-d + 2.0 * dd - ddd);
+  w[1] = 0.5 * (2.0 - 5.0 * dd + 3.0 * ddd);
+  w[2] = 0.5 * (d + 4.0 * dd - 3.0 * ddd);
+  w[3] = 0.5 * (-dd + ddd);
+  dw[0] = 0.5 * (-1.0 + 4.0 * d - 3.0 * dd);
+  dw[1] = 0.5 * (-10.0 * d + 9.0 * dd);
+  dw[2] = 0.5 * (1.0 + 8.0 * d - 9.0 * dd);
+  dw[3] = 0.5 * (-2.0 * d + 3.0 * dd);
+}
+
+// Bicubic value and its derivatives along dim 1 (x) and dim 2 (y) at the
+// 1-based point (xc, yc); tap k = a + 4 b has index idx[k] and weight wt[k].
+static double cubic_with_grad(const double* G, long W, long H, double xc, double yc, double* gx,
+                              double* gy, long idx[16], double wt[16]) {
+  const double xf = std::floor(xc), yf = std::floor(yc);
+  double wx[4], dwx[4], wy[4], dwy[4];
+  keys_weights(xc - xf, wx, dwx);
+  keys_weights(yc - yf, wy, dwy);
+  double t = 0, tx = 0, ty = 0;
+  for (int b = 0; b < 4; ++b) {
+    long cy = (long)yf - 2 + b;
+    cy = cy < 0 ? 0 : (cy >= H ? H - 1 : cy);
+    for (int a = 0; a < 4; ++a) {
+      long cx = (long)xf - 2 + a;
+      cx = cx < 0 ? 0 : (cx >= W ? W - 1 : cx);
+      const long k = cx + W * cy;
+      const double v = G[k];
+      t += wx[a] * wy[b] * v;
+      tx += dwx[a] * wy[b] * v;
+      ty += wx[a] * dwy[b] * v;
+      idx[a + 4 * b] = k;
+      wt[a + 4 * b] = wx[a] * wy[b];
+    }
+  }
+  *gx = tx;
+  *gy = ty;
+  return t;
+}
+
+static double adjoint_one(const double* f, const double* g, const uint8_t* mask, long W, long H,
+                          long x0, long y0, int ws, const double P[6], double dP[6], double* dg) {
+  const int h = ws / 2;
+  std::vector<double> fv, tv, gxv, gyv, wtv;
+  std::vector<long> dxv, dyv, idxv;
+  for (int j = -h; j <= h; ++j)
+    for (int i = -h; i <= h; ++i) {
+      const long x = x0 + i, y = y0 + j;
+      if (x < 1 || x > W || y < 1 || y > H) continue;
+      if (mask && !mask[(x - 1) + W * (y - 1)]) continue;
+      const double xw = (double)x0 + i + P[0] * i + P[2] * j + P[4];
+      const double yw = (double)y0 + j + P[1] * i + P[3] * j + P[5];
+      long idx[16];
+      double wt[16], gx, gy;
+      const double t = cubic_with_grad(g, W, H, xw, yw, &gx, &gy, idx, wt);
+      fv.push_back(f[(x - 1) + W * (y - 1)]);
+      tv.push_back(t);
+      gxv.push_back(gx);
+      gyv.push_back(gy);
+      dxv.push_back(i);
+      dyv.push_back(j);
+      idxv.insert(idxv.end(), idx, idx + 16);
+      wtv.insert(wtv.end(), wt, wt + 16);
+    }
+  for (int k = 0; k < 6; ++k) dP[k] = 0;
+  const size_t n = fv.size();
+  if (n < 2) return NAN;
+  double fm = 0, tm = 0;
+  for (size_t i = 0; i < n; ++i) { fm += fv[i]; tm += tv[i]; }
+  fm /= (double)n;
+  tm /= (double)n;
+  double sf = 0, st = 0, sft = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const double a = fv[i] - fm, b = tv[i] - tm;
+    sf += a * a;
+    st += b * b;
+    sft += a * b;
+  }
+  if (!(sf > 0) || !(st > 0) || !std::isfinite(st)) return NAN;
+  const double df = std::sqrt(sf), dt = std::sqrt(st);
+  const double rho = sft / (df * dt);
+  double cost = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const double a = (fv[i] - fm) / df, b = (tv[i] - tm) / dt;
+    cost += (a - b) * (a - b);
+    const double w = -2.0 * (a - rho * b) / dt;
+    const double wx = w * gxv[i], wy = w * gyv[i];
+    dP[0] += wx * dxv[i];
+    dP[1] += wy * dxv[i];
+    dP[2] += wx * dyv[i];
+    dP[3] += wy * dyv[i];
+    dP[4] += wx;
+    dP[5] += wy;
+    if (dg)
+      for (int k = 0; k < 16; ++k) dg[idxv[16 * i + k]] += w * wtv[16 * i + k];
+  }
+  return cost;
+}
+
+// cost (N), dU (2N), dF (4N) and dg (W x H, accumulated) may be NULL except cost.
+extern "C" void orc_adjoint(const double* f, const double* g, const uint8_t* mask, long W, long H,
+                            const double* coords, long N, int ws_all, const int32_t* ws_list,
+                            const double* U, const double* F, double* cost, double* dU, double* dF,
+                            double* dg) {
+#pragma omp parallel for schedule(dynamic, 16) if (!dg)
+  for (long n = 0; n < N; ++n) {
+    const long x0 = (long)std::round(coords[n]), y0 = (long)std::round(coords[N + n]);
+    const int ws = ws_list ? ws_list[n] : ws_all;
+    const double P[6] = {F[4 * n], F[4 * n + 1], F[4 * n + 2], F[4 * n + 3], U[2 * n], U[2 * n + 1]};
+    double dP[6];
+    cost[n] = adjoint_one(f, g, mask, W, H, x0, y0, ws, P, dP, dg);
+    if (dF)
+      for (int k = 0; k < 4; ++k) dF[4 * n + k] = dP[k];
+    if (dU) { dU[2 * n] = dP[4]; dU[2 * n + 1] = dP[5]; }
   }
 }
 

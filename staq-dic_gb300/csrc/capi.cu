@@ -3,6 +3,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -20,15 +22,15 @@ struct stdic_ctx {
   cudaStream_t stream = nullptr;
   void* ws = nullptr;
   size_t ws_size = 0;
-  int* scal = nullptr;  // device scalars: [0] queue head, [1] badnum, [2] iters, [3] status
+  int* scal = nullptr;  // device scalars: [1] badnum, [2] iters, [3] status, [4..5] queue heads, [6] queue split
   double* scald = nullptr;  // device double scalars: [0] residual
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t es0 = nullptr, es1 = nullptr;  // around the last IC-GN solver kernel
   bool solver_timed = false;
   std::string err;
   long long launches = 0;
-  // autotuner cache: (N bucket, npx_max, two_dof, frames) -> (warps per subset, threads)
-  std::map<std::tuple<int, int, int, int>, std::pair<int, int>> tune;
+  // autotuner cache: (N bucket, npx_max, two_dof, frames) -> index of the launch shape
+  std::map<std::tuple<int, int, int, int>, int> tune;
   int tuning = 1;
 };
 
@@ -391,27 +393,37 @@ bool frame_ok(const stdic_frame* fr) {
 // Candidate launch shapes of the persistent batched kernel: (warps per
 // subset, threads per CTA), each with its resident grid, its shared tile slot
 // and the global scratch its teams need.
+// split > 0: subsets of at least `split` pixels a side run on teams of tw
+// warps, the rest on single warps (queue in decreasing size).
 struct BatchedCand {
-  int tw, threads, blocks, smem_px;
+  int tw, threads, split, smem_per_warp, blocks, smem_px, smem_px_small;
   size_t scratch;
 };
 
 std::vector<BatchedCand> batched_candidates(stdic_ctx* c, bool two, int npx_max, int Ntot) {
   std::vector<BatchedCand> out;
-  const std::pair<int, int> shapes[] = {{1, 128}, {1, 256}, {2, 256}, {4, 256}};
-  for (auto sh : shapes) {
-    const int tw = sh.first, threads = sh.second;
+  // (warps per team, threads, split size, shared bytes per warp).  A smaller
+  // shared slot leaves more of the SM's unified L1 to cache the gathers of g
+  // and the gradients; tiles that do not fit use the warp's global slice.
+  const int shapes[][4] = {{1, 128, 0, 12800}, {1, 256, 0, 12800}, {2, 256, 0, 12800},
+                           {4, 256, 0, 12800}, {4, 256, 32, 12800}, {4, 256, 64, 12800},
+                           {8, 256, 64, 12800}, {1, 256, 0, 4800},   {4, 256, 64, 4800},
+                           {1, 256, 0, 2800},  {4, 256, 64, 2800}};
+  for (auto& sh : shapes) {
+    const int tw = sh[0], threads = sh[1], split = sh[2], per_warp = sh[3];
     const int teams_per_block = threads / (32 * tw);
-    // shared slot sized for about 12.5 KB per team (16 resident warps per SM)
     const int bpp = two ? 12 : 8;
-    int smem_px = (int)((12800 * tw - 512 - 32 * 4 * tw) / bpp);
+    int smem_px = (int)((per_warp * tw - 512 - 32 * 4 * tw) / bpp);
     smem_px = std::max(64, std::min(smem_px, npx_max));
     const int per_sm = stdic::batched_blocks_per_sm(tw, two, threads, smem_px);
     if (per_sm <= 0) continue;
     int blocks = c->nsm * per_sm;
-    blocks = std::max(1, std::min(blocks, (Ntot + teams_per_block - 1) / teams_per_block));
-    const long long teams = (long long)blocks * teams_per_block;
-    out.push_back({tw, threads, blocks, smem_px, stdic::batched_scratch_bytes(npx_max, two, teams)});
+    const int units_per_block = split ? threads / 32 : teams_per_block;
+    blocks = std::max(1, std::min(blocks, (Ntot + units_per_block - 1) / units_per_block));
+    const long long warps = (long long)blocks * (threads / 32);
+    const int small_px = split ? stdic::batched_small_px(smem_px, two, tw) : 0;
+    out.push_back({tw, threads, split, per_warp, blocks, smem_px, small_px,
+                   stdic::batched_scratch_bytes(npx_max, two, warps)});
   }
   return out;
 }
@@ -425,19 +437,48 @@ size_t batched_scratch_need(const std::vector<BatchedCand>& cs) {
 // Run the persistent batched kernel with the autotuned launch shape.  On a new
 // problem class every candidate is timed once on the real data (the outputs
 // are idempotent) and the fastest is cached in the context.
-int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector<BatchedCand>& cands) {
+// STDIC_TUNE_LOG=1 prints the autotuner's timing of every candidate to stderr.
+bool tune_log() {
+  static const bool on = [] {
+    const char* e = std::getenv("STDIC_TUNE_LOG");
+    return e && e[0] == '1';
+  }();
+  return on;
+}
+
+// Subset sizes the work queue is sorted by (one of ws_list, wsl2, ws_all).
+struct QueueKeys {
+  const int32_t* ws_list;
+  const int32_t* wsl2;
+  int ws_all;
+};
+
+int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector<BatchedCand>& cands,
+                const QueueKeys& qk) {
   const bool two = b.two_dof != 0;
   if (cands.empty()) return fail(c, STDIC_E_UNSUPPORTED, "no launch shape fits this subset size");
+  b.queue_head = c->scal + 4;  // [4] team phase, [5] single-warp phase
+  b.n_big = c->scal + 6;
   auto launch = [&](const BatchedCand& cd) -> int {
     b.warps_per_subset = cd.tw;
     b.smem_px = cd.smem_px;
+    b.split = cd.split > 0 ? 1 : 0;
+    b.smem_px_small = cd.smem_px_small;
+    // Single warps take the queue smallest first, so that the small subsets
+    // that run to the iteration limit start early; split teams take the large
+    // subsets largest first, then single warps the rest smallest first.
+    int rc = check_launch(c, stdic::launch_build_queue(qk.ws_list, qk.wsl2, qk.ws_all, b.a.N,
+                                                       (int32_t*)b.order, c->scal + 6, c->stream,
+                                                       cd.split ? 2 : (cd.tw == 1 ? 1 : 0), cd.split),
+                          "queue");
+    if (rc) return rc;
     // 2-DOF: one fused pass; 6-DOF: set-up, FP64 factorisation, iterations
     const int stages[2] = {two ? 0 : 1, 2};
     for (int k = 0; k < (two ? 1 : 2); ++k) {
-      cudaError_t e = cudaMemsetAsync(b.queue_head, 0, sizeof(int), c->stream);
+      cudaError_t e = cudaMemsetAsync(b.queue_head, 0, 2 * sizeof(int), c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "queue reset");
       b.stage = stages[k];
-      int rc = check_launch(c, stdic::launch_icgn_batched(b, cd.blocks, cd.threads, c->stream), "IC-GN batched");
+      rc = check_launch(c, stdic::launch_icgn_batched(b, cd.blocks, cd.threads, c->stream), "IC-GN batched");
       if (rc) return rc;
       if (!two && k == 0) {
         rc = check_launch(c, stdic::launch_factor6((const stdic::SubsetState6*)b.st6, b.H6, b.Hinv6, Ntot, c->stream),
@@ -451,7 +492,7 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
   const auto key = std::make_tuple(nb, b.a.npx_max, (int)two, b.frames);
   auto it = c->tune.find(key);
   if (it == c->tune.end()) {
-    std::pair<int, int> best{cands[0].tw, cands[0].threads};
+    int best = 0;
     if (c->tuning && Ntot > 0 && cands.size() > 1) {
       float bt = 1e30f;
       for (auto& cd : cands) {
@@ -462,14 +503,15 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
         cudaEventSynchronize(c->ev1);
         float ms = 0;
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-        if (ms < bt) { bt = ms; best = {cd.tw, cd.threads}; }
+        if (ms < bt) { bt = ms; best = (int)(&cd - cands.data()); }
+        if (tune_log())
+          std::fprintf(stderr, "stdic tune: N=%d two=%d warps/team=%d threads=%d split=%d smem/warp=%d blocks=%d smem_px=%d: %.3f ms\n",
+                       Ntot, (int)two, cd.tw, cd.threads, cd.split, cd.smem_per_warp, cd.blocks, cd.smem_px, ms);
       }
     }
     it = c->tune.emplace(key, best).first;
   }
-  const BatchedCand* chosen = &cands[0];
-  for (auto& cd : cands)
-    if (cd.tw == it->second.first && cd.threads == it->second.second) chosen = &cd;
+  const BatchedCand* chosen = &cands[std::min<size_t>((size_t)it->second, cands.size() - 1)];
   cudaEventRecord(c->es0, c->stream);
   const int rc = launch(*chosen);
   cudaEventRecord(c->es1, c->stream);
@@ -533,15 +575,14 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
       c->solver_timed = rc == STDIC_OK;
     } else {
       rc = convert_frame(c, fr, &d, 1);
-      if (!rc) rc = check_launch(c, stdic::launch_build_queue(a.ws_list, nullptr, winsize, N, order, nullptr, c->stream, 1), "queue");
       if (!rc) {
         stdic::BatchedArgs b{};
         b.a = a;
         b.f32 = d.f32; b.g32 = d.g32; b.dfdx32 = d.dfdx32; b.dfdy32 = d.dfdy32;
-        b.order = order; b.queue_head = c->scal; b.two_dof = 0; b.frames = 1; b.g_stride = 0;
+        b.order = order; b.two_dof = 0; b.frames = 1; b.g_stride = 0;
         b.scratch = bscr;
         b.st6 = st6; b.H6 = H6; b.Hinv6 = Hinv6;
-        rc = run_batched(c, b, N, cands);
+        rc = run_batched(c, b, N, cands, QueueKeys{a.ws_list, nullptr, winsize});
       }
     }
     if (rc) return rc;
@@ -655,14 +696,13 @@ static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, 
       c->solver_timed = rc == STDIC_OK;
     } else {
       rc = convert_frame(c, fr, &d, 1);
-      if (!rc) rc = check_launch(c, stdic::launch_build_queue(nullptr, a.wsl2, 0, N, order, nullptr, c->stream, 1), "queue");
       if (!rc) {
         stdic::BatchedArgs b{};
         b.a = a;
         b.f32 = d.f32; b.g32 = d.g32; b.dfdx32 = d.dfdx32; b.dfdy32 = d.dfdy32;
-        b.order = order; b.queue_head = c->scal; b.two_dof = 1; b.frames = 1; b.g_stride = 0;
+        b.order = order; b.two_dof = 1; b.frames = 1; b.g_stride = 0;
         b.scratch = bscr;
-        rc = run_batched(c, b, N, cands);
+        rc = run_batched(c, b, N, cands, QueueKeys{nullptr, a.wsl2, 0});
       }
     }
     if (rc) return rc;

@@ -88,38 +88,30 @@ struct Team {
 // (6x6 form) and produces DeltaP_k; the inverse-compositional update of P and
 // the image-bounds test of the next warp are also split over lanes, so the
 // narrow FP64 pipe sees a few dozen instructions per iteration.
-STDIC_DEV double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
-// P <- P o DeltaP^-1 (funICGNQuadtree.m:393-411), warp-parallel in FP32:
-// lane k < 6 forms tempP_(k+1), then the new P_(k+1); D is known on every
-// lane.  Returns false (P unchanged) when det(DeltaP) == 0.
+// P <- P o DeltaP^-1 (funICGNQuadtree.m:393-411) in FP32.  Every lane holds
+// the same D and P and computes all six parameters, so the lanes stay
+// identical without shuffles or lane-specialised branches.  Returns false (P
+// unchanged) when det(DeltaP) == 0.
 STDIC_DEV bool compose_warp(float P[6], const float D[6], int lane) {
+  (void)lane;
   const float det = (1.f + D[0]) * (1.f + D[3]) - D[1] * D[2];
   if (!(det != 0.f)) return false;
   const float inv = 1.f / det;
-  float t = 0.f;
-  switch (lane) {
-    case 0: t = (-D[0] - D[0] * D[3] + D[1] * D[2]) * inv; break;
-    case 1: t = -D[1] * inv; break;
-    case 2: t = -D[2] * inv; break;
-    case 3: t = (-D[3] - D[0] * D[3] + D[1] * D[2]) * inv; break;
-    case 4: t = (-D[4] - D[3] * D[4] + D[2] * D[5]) * inv; break;
-    case 5: t = (-D[5] - D[0] * D[5] + D[1] * D[4]) * inv; break;
-  }
-  float T[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) T[k] = __shfl_sync(0xffffffffu, t, k);
-  float pn = 0.f;
-  switch (lane) {
-    case 0: pn = P[0] + ((1.f + P[0]) * T[0] + P[2] * T[1]); break;
-    case 1: pn = P[1] * (1.f + T[0]) + (1.f + P[3]) * T[1]; break;
-    case 2: pn = (1.f + P[0]) * T[2] + P[2] * (1.f + T[3]); break;
-    case 3: pn = P[3] + (P[1] * T[2] + (1.f + P[3]) * T[3]); break;
-    case 4: pn = P[4] + ((1.f + P[0]) * T[4] + P[2] * T[5]); break;
-    case 5: pn = P[5] + (P[1] * T[4] + (1.f + P[3]) * T[5]); break;
-  }
-#pragma unroll
-  for (int k = 0; k < 6; ++k) P[k] = __shfl_sync(0xffffffffu, pn, k);
+  const float T0 = (-D[0] - D[0] * D[3] + D[1] * D[2]) * inv;
+  const float T1 = -D[1] * inv;
+  const float T2 = -D[2] * inv;
+  const float T3 = (-D[3] - D[0] * D[3] + D[1] * D[2]) * inv;
+  const float T4 = (-D[4] - D[3] * D[4] + D[2] * D[5]) * inv;
+  const float T5 = (-D[5] - D[0] * D[5] + D[1] * D[4]) * inv;
+  const float a = 1.f + P[0], d = 1.f + P[3];
+  const float n0 = P[0] + (a * T0 + P[2] * T1);
+  const float n1 = P[1] * (1.f + T0) + d * T1;
+  const float n2 = a * T2 + P[2] * (1.f + T3);
+  const float n3 = P[3] + (P[1] * T2 + d * T3);
+  const float n4 = P[4] + (a * T4 + P[2] * T5);
+  const float n5 = P[5] + (P[1] * T4 + d * T5);
+  P[0] = n0; P[1] = n1; P[2] = n2; P[3] = n3; P[4] = n4; P[5] = n5;
   return true;
 }
 
@@ -377,27 +369,41 @@ STDIC_DEV void chol6_solve(const Chol6& C, const double b[6], double x[6]) {
   }
 }
 
-// DeltaP = -H \ b by LU with partial pivoting for a Hessian whose Cholesky
-// factorisation failed (MATLAB's mldivide falls back the same way); kept out
-// of line so its local arrays exist only on this rare path.
-__device__ __noinline__ void singular_solve6(const double* __restrict__ H, const float b[6], float D[6]) {
-  double Hm[36], bd[6], Dd[6];
-  for (int r = 0; r < 6; ++r)
-    for (int c2 = 0; c2 <= r; ++c2) {
-      Hm[r * 6 + c2] = H[r * (r + 1) / 2 + c2];
-      Hm[c2 * 6 + r] = H[r * (r + 1) / 2 + c2];
-    }
-  for (int q = 0; q < 6; ++q) bd[q] = (double)b[q];
-  small_solve(Hm, bd, 6, Dd);
-  for (int q = 0; q < 6; ++q) D[q] = (float)(-Dd[q]);
-}
-
 struct TeamCtl {
-  double Hm[36];    // inverse Hessian of the team's current subset (6-DOF)
+  // inverse Hessian of the team's current subset (6-DOF, row-major), split
+  // into FP32 pairs hh + hl that carry its FP64 value to about 2^-48
+  float hh[36], hl[36];
   float jf[6], j1[6];
   int item;
   int pad[3];
 };
+
+// Double-float helpers: a pair (hi, lo) of FP32 values represents hi + lo.
+// fp64 -> pair (exact to about 2^-48 relative)
+STDIC_DEV void split_f64(double v, float& hi, float& lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+// sum_q (hh_q + hl_q) * x_q in double-float arithmetic, rounded once to FP32:
+// each product is split exactly by an FMA and the running sum is kept as an
+// error-free (TwoSum) pair, so the result matches an FP64 dot product of the
+// same operands rounded to FP32, without using the FP64 pipe.
+template <int K>
+STDIC_DEV float dot_df(const float* hh, const float* hl, const float* x) {
+  float S = 0.f, E = 0.f;
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    const float p = __fmul_rn(hh[q], x[q]);
+    const float e = fmaf(hl[q], x[q], fmaf(hh[q], x[q], -p));
+    const float t = __fadd_rn(S, p);
+    const float bp = __fsub_rn(t, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    E = __fadd_rn(E, __fadd_rn(err, e));
+    S = t;
+  }
+  return __fadd_rn(S, E);
+}
 
 }  // namespace
 
@@ -406,8 +412,16 @@ size_t batched_team_bytes(int sm_px, bool two, int tw) {
          sizeof(float) * 32 * tw + 16 * tw + 64;
 }
 
-size_t batched_scratch_bytes(int npx_max, bool two, long long teams) {
-  return ((size_t)npx_max * (two ? 8 : 4) + 4 * (size_t)npx_max) * (size_t)teams + 256;
+size_t batched_scratch_bytes(int npx_max, bool two, long long warps) {
+  return ((size_t)npx_max * (two ? 8 : 4) + 4 * (size_t)npx_max) * (size_t)warps + 256;
+}
+
+int batched_small_px(int sm_px, bool two, int tw) {
+  const size_t sub = (batched_team_bytes(sm_px, two, tw) / tw) & ~(size_t)15;
+  const long long fixed = (long long)(sizeof(TeamCtl) + sizeof(float) * 32 + 16 + 64 + 15);
+  long long px = ((long long)sub - fixed) / (two ? 12 : 8);
+  while (px > 0 && batched_team_bytes((int)px, two, 1) > sub) --px;
+  return (int)(px > 0 ? px : 0);
 }
 
 // Shared memory per team: smem_px floats (tempg) [+ smem_px floats (tempf,
@@ -420,545 +434,611 @@ size_t batched_scratch_bytes(int npx_max, bool two, long long teams) {
 // in FP64 between them.  Every warp of a team holds the team totals after each
 // reduction and runs the same FP64 update on them, so all warps carry
 // bit-identical P without a shared-memory broadcast.
+// One subset on one team: set-up, iterations and outputs.  base/ctl/fscr/iscr
+// are the team's shared slot of smpx tile pixels, gbase its global slice.
 template <int TW, bool TWO, int STAGE>
-__global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
-  extern __shared__ __align__(16) unsigned char dsm[];
+STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, unsigned char* base,
+                          TeamCtl* ctl, float* fscr, int* iscr, unsigned char* gbase, int smpx) {
   const IcgnArgs& a = B.a;
-  Team<TW> tm;
-  tm.id = threadIdx.x / Team<TW>::TT;
-  tm.tl = threadIdx.x % Team<TW>::TT;
   const int lane = threadIdx.x & 31;
   constexpr int stage = STAGE;
-  const int teams_per_block = blockDim.x / Team<TW>::TT;
-  const long long gteam = (long long)blockIdx.x * teams_per_block + tm.id;
-  const int smpx = B.smem_px;
+  SubsetState6* st6 = (SubsetState6*)B.st6;
+  const int Ntot = a.N * (B.frames > 0 ? B.frames : 1);
+  const float tolf = (float)a.tol;
+  const int node = item % a.N;
+  const int frame = item / a.N;
+  Frame32 fr{B.f32, B.g32 + (long long)frame * B.g_stride, a.mask, B.dfdx32, B.dfdy32, a.W, a.H};
+  const long long x0 = llround(a.coords[node]), y0 = llround(a.coords[a.N + node]);
+
+  // ---------------- per-subset set-up ----------------
+  int wx, wy;
+  float P[6];  // warp parameters [F11 F21 F12 F22 u v] in FP32
+  if constexpr (TWO) {
+    wx = a.wsl2[node]; wy = a.wsl2[a.N + node];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) P[k] = (float)a.FOld[4 * item + k];
+    P[4] = (float)a.UOld[2 * item]; P[5] = (float)a.UOld[2 * item + 1];
+  } else {
+    wx = wy = a.ws_list ? a.ws_list[node] : a.ws_all;
+    P[0] = P[1] = P[2] = P[3] = 0.f;
+    P[4] = (float)a.U0[2 * item]; P[5] = (float)a.U0[2 * item + 1];
+  }
+  const int ws0 = wx;
+  float uold0 = 0.f, uold1 = 0.f, vd0 = 0.f, vd1 = 0.f;
+  if constexpr (TWO) {
+    uold0 = P[4]; uold1 = P[5];
+    vd0 = (float)a.vdual[2 * item]; vd1 = (float)a.vdual[2 * item + 1];
+  }
+  long long x1 = x0 - wx / 2, x3 = x0 + wx / 2, y1 = y0 - wy / 2, y3 = y0 + wy / 2;
+  int code = 0;
+  bool nan_out = false;
+  const int err_code = TWO ? 0 : -1;  // value the reference leaves on a run-time error
+  int cntf = 0;
+  float meanf = 0.f, bottomf = 0.f, sabs = 0.f;
+  double A11 = 0, A12 = 0, A22 = 0;
+  int mx = 0, my = 0, npx = 0, sc = 0, sr = 0;
+  int4 pstart = make_int4(0, 0, 0, 0);  // PixIter start of this thread for the tile
+  float* tg = nullptr;
+  float* tf = nullptr;
+  uint8_t *mtile = nullptr, *bwf = nullptr, *bwg = nullptr, *tmp = nullptr;
+  bool has_masked = false;
+  bool decided = false;  // outputs of this subset already written by the set-up stage
+  const double npx0 = (double)(wx + 1) * (double)(wy + 1);
+
+  if (stage == 2) {
+    const SubsetState6 s6 = st6[item];
+    if (s6.code != 0) {
+      decided = true;
+    } else {
+      wx = wy = s6.ws;
+      x1 = x0 - wx / 2; x3 = x0 + wx / 2; y1 = y0 - wy / 2; y3 = y0 + wy / 2;
+      cntf = s6.cntf;
+      has_masked = s6.masked != 0;
+      meanf = s6.meanf; bottomf = s6.bottomf; sabs = s6.sabs;
+    }
+  } else {
+    const bool crop_valid = !((wx & 1) || (wy & 1)) && wx >= 0 && wy >= 0 && wx <= a.ws_max &&
+                            wy <= a.ws_max && mask_crop_ok32(fr, x1, x3, y1, y3);
+    int nanf = 0;
+    if (crop_valid) {
+      const int mx0 = wx + 1, np0 = (wx + 1) * (wy + 1);
+      PixIter it(tm.tl, tm.TT, mx0);
+      for (int p = tm.tl; p < np0; p += tm.TT, it.next()) {
+        const float t = fr.F(x1 + it.i, y1 + it.j) * fr.M(x1 + it.i, y1 + it.j);
+        if (t != t) nanf = 1;
+        if (t == 0.f) ++cntf;
+      }
+    }
+    cntf = tm.sum_int(cntf, iscr);
+    nanf = tm.any(nanf, iscr);
+    if constexpr (!TWO) {
+      if (a.mark && tm.tl == 0) a.mark[item] = (!crop_valid || cntf > 0) ? 1 : 0;
+    }
+    if (!crop_valid || !crop_ok32(fr, x1, x3, y1, y3) || nanf) {
+      code = err_code; nan_out = true;
+    } else if (!((double)cntf < 0.4 * npx0)) {
+      code = kMaxIter + 2;
+    } else if ((double)cntf > 0.0 * npx0) {
+      if constexpr (TWO) {
+        {
+          const double aa = (double)(wx + 1) * (double)(wy + 1);
+          wx = (int)grow_window(aa, aa - (double)cntf, wx);
+        }
+        {
+          const double aa = (double)(wx + 1) * (double)(wy + 1);
+          wy = (int)grow_window(aa, aa - (double)cntf, wy);
+        }
+      } else {
+        wx = wy = (int)grow_window(npx0, npx0 - (double)cntf, wx);
+      }
+      x1 = x0 - wx / 2; x3 = x0 + wx / 2; y1 = y0 - wy / 2; y3 = y0 + wy / 2;
+      if (!mask_crop_ok32(fr, x1, x3, y1, y3) || !crop_ok32(fr, x1, x3, y1, y3) ||
+          (wx + 1) * (wy + 1) > a.npx_max) {
+        code = err_code; nan_out = true;
+      }
+    }
+  }
+  // tile storage, mask tile and the 4-connected f selection
+  if (!decided && code == 0 && !nan_out) {
+    mx = wx + 1; my = wy + 1; npx = mx * my;
+    sc = (wx + 1) / 2; sr = (wy + 1) / 2;
+    pstart = make_int4(tm.tl % mx, tm.tl / mx, tm.TT % mx, tm.TT / mx);
+    const bool in_smem = npx <= smpx;
+    const int cap = in_smem ? smpx : a.npx_max;
+    unsigned char* stp = in_smem ? base : gbase;
+    tg = (float*)stp;
+    tf = tg + cap;
+    mtile = (uint8_t*)(tg + (TWO ? 2 : 1) * cap);
+    bwf = mtile + cap;
+    bwg = bwf + cap;
+    tmp = bwg + cap;
+    int z = 0;
+    PixIter it(pstart, mx);
+    for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+      const uint8_t mk = __ldg(fr.mask + (y1 + it.j - 1) * fr.W + (x1 + it.i - 1)) != 0;
+      mtile[p] = mk;
+      if (!mk) z = 1;
+    }
+    if (stage != 2) has_masked = tm.any(z, iscr) != 0;
+    if (has_masked) bwselect_team(tm, mtile, bwf, mx, my, sr, sc, 4, iscr);
+    tm.sync();
+  }
+
+  const uint8_t* bw = has_masked ? bwf : nullptr;  // nullptr: every pixel selected
+  constexpr int NQ = TWO ? 2 : 6;  // parameters of the b-vector
+  // inverse of the 2x2 system (2-DOF) as double-float pairs: row k of lane k < 2
+  float ih[2] = {0.f, 0.f}, il[2] = {0.f, 0.f};
+  // f-side parts of b: jf = sum J (tempf - meanf), j1 = sum J
+  float jf[NQ], j1[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) { jf[q] = 0.f; j1[q] = 0.f; }
+  // steepest-descent images J of pixel (i, j): [dx gx, dx gy, dy gx, dy gy, gx, gy]
+  // (6-DOF) or [gx, gy] (2-DOF), gx/gy masked by the current selection
+  auto jac = [&](int i, int j, float s, float (&J)[NQ]) {
+    const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
+    if constexpr (TWO) {
+      J[0] = gx; J[1] = gy;
+    } else {
+      const float dx = (float)(int)(x1 + i - x0), dy = (float)(int)(y1 + j - y0);
+      J[0] = dx * gx; J[1] = dx * gy; J[2] = dy * gx; J[3] = dy * gy; J[4] = gx; J[5] = gy;
+    }
+  };
+  // f-side statistics: Hessian (6x6 or 2x2), meanf, bottomf, sum |tempf|, jf, j1.
+  // The 6-DOF set-up stage stores them; the 2-DOF form recomputes them when
+  // the g selection changes (funICGN_Subpb1.m:171-190).
+  auto f_side = [&]() {
+    float hs[21];
+#pragma unroll
+    for (int k = 0; k < 21; ++k) hs[k] = 0.f;
+    Kahan sf;
+    float nf = 0.f, sa = 0.f;
+    PixIter it(pstart, mx);
+    for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+      const int i = it.i, j = it.j;
+      const float s = bw ? (float)bw[p] : 1.f;
+      const float fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
+      if constexpr (TWO) tf[p] = fv;
+      sa += fabsf(fv);
+      if (fabsf(fv) > 1e-10f) { sf.add(fv); nf += 1.f; }
+      float J[NQ];
+      jac(i, j, s, J);
+      int q = 0;
+#pragma unroll
+      for (int aa = 0; aa < NQ; ++aa)
+#pragma unroll
+        for (int bb = aa; bb < NQ; ++bb) hs[q++] += J[aa] * J[bb];
+    }
+    float st4[4] = {sf.s, -sf.c, nf, sa};
+    tm.template sumf<4>(st4, fscr);
+    const float cnt = st4[2];
+    const float mean = (st4[0] + st4[1]) / cnt;
+    Kahan q, kjf[NQ], kj1[NQ];
+    PixIter it2(pstart, mx);
+    for (int p = tm.tl; p < npx; p += tm.TT, it2.next()) {
+      const float s = bw ? (float)bw[p] : 1.f;
+      float fv;
+      if constexpr (TWO) fv = tf[p];
+      else fv = fr.F(x1 + it2.i, y1 + it2.j) * fr.M(x1 + it2.i, y1 + it2.j) * s;
+      if (fabsf(fv) > 1e-10f) { const float d = fv - mean; q.add(d * d); }
+      float J[NQ];
+      jac(it2.i, it2.j, s, J);
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) { kjf[k].add(J[k] * (fv - mean)); kj1[k].add(J[k]); }
+    }
+    float qq[2 + 4 * NQ];
+    qq[0] = q.s; qq[1] = -q.c;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      qq[2 + 4 * k] = kjf[k].s; qq[3 + 4 * k] = -kjf[k].c;
+      qq[4 + 4 * k] = kj1[k].s; qq[5 + 4 * k] = -kj1[k].c;
+    }
+    tm.template sumf<2 + 4 * NQ>(qq, fscr);
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) { jf[k] = qq[2 + 4 * k] + qq[3 + 4 * k]; j1[k] = qq[4 + 4 * k] + qq[5 + 4 * k]; }
+    const float var = cnt == 0.f ? __int_as_float(0x7fc00000) : (cnt == 1.f ? 0.f : (qq[0] + qq[1]) / (cnt - 1.f));
+    meanf = mean;
+    bottomf = sqrtf((cnt - 1.f) * var);
+    sabs = st4[3];
+    if constexpr (TWO) {
+      tm.template sumf<3>(*reinterpret_cast<float(*)[3]>(hs), fscr);
+      const double b2 = (double)bottomf * (double)bottomf;
+      A11 = (double)hs[0] * 2 / b2 + a.mu;
+      A12 = (double)hs[1] * 2 / b2;
+      A22 = (double)hs[2] * 2 / b2 + a.mu;
+      // H2 + 1e-3 max(diag H2) I of funICGN_Subpb1.m:391-394, inverted once per change
+      const double dmax = isnan(A11) ? A22 : (isnan(A22) ? A11 : fmax(A11, A22));
+      double i00, i01, i10, i11;
+      solve2(A11 + 1e-3 * dmax, A12, A22 + 1e-3 * dmax, 1.0, 0.0, &i00, &i10);
+      solve2(A11 + 1e-3 * dmax, A12, A22 + 1e-3 * dmax, 0.0, 1.0, &i01, &i11);
+      split_f64(lane == 1 ? i10 : i00, ih[0], il[0]);
+      split_f64(lane == 1 ? i11 : i01, ih[1], il[1]);
+    } else {
+      tm.template sumf<21>(hs, fscr);
+      // packed lower (row-major) Hessian for the factor kernel and the output
+      if (tm.tl < 21) {
+        float v = 0.f;
+#pragma unroll
+        for (int k = 0; k < 21; ++k)
+          if (k == tm.tl) v = hs[k];
+        // hs index of (row aa, col bb >= aa) -> packed lower (bb, aa)
+        int aa = 0, rem = tm.tl;
+        while (rem >= 6 - aa) { rem -= 6 - aa; ++aa; }
+        const int bb = aa + rem;
+        B.H6[(size_t)item * 21 + bb * (bb + 1) / 2 + aa] = (double)v;
+        // HGlobal = [H(1:6) H(8:12) ...]: column aa, rows aa..5 in the order of hs
+        if (a.Hpk) a.Hpk[(size_t)tm.tl * Ntot + item] = (double)v;
+      }
+    }
+    tm.sync();
+  };
+
+  if (stage != 2 && !decided && code == 0 && !nan_out) f_side();
+
+  if (stage == 1) {
+    // hand the subset to the factor kernel and the iteration stage
+    if (tm.tl == 0) {
+      SubsetState6 s6;
+      s6.code = nan_out ? -1 : code;
+      s6.ws = wx; s6.cntf = cntf; s6.masked = has_masked ? 1 : 0;
+      s6.meanf = meanf; s6.bottomf = bottomf; s6.sabs = sabs; s6.pad = 0.f;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) { s6.Jf[k] = jf[k < NQ ? k : 0]; s6.J1[k] = j1[k < NQ ? k : 0]; }
+      st6[item] = s6;
+      if (code != 0 || nan_out) {
+        a.conv[item] = code;
+        // decided in the set-up: P is still the initial guess, passed through in FP64
+        a.U[2 * item] = nan_out ? nan("") : a.U0[2 * item];
+        a.U[2 * item + 1] = nan_out ? nan("") : a.U0[2 * item + 1];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) a.F[4 * item + k] = nan_out ? nan("") : 0.0;
+        if (a.Hpk)
+          for (int q = 0; q < 21; ++q) a.Hpk[(size_t)q * Ntot + item] = 0.0;
+      }
+    }
+    tm.sync();
+    return;
+  }
+  if (decided) {
+    tm.sync();
+    return;
+  }
+  if constexpr (!TWO) {
+    // the subset's inverse Hessian and f-side sums, once, into the team's control block
+    for (int k = tm.tl; k < 36; k += tm.TT) split_f64(B.Hinv6[(size_t)item * 36 + k], ctl->hh[k], ctl->hl[k]);
+    if (tm.tl < 6) { ctl->jf[tm.tl] = st6[item].Jf[tm.tl]; ctl->j1[tm.tl] = st6[item].J1[tm.tl]; }
+    tm.sync();
+  }
+  const bool run = (code == 0 && !nan_out);
+  float normNew = 1.f, normAbs = 1.f, normInit = 0.f;
+  int step = 0, cg = 0, nupd = 0, last_cg = -1, last_nws = wx;
+  bool err = false;
+  bool oob = run ? corners_oob_warp(P, (int)x0, (int)y0, (int)x1, (int)y1, mx, my, a.W, a.H, lane) : false;
+  float ibf = 1.f / bottomf;
+  while (run && step <= kMaxIter && normNew > tolf && normAbs > tolf) {
+    ++step;
+    if constexpr (!TWO) {
+      if (step > 1 && (double)cntf > 0.0 * npx0) {
+        // window growth test of funICGNQuadtree.m:140 (FP64, recomputed only
+        // when the count of selected g pixels changes)
+        int nws = last_nws;
+        if (cg != last_cg) {
+          const double r = sqrt((double)((ws0 + 1) * (ws0 + 1)) / (double)cg) * wx / 2;
+          if (!isfinite(r)) { err = true; break; }
+          nws = 2 * (int)ceil(r);
+          last_cg = cg;
+          last_nws = nws;
+        }
+        if (nws != wx) {
+          const long long nx1 = x0 - nws / 2, nx3 = x0 + nws / 2, ny1 = y0 - nws / 2, ny3 = y0 + nws / 2;
+          if (!mask_crop_ok32(fr, nx1, nx3, ny1, ny3)) { err = true; break; }
+          if (corners_oob_warp(P, (int)x0, (int)y0, (int)nx1, (int)ny1, nws + 1, nws + 1, a.W, a.H, lane)) { normNew = 1e6f; break; }
+          err = true;
+          break;
+        }
+      }
+    }
+    if (oob) { normNew = 1e6f; break; }
+    // integer base + FP32 offsets of the warp
+    const float flu = floorf(P[4]), flv = floorf(P[5]);
+    const int iu = (int)x0 + (int)flu, iv = (int)y0 + (int)flv;
+    const float fu = P[4] - flu, fv0 = P[5] - flv;
+    const float p0 = 1.f + P[0], p1 = P[1], p2 = P[2], p3 = 1.f + P[3];
+    const float dx0 = (float)(int)(x1 - x0), dy0 = (float)(int)(y1 - y0);
+    const float shift = meanf;  // one-pass variance around meanf
+    // one pass: interpolation, zero/NaN counts, g statistics and sum J g
+    constexpr int NR = 7 + 2 * NQ;
+    float red[NR];
+    {
+      int zg = 0, nang = 0;
+      Kahan sg, qg, kg[NQ];
+      float ng = 0.f;
+      PixIter it(pstart, mx);
+      auto one = [&](int p, int i, int j, float t) {
+        tg[p] = t;
+        if (t != t) nang = 1;
+        if (t == 0.f) ++zg;
+        if (fabsf(t) > 1e-10f) {
+          const float d = t - shift;
+          sg.add(d);
+          qg.add(d * d);
+          ng += 1.f;
+        }
+        float J[NQ];
+        jac(i, j, bw ? (float)bw[p] : 1.f, J);
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) kg[k].add(J[k] * t);
+      };
+      int p = tm.tl;
+      // two pixels per trip so that both pixels' 16 taps are in flight together
+      for (; p + tm.TT < npx; p += 2 * tm.TT) {
+        const int ia = it.i, ja = it.j;
+        it.next();
+        const int ib = it.i, jb = it.j;
+        it.next();
+        const float dxa = dx0 + (float)ia, dya = dy0 + (float)ja;
+        const float dxb = dx0 + (float)ib, dyb = dy0 + (float)jb;
+        const float ta = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dxa + p2 * dya, iv, fv0 + p1 * dxa + p3 * dya);
+        const float tb2 = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dxb + p2 * dyb, iv, fv0 + p1 * dxb + p3 * dyb);
+        one(p, ia, ja, ta);
+        one(p + tm.TT, ib, jb, tb2);
+      }
+      if (p < npx) {
+        const float dx = dx0 + (float)it.i, dy = dy0 + (float)it.j;
+        const float t = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dx + p2 * dy, iv, fv0 + p1 * dx + p3 * dy);
+        one(p, it.i, it.j, t);
+      }
+      red[0] = (float)zg; red[1] = (float)nang;
+      red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) { red[7 + 2 * k] = kg[k].s; red[8 + 2 * k] = -kg[k].c; }
+    }
+    tm.template sumf<NR>(red, fscr);
+    if (red[1] > 0.f) { err = true; break; }
+    if (cntf > 0 || red[0] > 0.f) {
+      for (int p = tm.tl; p < npx; p += tm.TT) tmp[p] = tg[p] != 0.f;
+      tm.sync();
+      bwselect_team(tm, tmp, bwg, mx, my, sr, sc, TWO ? 4 : 8, iscr);
+      int anyzero = 0;
+      for (int p = tm.tl; p < npx; p += tm.TT) anyzero |= !bwg[p];
+      if (!tm.any(anyzero, iscr)) bwselect_team(tm, mtile, bwg, mx, my, sr, sc, 8, iscr);
+      if constexpr (TWO) {
+        bw = bwg;
+        f_side();
+        ibf = 1.f / bottomf;
+      }
+      // the g tile restricted to its selection, and its sums again
+      int cnt = 0;
+      Kahan sg, qg, kg[NQ];
+      float ng = 0.f;
+      PixIter it(pstart, mx);
+      for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+        const float t = tg[p] * (float)bwg[p];
+        tg[p] = t;
+        cnt += bwg[p];
+        if (fabsf(t) > 1e-10f) {
+          const float d = t - shift;
+          sg.add(d);
+          qg.add(d * d);
+          ng += 1.f;
+        }
+        float J[NQ];
+        jac(it.i, it.j, bw ? (float)bw[p] : 1.f, J);
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) kg[k].add(J[k] * t);
+      }
+      red[0] = (float)cnt; red[1] = 0.f;
+      red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) { red[7 + 2 * k] = kg[k].s; red[8 + 2 * k] = -kg[k].c; }
+      tm.template sumf<NR>(red, fscr);
+      cg = (int)red[0];
+    }
+    // g statistics from the shifted one-pass sums: mean and
+    // sqrt((n-1) var) = sqrt(max(s2 - s1^2/n, 0)) (NaN for n = 0, 0 for n = 1)
+    const float cntg = red[6];
+    const float s1 = red[2] + red[3], s2 = red[4] + red[5];
+    const float icnt = 1.f / cntg;
+    const float meang = shift + s1 * icnt;
+    float bg2 = fmaxf(s2 - s1 * s1 * icnt, 0.f);
+    if (cntg == 1.f) bg2 = 0.f;
+    if (cntg == 0.f) bg2 = __int_as_float(0x7fc00000);
+    const float ibg = 1.f / sqrtf(bg2);
+    // b2 = sum J [(tempf - meanf)/bottomf - (tempg - meang)/bottomg]; the
+    // 6-DOF f-side sums come from the set-up stage (read here, not held
+    // in registers across the pixel pass)
+    if constexpr (!TWO) {
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) { jf[k] = ctl->jf[k]; j1[k] = ctl->j1[k]; }
+    }
+    float b2[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      const float jg = red[7 + 2 * k] + red[8 + 2 * k];
+      b2[k] = jf[k] * ibf - (jg - meang * j1[k]) * ibg;
+    }
+    // convergence test (FP32) and the FP64 update, identical on every warp
+    int done = 0;
+    float nb = 0.f;
+    float D[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if constexpr (TWO) {
+      const float b0 = bottomf * b2[0], b1 = bottomf * b2[1];
+      const float sc2 = 2.f / (bottomf * bottomf);
+      const float tb0 = b0 * sc2 + (float)a.mu * (P[4] - uold0 - vd0);
+      const float tb1 = b1 * sc2 + (float)a.mu * (P[5] - uold1 - vd1);
+      nb = tb0 * tb0 + tb1 * tb1;
+      // 2x2 solve with the FP64 inverse: lane 0 forms DeltaP_5, lane 1 DeltaP_6
+      const float tb[2] = {tb0, tb1};
+      const float dkf = -dot_df<2>(ih, il, tb);
+      D[4] = __shfl_sync(0xffffffffu, dkf, 0);
+      D[5] = __shfl_sync(0xffffffffu, dkf, 1);
+    } else {
+      float b[6];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) { b[q] = bottomf * b2[q < NQ ? q : 0]; nb += b[q] * b[q]; }
+      // DeltaP = -H^-1 b with the FP64 inverse: every lane holds b, lane k
+      // forms row k in double-float arithmetic
+      const int r = (lane < 6 ? lane : 0) * 6;
+      const float dkf = -dot_df<6>(ctl->hh + r, ctl->hl + r, b);
+#pragma unroll
+      for (int q = 0; q < 6; ++q) D[q] = __shfl_sync(0xffffffffu, dkf, q);
+    }
+    float nN = sqrtf(nb);
+    const float nA = nN;
+    if (step == 1) normInit = nN;
+    nN = normInit > tolf ? nN / normInit : 0.f;
+    normNew = nN;
+    normAbs = nA;
+    if (nN < tolf || nA < tolf) done = 1;
+    else if (!compose_warp(P, D, lane)) done = 2;
+    else ++nupd;
+    if (done) break;
+    oob = corners_oob_warp(P, (int)x0, (int)y0, (int)x1, (int)y1, mx, my, a.W, a.H, lane);
+  }
+  if (run) {
+    if (err) { code = err_code; nan_out = true; }
+    else {
+      code = step;
+      if (!(normNew < tolf || normAbs < tolf)) code = kMaxIter + 1;
+      if (isnan(normNew)) code = kMaxIter + 1;
+      if constexpr (TWO) {
+        float v[1] = {0.f};
+        for (int p = tm.tl; p < npx; p += tm.TT) v[0] += fabsf(tf[p]);
+        tm.template sumf<1>(v, fscr);
+        sabs = v[0];
+      }
+      if (sabs < 1e-6f) code = kMaxIter + 3;
+    }
+  }
+  if (tm.tl == 0) {
+    a.conv[item] = code;
+    // a subset that never updated P returns its initial guess bit-exactly
+    const bool moved = nupd > 0;
+    if constexpr (TWO) {
+      a.U[2 * item] = nan_out ? nan("") : (moved ? (double)P[4] : a.UOld[2 * item]);
+      a.U[2 * item + 1] = nan_out ? nan("") : (moved ? (double)P[5] : a.UOld[2 * item + 1]);
+    } else {
+      a.U[2 * item] = nan_out ? nan("") : (moved ? (double)P[4] : a.U0[2 * item]);
+      a.U[2 * item + 1] = nan_out ? nan("") : (moved ? (double)P[5] : a.U0[2 * item + 1]);
+    }
+    if constexpr (!TWO) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) a.F[4 * item + k] = nan_out ? nan("") : (double)P[k];
+      if (a.Hpk && nan_out)
+        for (int q = 0; q < 21; ++q) a.Hpk[(size_t)q * Ntot + item] = 0.0;
+    }
+  }
+  tm.sync();
+}
+
+// Pulls queue positions [lo, hi) from counter *head, one subset per team.
+// Frames are interleaved so that every frame's largest subsets start first.
+template <int TW, bool TWO, int STAGE>
+STDIC_DEV void team_loop(const BatchedArgs& B, const Team<TW>& tm, int* head, int lo, int hi,
+                         unsigned char* base, int smpx, unsigned char* gbase) {
   const size_t tiles_b = ((size_t)smpx * (TWO ? 8 : 4) + 4 * (size_t)smpx + 15) / 16 * 16;
-  const size_t tb = tiles_b + sizeof(TeamCtl) + sizeof(float) * 32 * TW + 16 * TW + 64;
-  unsigned char* base = dsm + tb * tm.id;
   TeamCtl* ctl = (TeamCtl*)(base + tiles_b);
   float* fscr = (float*)(ctl + 1);
   int* iscr = (int*)(fscr + 32 * TW);
-  const size_t gstride = (size_t)a.npx_max * (TWO ? 8 : 4) + 4 * (size_t)a.npx_max;
-  unsigned char* gbase = B.scratch + gstride * gteam;
-  SubsetState6* st6 = (SubsetState6*)B.st6;
-
-  const int Ntot = a.N * (B.frames > 0 ? B.frames : 1);
-  const float tolf = (float)a.tol;
+  const int nf = B.frames > 0 ? B.frames : 1;
   for (;;) {
     if (tm.tl == 0) {
-      // frames interleaved so that every frame's largest subsets start first
-      const int q = atomicAdd(B.queue_head, 1);
-      const int nf = B.frames > 0 ? B.frames : 1;
-      ctl->item = q < Ntot ? B.order[q / nf] + (q % nf) * a.N : -1;
+      const int q = lo + atomicAdd(head, 1);
+      ctl->item = q < hi ? B.order[q / nf] + (q % nf) * B.a.N : -1;
     }
     tm.sync();
     const int item = ctl->item;
     tm.sync();
     if (item < 0) break;
-    const int node = item % a.N;
-    const int frame = item / a.N;
-    Frame32 fr{B.f32, B.g32 + (long long)frame * B.g_stride, a.mask, B.dfdx32, B.dfdy32, a.W, a.H};
-    const long long x0 = llround(a.coords[node]), y0 = llround(a.coords[a.N + node]);
-
-    // ---------------- per-subset set-up ----------------
-    int wx, wy;
-    float P[6];  // warp parameters [F11 F21 F12 F22 u v] in FP32
-    if constexpr (TWO) {
-      wx = a.wsl2[node]; wy = a.wsl2[a.N + node];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) P[k] = (float)a.FOld[4 * item + k];
-      P[4] = (float)a.UOld[2 * item]; P[5] = (float)a.UOld[2 * item + 1];
-    } else {
-      wx = wy = a.ws_list ? a.ws_list[node] : a.ws_all;
-      P[0] = P[1] = P[2] = P[3] = 0.f;
-      P[4] = (float)a.U0[2 * item]; P[5] = (float)a.U0[2 * item + 1];
-    }
-    const int ws0 = wx;
-    float uold0 = 0.f, uold1 = 0.f, vd0 = 0.f, vd1 = 0.f;
-    if constexpr (TWO) {
-      uold0 = P[4]; uold1 = P[5];
-      vd0 = (float)a.vdual[2 * item]; vd1 = (float)a.vdual[2 * item + 1];
-    }
-    long long x1 = x0 - wx / 2, x3 = x0 + wx / 2, y1 = y0 - wy / 2, y3 = y0 + wy / 2;
-    int code = 0;
-    bool nan_out = false;
-    const int err_code = TWO ? 0 : -1;  // value the reference leaves on a run-time error
-    int cntf = 0;
-    float meanf = 0.f, bottomf = 0.f, sabs = 0.f;
-    double A11 = 0, A12 = 0, A22 = 0;
-    int mx = 0, my = 0, npx = 0, sc = 0, sr = 0;
-    int4 pstart = make_int4(0, 0, 0, 0);  // PixIter start of this thread for the tile
-    float* tg = nullptr;
-    float* tf = nullptr;
-    uint8_t *mtile = nullptr, *bwf = nullptr, *bwg = nullptr, *tmp = nullptr;
-    bool has_masked = false;
-    bool decided = false;  // outputs of this subset already written by the set-up stage
-    const double npx0 = (double)(wx + 1) * (double)(wy + 1);
-
-    if (stage == 2) {
-      const SubsetState6 s6 = st6[item];
-      if (s6.code != 0) {
-        decided = true;
-      } else {
-        wx = wy = s6.ws;
-        x1 = x0 - wx / 2; x3 = x0 + wx / 2; y1 = y0 - wy / 2; y3 = y0 + wy / 2;
-        cntf = s6.cntf;
-        has_masked = s6.masked != 0;
-        meanf = s6.meanf; bottomf = s6.bottomf; sabs = s6.sabs;
-      }
-    } else {
-      const bool crop_valid = !((wx & 1) || (wy & 1)) && wx >= 0 && wy >= 0 && wx <= a.ws_max &&
-                              wy <= a.ws_max && mask_crop_ok32(fr, x1, x3, y1, y3);
-      int nanf = 0;
-      if (crop_valid) {
-        const int mx0 = wx + 1, np0 = (wx + 1) * (wy + 1);
-        PixIter it(tm.tl, tm.TT, mx0);
-        for (int p = tm.tl; p < np0; p += tm.TT, it.next()) {
-          const float t = fr.F(x1 + it.i, y1 + it.j) * fr.M(x1 + it.i, y1 + it.j);
-          if (t != t) nanf = 1;
-          if (t == 0.f) ++cntf;
-        }
-      }
-      cntf = tm.sum_int(cntf, iscr);
-      nanf = tm.any(nanf, iscr);
-      if constexpr (!TWO) {
-        if (a.mark && tm.tl == 0) a.mark[item] = (!crop_valid || cntf > 0) ? 1 : 0;
-      }
-      if (!crop_valid || !crop_ok32(fr, x1, x3, y1, y3) || nanf) {
-        code = err_code; nan_out = true;
-      } else if (!((double)cntf < 0.4 * npx0)) {
-        code = kMaxIter + 2;
-      } else if ((double)cntf > 0.0 * npx0) {
-        if constexpr (TWO) {
-          {
-            const double aa = (double)(wx + 1) * (double)(wy + 1);
-            wx = (int)grow_window(aa, aa - (double)cntf, wx);
-          }
-          {
-            const double aa = (double)(wx + 1) * (double)(wy + 1);
-            wy = (int)grow_window(aa, aa - (double)cntf, wy);
-          }
-        } else {
-          wx = wy = (int)grow_window(npx0, npx0 - (double)cntf, wx);
-        }
-        x1 = x0 - wx / 2; x3 = x0 + wx / 2; y1 = y0 - wy / 2; y3 = y0 + wy / 2;
-        if (!mask_crop_ok32(fr, x1, x3, y1, y3) || !crop_ok32(fr, x1, x3, y1, y3) ||
-            (wx + 1) * (wy + 1) > a.npx_max) {
-          code = err_code; nan_out = true;
-        }
-      }
-    }
-    // tile storage, mask tile and the 4-connected f selection
-    if (!decided && code == 0 && !nan_out) {
-      mx = wx + 1; my = wy + 1; npx = mx * my;
-      sc = (wx + 1) / 2; sr = (wy + 1) / 2;
-      pstart = make_int4(tm.tl % mx, tm.tl / mx, tm.TT % mx, tm.TT / mx);
-      const bool in_smem = npx <= smpx;
-      const int cap = in_smem ? smpx : a.npx_max;
-      unsigned char* stp = in_smem ? base : gbase;
-      tg = (float*)stp;
-      tf = tg + cap;
-      mtile = (uint8_t*)(tg + (TWO ? 2 : 1) * cap);
-      bwf = mtile + cap;
-      bwg = bwf + cap;
-      tmp = bwg + cap;
-      int z = 0;
-      PixIter it(pstart, mx);
-      for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
-        const uint8_t mk = __ldg(fr.mask + (y1 + it.j - 1) * fr.W + (x1 + it.i - 1)) != 0;
-        mtile[p] = mk;
-        if (!mk) z = 1;
-      }
-      if (stage != 2) has_masked = tm.any(z, iscr) != 0;
-      if (has_masked) bwselect_team(tm, mtile, bwf, mx, my, sr, sc, 4, iscr);
-      tm.sync();
-    }
-
-    const uint8_t* bw = has_masked ? bwf : nullptr;  // nullptr: every pixel selected
-    constexpr int NQ = TWO ? 2 : 6;  // parameters of the b-vector
-    double hinv[6];  // lane k < 6: row k of the inverse Hessian (6-DOF)
-    bool hok = false;
-    double i00 = 0, i01 = 0, i10 = 0, i11 = 0;  // inverse of the 2x2 system (2-DOF)
-    // f-side parts of b: jf = sum J (tempf - meanf), j1 = sum J
-    float jf[NQ], j1[NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) { jf[q] = 0.f; j1[q] = 0.f; }
-    // steepest-descent images J of pixel (i, j): [dx gx, dx gy, dy gx, dy gy, gx, gy]
-    // (6-DOF) or [gx, gy] (2-DOF), gx/gy masked by the current selection
-    auto jac = [&](int i, int j, float s, float (&J)[NQ]) {
-      const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
-      if constexpr (TWO) {
-        J[0] = gx; J[1] = gy;
-      } else {
-        const float dx = (float)(int)(x1 + i - x0), dy = (float)(int)(y1 + j - y0);
-        J[0] = dx * gx; J[1] = dx * gy; J[2] = dy * gx; J[3] = dy * gy; J[4] = gx; J[5] = gy;
-      }
-    };
-    // f-side statistics: Hessian (6x6 or 2x2), meanf, bottomf, sum |tempf|, jf, j1.
-    // The 6-DOF set-up stage stores them; the 2-DOF form recomputes them when
-    // the g selection changes (funICGN_Subpb1.m:171-190).
-    auto f_side = [&]() {
-      float hs[21];
-#pragma unroll
-      for (int k = 0; k < 21; ++k) hs[k] = 0.f;
-      Kahan sf;
-      float nf = 0.f, sa = 0.f;
-      PixIter it(pstart, mx);
-      for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
-        const int i = it.i, j = it.j;
-        const float s = bw ? (float)bw[p] : 1.f;
-        const float fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
-        if constexpr (TWO) tf[p] = fv;
-        sa += fabsf(fv);
-        if (fabsf(fv) > 1e-10f) { sf.add(fv); nf += 1.f; }
-        float J[NQ];
-        jac(i, j, s, J);
-        int q = 0;
-#pragma unroll
-        for (int aa = 0; aa < NQ; ++aa)
-#pragma unroll
-          for (int bb = aa; bb < NQ; ++bb) hs[q++] += J[aa] * J[bb];
-      }
-      float st4[4] = {sf.s, -sf.c, nf, sa};
-      tm.template sumf<4>(st4, fscr);
-      const float cnt = st4[2];
-      const float mean = (st4[0] + st4[1]) / cnt;
-      Kahan q, kjf[NQ], kj1[NQ];
-      PixIter it2(pstart, mx);
-      for (int p = tm.tl; p < npx; p += tm.TT, it2.next()) {
-        const float s = bw ? (float)bw[p] : 1.f;
-        float fv;
-        if constexpr (TWO) fv = tf[p];
-        else fv = fr.F(x1 + it2.i, y1 + it2.j) * fr.M(x1 + it2.i, y1 + it2.j) * s;
-        if (fabsf(fv) > 1e-10f) { const float d = fv - mean; q.add(d * d); }
-        float J[NQ];
-        jac(it2.i, it2.j, s, J);
-#pragma unroll
-        for (int k = 0; k < NQ; ++k) { kjf[k].add(J[k] * (fv - mean)); kj1[k].add(J[k]); }
-      }
-      float qq[2 + 4 * NQ];
-      qq[0] = q.s; qq[1] = -q.c;
-#pragma unroll
-      for (int k = 0; k < NQ; ++k) {
-        qq[2 + 4 * k] = kjf[k].s; qq[3 + 4 * k] = -kjf[k].c;
-        qq[4 + 4 * k] = kj1[k].s; qq[5 + 4 * k] = -kj1[k].c;
-      }
-      tm.template sumf<2 + 4 * NQ>(qq, fscr);
-#pragma unroll
-      for (int k = 0; k < NQ; ++k) { jf[k] = qq[2 + 4 * k] + qq[3 + 4 * k]; j1[k] = qq[4 + 4 * k] + qq[5 + 4 * k]; }
-      const float var = cnt == 0.f ? __int_as_float(0x7fc00000) : (cnt == 1.f ? 0.f : (qq[0] + qq[1]) / (cnt - 1.f));
-      meanf = mean;
-      bottomf = sqrtf((cnt - 1.f) * var);
-      sabs = st4[3];
-      if constexpr (TWO) {
-        tm.template sumf<3>(*reinterpret_cast<float(*)[3]>(hs), fscr);
-        const double b2 = (double)bottomf * (double)bottomf;
-        A11 = (double)hs[0] * 2 / b2 + a.mu;
-        A12 = (double)hs[1] * 2 / b2;
-        A22 = (double)hs[2] * 2 / b2 + a.mu;
-        // H2 + 1e-3 max(diag H2) I of funICGN_Subpb1.m:391-394, inverted once per change
-        const double dmax = isnan(A11) ? A22 : (isnan(A22) ? A11 : fmax(A11, A22));
-        solve2(A11 + 1e-3 * dmax, A12, A22 + 1e-3 * dmax, 1.0, 0.0, &i00, &i10);
-        solve2(A11 + 1e-3 * dmax, A12, A22 + 1e-3 * dmax, 0.0, 1.0, &i01, &i11);
-      } else {
-        tm.template sumf<21>(hs, fscr);
-        // packed lower (row-major) Hessian for the factor kernel and the output
-        if (tm.tl < 21) {
-          float v = 0.f;
-#pragma unroll
-          for (int k = 0; k < 21; ++k)
-            if (k == tm.tl) v = hs[k];
-          // hs index of (row aa, col bb >= aa) -> packed lower (bb, aa)
-          int aa = 0, rem = tm.tl;
-          while (rem >= 6 - aa) { rem -= 6 - aa; ++aa; }
-          const int bb = aa + rem;
-          B.H6[(size_t)item * 21 + bb * (bb + 1) / 2 + aa] = (double)v;
-          // HGlobal = [H(1:6) H(8:12) ...]: column aa, rows aa..5 in the order of hs
-          if (a.Hpk) a.Hpk[(size_t)tm.tl * Ntot + item] = (double)v;
-        }
-      }
-      tm.sync();
-    };
-
-    if (stage != 2 && !decided && code == 0 && !nan_out) f_side();
-
-    if (stage == 1) {
-      // hand the subset to the factor kernel and the iteration stage
-      if (tm.tl == 0) {
-        SubsetState6 s6;
-        s6.code = nan_out ? -1 : code;
-        s6.ws = wx; s6.cntf = cntf; s6.masked = has_masked ? 1 : 0;
-        s6.meanf = meanf; s6.bottomf = bottomf; s6.sabs = sabs; s6.pad = 0.f;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) { s6.Jf[k] = jf[k < NQ ? k : 0]; s6.J1[k] = j1[k < NQ ? k : 0]; }
-        st6[item] = s6;
-        if (code != 0 || nan_out) {
-          a.conv[item] = code;
-          // decided in the set-up: P is still the initial guess, passed through in FP64
-          a.U[2 * item] = nan_out ? nan("") : a.U0[2 * item];
-          a.U[2 * item + 1] = nan_out ? nan("") : a.U0[2 * item + 1];
-#pragma unroll
-          for (int k = 0; k < 4; ++k) a.F[4 * item + k] = nan_out ? nan("") : 0.0;
-          if (a.Hpk)
-            for (int q = 0; q < 21; ++q) a.Hpk[(size_t)q * Ntot + item] = 0.0;
-        }
-      }
-      tm.sync();
-      continue;
-    }
-    if (decided) {
-      tm.sync();
-      continue;
-    }
-    if constexpr (!TWO) {
-      // the subset's inverse Hessian and f-side sums, once, into the team's control block
-      for (int k = tm.tl; k < 36; k += tm.TT) ctl->Hm[k] = B.Hinv6[(size_t)item * 36 + k];
-      if (tm.tl < 6) { ctl->jf[tm.tl] = st6[item].Jf[tm.tl]; ctl->j1[tm.tl] = st6[item].J1[tm.tl]; }
-      tm.sync();
-      hok = !isnan(ctl->Hm[0]);
-    }
-    const bool run = (code == 0 && !nan_out);
-    float normNew = 1.f, normAbs = 1.f, normInit = 0.f;
-    int step = 0, cg = 0, nupd = 0, last_cg = -1, last_nws = wx;
-    bool err = false;
-    bool oob = run ? corners_oob_warp(P, (int)x0, (int)y0, (int)x1, (int)y1, mx, my, a.W, a.H, lane) : false;
-    while (run && step <= kMaxIter && normNew > tolf && normAbs > tolf) {
-      ++step;
-      if constexpr (!TWO) {
-        if (step > 1 && (double)cntf > 0.0 * npx0) {
-          // window growth test of funICGNQuadtree.m:140 (FP64, recomputed only
-          // when the count of selected g pixels changes)
-          int nws = last_nws;
-          if (cg != last_cg) {
-            const double r = sqrt((double)((ws0 + 1) * (ws0 + 1)) / (double)cg) * wx / 2;
-            if (!isfinite(r)) { err = true; break; }
-            nws = 2 * (int)ceil(r);
-            last_cg = cg;
-            last_nws = nws;
-          }
-          if (nws != wx) {
-            const long long nx1 = x0 - nws / 2, nx3 = x0 + nws / 2, ny1 = y0 - nws / 2, ny3 = y0 + nws / 2;
-            if (!mask_crop_ok32(fr, nx1, nx3, ny1, ny3)) { err = true; break; }
-            if (corners_oob_warp(P, (int)x0, (int)y0, (int)nx1, (int)ny1, nws + 1, nws + 1, a.W, a.H, lane)) { normNew = 1e6f; break; }
-            err = true;
-            break;
-          }
-        }
-      }
-      if (oob) { normNew = 1e6f; break; }
-      // integer base + FP32 offsets of the warp
-      const float flu = floorf(P[4]), flv = floorf(P[5]);
-      const int iu = (int)x0 + (int)flu, iv = (int)y0 + (int)flv;
-      const float fu = P[4] - flu, fv0 = P[5] - flv;
-      const float p0 = 1.f + P[0], p1 = P[1], p2 = P[2], p3 = 1.f + P[3];
-      const float dx0 = (float)(int)(x1 - x0), dy0 = (float)(int)(y1 - y0);
-      const float shift = meanf;  // one-pass variance around meanf
-      // one pass: interpolation, zero/NaN counts, g statistics and sum J g
-      constexpr int NR = 7 + 2 * NQ;
-      float red[NR];
-      {
-        int zg = 0, nang = 0;
-        Kahan sg, qg, kg[NQ];
-        float ng = 0.f;
-        PixIter it(pstart, mx);
-        auto one = [&](int p, int i, int j, float t) {
-          tg[p] = t;
-          if (t != t) nang = 1;
-          if (t == 0.f) ++zg;
-          if (fabsf(t) > 1e-10f) {
-            const float d = t - shift;
-            sg.add(d);
-            qg.add(d * d);
-            ng += 1.f;
-          }
-          float J[NQ];
-          jac(i, j, bw ? (float)bw[p] : 1.f, J);
-#pragma unroll
-          for (int k = 0; k < NQ; ++k) kg[k].add(J[k] * t);
-        };
-        int p = tm.tl;
-        // two pixels per trip so that both pixels' 16 taps are in flight together
-        for (; p + tm.TT < npx; p += 2 * tm.TT) {
-          const int ia = it.i, ja = it.j;
-          it.next();
-          const int ib = it.i, jb = it.j;
-          it.next();
-          const float dxa = dx0 + (float)ia, dya = dy0 + (float)ja;
-          const float dxb = dx0 + (float)ib, dyb = dy0 + (float)jb;
-          const float ta = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dxa + p2 * dya, iv, fv0 + p1 * dxa + p3 * dya);
-          const float tb2 = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dxb + p2 * dyb, iv, fv0 + p1 * dxb + p3 * dyb);
-          one(p, ia, ja, ta);
-          one(p + tm.TT, ib, jb, tb2);
-        }
-        if (p < npx) {
-          const float dx = dx0 + (float)it.i, dy = dy0 + (float)it.j;
-          const float t = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dx + p2 * dy, iv, fv0 + p1 * dx + p3 * dy);
-          one(p, it.i, it.j, t);
-        }
-        red[0] = (float)zg; red[1] = (float)nang;
-        red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
-#pragma unroll
-        for (int k = 0; k < NQ; ++k) { red[7 + 2 * k] = kg[k].s; red[8 + 2 * k] = -kg[k].c; }
-      }
-      tm.template sumf<NR>(red, fscr);
-      if (red[1] > 0.f) { err = true; break; }
-      if (cntf > 0 || red[0] > 0.f) {
-        for (int p = tm.tl; p < npx; p += tm.TT) tmp[p] = tg[p] != 0.f;
-        tm.sync();
-        bwselect_team(tm, tmp, bwg, mx, my, sr, sc, TWO ? 4 : 8, iscr);
-        int anyzero = 0;
-        for (int p = tm.tl; p < npx; p += tm.TT) anyzero |= !bwg[p];
-        if (!tm.any(anyzero, iscr)) bwselect_team(tm, mtile, bwg, mx, my, sr, sc, 8, iscr);
-        if constexpr (TWO) {
-          bw = bwg;
-          f_side();
-        }
-        // the g tile restricted to its selection, and its sums again
-        int cnt = 0;
-        Kahan sg, qg, kg[NQ];
-        float ng = 0.f;
-        PixIter it(pstart, mx);
-        for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
-          const float t = tg[p] * (float)bwg[p];
-          tg[p] = t;
-          cnt += bwg[p];
-          if (fabsf(t) > 1e-10f) {
-            const float d = t - shift;
-            sg.add(d);
-            qg.add(d * d);
-            ng += 1.f;
-          }
-          float J[NQ];
-          jac(it.i, it.j, bw ? (float)bw[p] : 1.f, J);
-#pragma unroll
-          for (int k = 0; k < NQ; ++k) kg[k].add(J[k] * t);
-        }
-        red[0] = (float)cnt; red[1] = 0.f;
-        red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
-#pragma unroll
-        for (int k = 0; k < NQ; ++k) { red[7 + 2 * k] = kg[k].s; red[8 + 2 * k] = -kg[k].c; }
-        tm.template sumf<NR>(red, fscr);
-        cg = (int)red[0];
-      }
-      // g statistics: mean and sqrt((n-1) var) from the shifted one-pass sums
-      const float cntg = red[6];
-      const float s1 = red[2] + red[3], s2 = red[4] + red[5];
-      const float meang = shift + s1 / cntg;
-      const float varg = cntg == 0.f ? __int_as_float(0x7fc00000)
-                                     : (cntg == 1.f ? 0.f : fmaxf(s2 - s1 * s1 / cntg, 0.f) / (cntg - 1.f));
-      const float bottomg = sqrtf((cntg - 1.f) * varg);
-      const float ibf = 1.f / bottomf, ibg = 1.f / bottomg;
-      // b2 = sum J [(tempf - meanf)/bottomf - (tempg - meang)/bottomg]; the
-      // 6-DOF f-side sums come from the set-up stage (read here, not held
-      // in registers across the pixel pass)
-      if constexpr (!TWO) {
-#pragma unroll
-        for (int k = 0; k < NQ; ++k) { jf[k] = ctl->jf[k]; j1[k] = ctl->j1[k]; }
-      }
-      float b2[NQ];
-#pragma unroll
-      for (int k = 0; k < NQ; ++k) {
-        const float jg = red[7 + 2 * k] + red[8 + 2 * k];
-        b2[k] = jf[k] * ibf - (jg - meang * j1[k]) * ibg;
-      }
-      // convergence test (FP32) and the FP64 update, identical on every warp
-      int done = 0;
-      float nb = 0.f;
-      float D[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      if constexpr (TWO) {
-        const float b0 = bottomf * b2[0], b1 = bottomf * b2[1];
-        const float sc2 = 2.f / (bottomf * bottomf);
-        const float tb0 = b0 * sc2 + (float)a.mu * (P[4] - uold0 - vd0);
-        const float tb1 = b1 * sc2 + (float)a.mu * (P[5] - uold1 - vd1);
-        nb = tb0 * tb0 + tb1 * tb1;
-        // FP64 2x2 solve: lane 0 forms DeltaP_5, lane 1 DeltaP_6
-        const double t0 = (double)tb0, t1 = (double)tb1;
-        const double dk = lane == 0 ? -(i00 * t0 + i01 * t1) : -(i10 * t0 + i11 * t1);
-        const float dkf = (float)dk;
-        D[4] = __shfl_sync(0xffffffffu, dkf, 0);
-        D[5] = __shfl_sync(0xffffffffu, dkf, 1);
-      } else {
-        float b[6];
-#pragma unroll
-        for (int q = 0; q < 6; ++q) { b[q] = bottomf * b2[q < NQ ? q : 0]; nb += b[q] * b[q]; }
-        if (hok) {
-          // FP64 solve DeltaP = -H^-1 b: lane q converts b_q, lane k forms row k
-          const double* hr = ctl->Hm + (lane < 6 ? lane : 0) * 6;
-#pragma unroll
-          for (int k = 0; k < 6; ++k) hinv[k] = hr[k];
-          float bl = 0.f;
-#pragma unroll
-          for (int q = 0; q < 6; ++q)
-            if (lane == q) bl = b[q];
-          const double bd = (double)bl;
-          double bb[6];
-#pragma unroll
-          for (int q = 0; q < 6; ++q) bb[q] = shfl_d(bd, q);
-          // depth-3 tree for the row dot product
-          const double d01 = fma(hinv[1], bb[1], hinv[0] * bb[0]);
-          const double d23 = fma(hinv[3], bb[3], hinv[2] * bb[2]);
-          const double d45 = fma(hinv[5], bb[5], hinv[4] * bb[4]);
-          const double dk = (d01 + d23) + d45;
-          const float dkf = (float)(-dk);
-#pragma unroll
-          for (int q = 0; q < 6; ++q) D[q] = __shfl_sync(0xffffffffu, dkf, q);
-        } else {
-          singular_solve6(B.H6 + (size_t)item * 21, b, D);
-        }
-      }
-      float nN = sqrtf(nb);
-      const float nA = nN;
-      if (step == 1) normInit = nN;
-      nN = normInit > tolf ? nN / normInit : 0.f;
-      normNew = nN;
-      normAbs = nA;
-      if (nN < tolf || nA < tolf) done = 1;
-      else if (!compose_warp(P, D, lane)) done = 2;
-      else ++nupd;
-      if (done) break;
-      oob = corners_oob_warp(P, (int)x0, (int)y0, (int)x1, (int)y1, mx, my, a.W, a.H, lane);
-    }
-    if (run) {
-      if (err) { code = err_code; nan_out = true; }
-      else {
-        code = step;
-        if (!(normNew < tolf || normAbs < tolf)) code = kMaxIter + 1;
-        if (isnan(normNew)) code = kMaxIter + 1;
-        if constexpr (TWO) {
-          float v[1] = {0.f};
-          for (int p = tm.tl; p < npx; p += tm.TT) v[0] += fabsf(tf[p]);
-          tm.template sumf<1>(v, fscr);
-          sabs = v[0];
-        }
-        if (sabs < 1e-6f) code = kMaxIter + 3;
-      }
-    }
-    if (tm.tl == 0) {
-      a.conv[item] = code;
-      // a subset that never updated P returns its initial guess bit-exactly
-      const bool moved = nupd > 0;
-      if constexpr (TWO) {
-        a.U[2 * item] = nan_out ? nan("") : (moved ? (double)P[4] : a.UOld[2 * item]);
-        a.U[2 * item + 1] = nan_out ? nan("") : (moved ? (double)P[5] : a.UOld[2 * item + 1]);
-      } else {
-        a.U[2 * item] = nan_out ? nan("") : (moved ? (double)P[4] : a.U0[2 * item]);
-        a.U[2 * item + 1] = nan_out ? nan("") : (moved ? (double)P[5] : a.U0[2 * item + 1]);
-      }
-      if constexpr (!TWO) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) a.F[4 * item + k] = nan_out ? nan("") : (double)P[k];
-        if (a.Hpk && nan_out)
-          for (int q = 0; q < 21; ++q) a.Hpk[(size_t)q * Ntot + item] = 0.0;
-      }
-    }
-    tm.sync();
+    run_subset<TW, TWO, STAGE>(B, tm, item, base, ctl, fscr, iscr, gbase, smpx);
   }
 }
 
-// FP64 Cholesky factorisation and inverse of each subset's 6x6 Hessian, one
-// thread per subset (between the set-up and iteration stages).  A matrix whose
-// factorisation fails gets Hinv6[0] = NaN; the iteration stage then solves
-// with LU and pivoting as MATLAB's mldivide does for such a matrix.
+// The persistent kernel.  Without B.split every subset runs on a team of TW
+// warps.  With B.split (TW > 1) the queue is ordered by decreasing size and
+// the first *B.n_big positions (subsets of at least B.big_ws pixels a side)
+// run on teams of TW warps; once they are all taken, each warp of a team
+// pulls the remaining small subsets on its own, in a 1/TW share of the team's
+// shared slot (B.smem_px_small tile pixels).  The largest subsets thus start
+// first and get the widest teams, and no warp idles while small work is left.
+//
+// Shared memory per team: smem_px floats (tempg) [+ smem_px floats (tempf,
+// 2-DOF)] + 4 smem_px bytes of bitmaps, then the control block and reduction
+// scratch.  Global scratch: one slice of the same layout for npx_max pixels
+// per warp (a team uses the slice of its first warp).
+//
+// Stages (B.stage): 0 runs the 2-DOF form fused; for the 6-DOF form stage 1
+// does the per-subset set-up (window, masks, f statistics, FP32 Hessian) and
+// stage 2 the iterations with the inverse Hessian the factor kernel produced
+// in FP64 between them.  Every warp of a team holds the team totals after each
+// reduction and runs the same FP64 update on them, so all warps carry
+// bit-identical P without a shared-memory broadcast.
+template <int TW, bool TWO, int STAGE>
+__global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  const int nf = B.frames > 0 ? B.frames : 1;
+  const int Ntot = B.a.N * nf;
+  const int warp = threadIdx.x >> 5;
+  const size_t gstride = (size_t)B.a.npx_max * (TWO ? 8 : 4) + 4 * (size_t)B.a.npx_max;
+  const long long gwarp0 = (long long)blockIdx.x * (blockDim.x >> 5);
+  // team slot bytes (the layout of batched_team_bytes)
+  const size_t tb = ((size_t)B.smem_px * (TWO ? 8 : 4) + 4 * (size_t)B.smem_px + 15) / 16 * 16 +
+                    sizeof(TeamCtl) + sizeof(float) * 32 * TW + 16 * TW + 64;
+  Team<TW> tm;
+  tm.id = threadIdx.x / Team<TW>::TT;
+  tm.tl = threadIdx.x % Team<TW>::TT;
+  unsigned char* tbase = dsm + tb * tm.id;
+  const bool split = TW > 1 && B.split;
+  const int split_q = split ? min(*B.n_big * nf, Ntot) : Ntot;
+  team_loop<TW, TWO, STAGE>(B, tm, B.queue_head, 0, split_q, tbase, B.smem_px,
+                            B.scratch + gstride * (gwarp0 + (long long)tm.id * TW));
+  if constexpr (TW > 1) {
+    if (split) {
+      Team<1> t1;
+      t1.id = warp;
+      t1.tl = threadIdx.x & 31;
+      const size_t sub = (tb / TW) & ~(size_t)15;
+      team_loop<1, TWO, STAGE>(B, t1, B.queue_head + 1, split_q, Ntot,
+                               tbase + sub * (warp % TW), B.smem_px_small,
+                               B.scratch + gstride * (gwarp0 + warp));
+    }
+  }
+}
+
+// FP64 inverse of each subset's 6x6 Hessian, one thread per subset (between
+// the set-up and iteration stages): by Cholesky, or, when that fails, by LU
+// with partial pivoting as MATLAB's mldivide falls back for such a matrix (a
+// singular matrix gives a non-finite inverse, as H \ b gives non-finite steps).
+// Inverse of the packed symmetric 6x6 H (lower, row-major) by Gauss-Jordan
+// elimination of [H | I] with partial pivoting (the row operations of LU with
+// partial pivoting, applied to the six unit right-hand sides at once); a zero
+// pivot gives a non-finite inverse.  Out of line so that its local arrays
+// exist only on this rare path.
+__device__ __noinline__ void lu_inverse6(const double* __restrict__ H, double* __restrict__ out) {
+  double A[6][12];
+  for (int r = 0; r < 6; ++r)
+    for (int c2 = 0; c2 < 6; ++c2) {
+      A[r][c2] = r >= c2 ? H[r * (r + 1) / 2 + c2] : H[c2 * (c2 + 1) / 2 + r];
+      A[r][6 + c2] = r == c2 ? 1.0 : 0.0;
+    }
+  for (int k = 0; k < 6; ++k) {
+    int p = k;
+    double amax = fabs(A[k][k]);
+    for (int i = k + 1; i < 6; ++i)
+      if (fabs(A[i][k]) > amax) { amax = fabs(A[i][k]); p = i; }
+    if (p != k)
+      for (int j = 0; j < 12; ++j) { const double t = A[k][j]; A[k][j] = A[p][j]; A[p][j] = t; }
+    const double inv = 1.0 / A[k][k];
+    for (int j = 0; j < 12; ++j) A[k][j] *= inv;
+    for (int i = 0; i < 6; ++i) {
+      if (i == k) continue;
+      const double f = A[i][k];
+      for (int j = 0; j < 12; ++j) A[i][j] -= f * A[k][j];
+    }
+  }
+  for (int r = 0; r < 6; ++r)
+    for (int c2 = 0; c2 < 6; ++c2) out[r * 6 + c2] = A[r][6 + c2];
+}
+
 __global__ void __launch_bounds__(128) factor6_kernel(const SubsetState6* __restrict__ st,
                                                       const double* __restrict__ H6,
                                                       double* __restrict__ Hinv6, int n) {
@@ -971,7 +1051,7 @@ __global__ void __launch_bounds__(128) factor6_kernel(const SubsetState6* __rest
   chol6_factor(H, C);
   double* out = Hinv6 + (size_t)t * 36;
   if (!C.ok) {
-    out[0] = nan("");
+    lu_inverse6(H6 + (size_t)t * 21, out);
     return;
   }
 #pragma unroll
@@ -1016,6 +1096,7 @@ cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, c
     case 1: return launch_stage<1>(b, blocks, threads, s);
     case 2: return launch_stage<2>(b, blocks, threads, s);
     case 4: return launch_stage<4>(b, blocks, threads, s);
+    case 8: return launch_stage<8>(b, blocks, threads, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -1038,6 +1119,7 @@ int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px) {
     case 1: if (two) { STDIC_OCC(1, true, 0) } else { STDIC_OCC(1, false, 2) } break;
     case 2: if (two) { STDIC_OCC(2, true, 0) } else { STDIC_OCC(2, false, 2) } break;
     case 4: if (two) { STDIC_OCC(4, true, 0) } else { STDIC_OCC(4, false, 2) } break;
+    case 8: if (two) { STDIC_OCC(8, true, 0) } else { STDIC_OCC(8, false, 2) } break;
     default: return 0;
   }
 #undef STDIC_OCC

@@ -51,8 +51,11 @@ struct BatchedArgs {
   const float* g32;
   const float* dfdx32;
   const float* dfdy32;
-  const int32_t* order;   // node order of the work queue (largest tiles first)
-  int* queue_head;        // global work counter (scratch)
+  const int32_t* order;   // node order of the work queue
+  int* queue_head;        // two global work counters (team phase, single-warp phase)
+  const int* n_big;       // split: number of queue entries of the team phase (device)
+  int split;              // 1: large subsets on teams of warps_per_subset, the rest on single warps
+  int smem_px_small;      // split: tile pixels of a single warp's share of the team slot
   int warps_per_subset;
   int two_dof;
   int frames;             // number of frame pairs stacked in g32 (multi-frame)
@@ -64,7 +67,7 @@ struct BatchedArgs {
   int stage;
   void* st6;              // SubsetState6 per item
   double* H6;             // 21 per item: packed lower Hessian (row-major)
-  double* Hinv6;          // 36 per item: inverse Hessian (row-major), Hinv6[0] = NaN if singular
+  double* Hinv6;          // 36 per item: FP64 inverse Hessian (row-major)
 };
 
 // Per-subset state handed from the 6-DOF set-up stage to the iterations.
@@ -84,7 +87,7 @@ cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hin
 
 // Size of one team's shared slot / global slice of the batched kernel.
 size_t batched_team_bytes(int sm_px, bool two, int tw);
-size_t batched_scratch_bytes(int npx_max, bool two, long long teams);
+size_t batched_scratch_bytes(int npx_max, bool two, long long warps);
 int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px);
 
 cudaError_t launch_interp(const void* F, long long M, long long N, long long P, const void* X,
@@ -100,8 +103,15 @@ cudaError_t launch_icgn2_plain(const IcgnArgs& a, cudaStream_t s);
 cudaError_t launch_badpoints(int32_t* conv, int N, double* U, double* F, int two_dof,
                              int* badnum_dev, cudaStream_t s);
 cudaError_t launch_to_f32(const double* in, float* out, long long n, cudaStream_t s);
+// Counting sort of the nodes by subset size into order: ascending 0 sorts by
+// decreasing size, 1 by increasing size, 2 puts the subsets of at least big_ws
+// pixels a side first (decreasing) and the rest after them (increasing).
+// n_big (optional) receives the number of nodes whose size is at least big_ws.
 cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int ws_all, int N,
-                               int32_t* order, int* scratch, cudaStream_t s, int ascending = 0);
+                               int32_t* order, int* n_big, cudaStream_t s, int ascending = 0,
+                               int big_ws = 0);
+// Largest tile of a single warp's share of a split team slot.
+int batched_small_px(int sm_px, bool two, int tw);
 cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, cudaStream_t s);
 
 // Subpb2 (FEM).  All pointers are device pointers.

@@ -403,23 +403,33 @@ cudaError_t launch_to_f32(const double* in, float* out, long long n, cudaStream_
 __global__ void __launch_bounds__(1024) build_queue_kernel(const int32_t* __restrict__ ws_list,
                                                            const int32_t* __restrict__ wsl2,
                                                            int ws_all, int N, int32_t* order,
-                                                           int ascending) {
+                                                           int ascending, int big_ws, int* n_big) {
   __shared__ int hist[256];
   __shared__ int start[256];
   for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
   __syncthreads();
+  // order 0: larger subsets first; 1: smaller first; 2: subsets of at least
+  // big_ws pixels a side first (larger first), then the rest smaller first
+  const int bw = min(max(big_ws, 1), 255);
   auto key = [&](int k) {
     int w = ws_all;
     if (wsl2) w = max(wsl2[k], wsl2[N + k]);
     else if (ws_list) w = ws_list[k];
     const int b = min(max(w, 0), 255);
-    return ascending ? b : 255 - b;  // larger subsets first unless ascending
+    if (ascending == 2) return b >= bw ? 255 - b : 256 - bw + b;
+    return ascending ? b : 255 - b;
   };
   for (int k = threadIdx.x; k < N; k += blockDim.x) atomicAdd(&hist[key(k)], 1);
   __syncthreads();
   if (threadIdx.x == 0) {
     int acc = 0;
     for (int b = 0; b < 256; ++b) { start[b] = acc; acc += hist[b]; }
+    if (n_big) {
+      int nb = 0;
+      for (int w = max(big_ws, 0); w < 256; ++w)
+        nb += hist[ascending == 2 ? 255 - w : (ascending ? w : 255 - w)];
+      *n_big = nb;
+    }
   }
   __syncthreads();
   for (int k = threadIdx.x; k < N; k += blockDim.x) {
@@ -429,10 +439,10 @@ __global__ void __launch_bounds__(1024) build_queue_kernel(const int32_t* __rest
 }
 
 cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int ws_all, int N,
-                               int32_t* order, int* scratch, cudaStream_t s, int ascending) {
-  (void)scratch;
+                               int32_t* order, int* n_big, cudaStream_t s, int ascending,
+                               int big_ws) {
   if (N <= 0) return cudaSuccess;
-  build_queue_kernel<<<1, 1024, 0, s>>>(ws_list, wsl2, ws_all, N, order, ascending);
+  build_queue_kernel<<<1, 1024, 0, s>>>(ws_list, wsl2, ws_all, N, order, ascending, big_ws, n_big);
   return cudaGetLastError();
 }
 

@@ -396,33 +396,37 @@ bool frame_ok(const stdic_frame* fr) {
 // split > 0: subsets of at least `split` pixels a side run on teams of tw
 // warps, the rest on single warps (queue in decreasing size).
 struct BatchedCand {
-  int tw, threads, split, smem_per_warp, blocks, smem_px, smem_px_small;
+  int tw, threads, split, smem_per_warp, gtile_per_warp, blocks, smem_px, smem_px_small;
   size_t scratch;
 };
 
 std::vector<BatchedCand> batched_candidates(stdic_ctx* c, bool two, int npx_max, int Ntot) {
   std::vector<BatchedCand> out;
-  // (warps per team, threads, split size, shared bytes per warp).  A smaller
-  // shared slot leaves more of the SM's unified L1 to cache the gathers of g
-  // and the gradients; tiles that do not fit use the warp's global slice.
-  const int shapes[][4] = {{1, 128, 0, 12800}, {1, 256, 0, 12800}, {2, 256, 0, 12800},
-                           {4, 256, 0, 12800}, {4, 256, 32, 12800}, {4, 256, 64, 12800},
-                           {8, 256, 64, 12800}, {1, 256, 0, 4800},   {4, 256, 64, 4800},
-                           {1, 256, 0, 2800},  {4, 256, 64, 2800}};
+  // (warps per team, threads, split size, shared bytes per warp for the
+  // per-pixel arrays, floats per warp for the staged g footprint).  A smaller
+  // per-pixel slot leaves more of the SM's unified L1 to cache the gradients;
+  // tiles that do not fit use the warp's global slice, footprints that do not
+  // fit are gathered from global memory.
+  const int shapes[][5] = {{1, 256, 0, 12800, 0},   {4, 256, 64, 2800, 0},
+                           {1, 256, 0, 2800, 1600}, {1, 256, 0, 4800, 1600},
+                           {4, 256, 32, 2800, 1300}, {4, 256, 64, 2800, 1300},
+                           {8, 256, 64, 2800, 650},  {4, 256, 32, 2800, 1600},
+                           {2, 256, 32, 2800, 1300}};
   for (auto& sh : shapes) {
-    const int tw = sh[0], threads = sh[1], split = sh[2], per_warp = sh[3];
+    const int tw = sh[0], threads = sh[1], split = sh[2], per_warp = sh[3], gt_warp = sh[4];
     const int teams_per_block = threads / (32 * tw);
     const int bpp = two ? 12 : 8;
     int smem_px = (int)((per_warp * tw - 512 - 32 * 4 * tw) / bpp);
     smem_px = std::max(64, std::min(smem_px, npx_max));
-    const int per_sm = stdic::batched_blocks_per_sm(tw, two, threads, smem_px);
+    const int gtile = gt_warp * tw;
+    const int per_sm = stdic::batched_blocks_per_sm(tw, two, threads, smem_px, gtile);
     if (per_sm <= 0) continue;
     int blocks = c->nsm * per_sm;
     const int units_per_block = split ? threads / 32 : teams_per_block;
     blocks = std::max(1, std::min(blocks, (Ntot + units_per_block - 1) / units_per_block));
     const long long warps = (long long)blocks * (threads / 32);
-    const int small_px = split ? stdic::batched_small_px(smem_px, two, tw) : 0;
-    out.push_back({tw, threads, split, per_warp, blocks, smem_px, small_px,
+    const int small_px = split ? stdic::batched_small_px(smem_px, two, tw, gtile) : 0;
+    out.push_back({tw, threads, split, per_warp, gt_warp, blocks, smem_px, small_px,
                    stdic::batched_scratch_bytes(npx_max, two, warps)});
   }
   return out;
@@ -464,6 +468,8 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
     b.smem_px = cd.smem_px;
     b.split = cd.split > 0 ? 1 : 0;
     b.smem_px_small = cd.smem_px_small;
+    b.gtile = cd.gtile_per_warp * cd.tw;
+    b.gtile_small = cd.split ? cd.gtile_per_warp : 0;
     // Single warps take the queue smallest first, so that the small subsets
     // that run to the iteration limit start early; split teams take the large
     // subsets largest first, then single warps the rest smallest first.
@@ -484,6 +490,14 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
         rc = check_launch(c, stdic::launch_factor6((const stdic::SubsetState6*)b.st6, b.H6, b.Hinv6, Ntot, c->stream),
                           "Hessian factorisation");
         if (rc) return rc;
+        if (cd.split && b.frames <= 1) {
+          // masked subsets refill their selections every iteration: they join
+          // the large ones on the wide teams in the iteration stage
+          rc = check_launch(c, stdic::launch_build_queue6((const stdic::SubsetState6*)b.st6, b.a.N, cd.split,
+                                                          (int32_t*)b.order, c->scal + 6, c->stream),
+                            "queue");
+          if (rc) return rc;
+        }
       }
     }
     return STDIC_OK;
@@ -505,8 +519,8 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);
         if (ms < bt) { bt = ms; best = (int)(&cd - cands.data()); }
         if (tune_log())
-          std::fprintf(stderr, "stdic tune: N=%d two=%d warps/team=%d threads=%d split=%d smem/warp=%d blocks=%d smem_px=%d: %.3f ms\n",
-                       Ntot, (int)two, cd.tw, cd.threads, cd.split, cd.smem_per_warp, cd.blocks, cd.smem_px, ms);
+          std::fprintf(stderr, "stdic tune: N=%d two=%d warps/team=%d threads=%d split=%d smem/warp=%d gtile/warp=%d blocks=%d smem_px=%d: %.3f ms\n",
+                       Ntot, (int)two, cd.tw, cd.threads, cd.split, cd.smem_per_warp, cd.gtile_per_warp, cd.blocks, cd.smem_px, ms);
       }
     }
     it = c->tune.emplace(key, best).first;

@@ -1,13 +1,15 @@
 // Batched IC-GN (6-DOF first pass and 2-DOF Subpb1) as one persistent kernel.
 //
-// A team of TW warps (one warp by default) pulls the next subset from a global
-// work queue ordered by decreasing subset size, so the longest solves start
-// first, and runs it with the control flow, mask logic and result codes of the
-// plain FP64 kernels (funICGNQuadtree.m / funICGN_Subpb1.m).
+// Teams of warps pull subsets from a global work queue and run each with the
+// control flow, mask logic and result codes of the plain FP64 kernels
+// (funICGNQuadtree.m / funICGN_Subpb1.m).  The queue is a counting sort by
+// subset size; in the split form the large subsets go first to teams of
+// several warps and the rest to single warps, smallest first, so that neither
+// a large subset nor a small one that runs to the iteration limit starts late.
 //
 // Per-subset scratch (interpolated g tile, tempf for the 2-DOF form, four
 // flood-fill bitmaps) lives in shared memory when the tile fits the team's
-// shared slot and otherwise in a per-team slice of a global scratch buffer, so
+// shared slot and otherwise in a per-warp slice of a global scratch buffer, so
 // occupancy is set by registers, not by the largest subset of the batch.
 //
 // Precision: warped positions are an integer base plus an FP32 offset;
@@ -15,9 +17,12 @@
 // Kahan-compensated FP32 (b-vector and g statistics; the g variance is a
 // one-pass shifted sum around meanf), reduced across lanes in FP32 together
 // with their compensations; the Hessian is accumulated in plain FP32 (it only
-// scales the step, never the converged point).  Team totals, the Cholesky
-// factor of the 6x6 Hessian (once per subset), the triangular solves of every
-// iteration and the warp-parameter update are FP64.
+// scales the step, never the converged point).  The 6x6 Hessian is reduced,
+// factorised (Cholesky, else LU with partial pivoting) and inverted in FP64
+// once per subset; every iteration applies that FP64 inverse to the FP32
+// right-hand side in double-float arithmetic (FP32 pairs with exact products
+// and error-free sums, about 2^-48 relative), because GB300's FP64 pipe issues
+// at a small fraction of the FP32 rate.  The warp-parameter update is FP32.
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -83,11 +88,6 @@ struct Team {
     }
   }
 };
-
-// Warp-parallel FP64 Gauss-Newton update.  Lane k < 6 holds row k of H^-1
-// (6x6 form) and produces DeltaP_k; the inverse-compositional update of P and
-// the image-bounds test of the next warp are also split over lanes, so the
-// narrow FP64 pipe sees a few dozen instructions per iteration.
 
 // P <- P o DeltaP^-1 (funICGNQuadtree.m:393-411) in FP32.  Every lane holds
 // the same D and P and computes all six parameters, so the lanes stay
@@ -211,16 +211,55 @@ STDIC_DEV void bwselect_warp_bits(const uint8_t* allow, uint8_t* sel, int m, int
   __syncwarp();
 }
 
-// flood fill of bwselect restricted to a team (see bwselect_block)
+// The same fill for m <= 32, n <= 32 with one 32-bit column word per lane.
+STDIC_DEV uint32_t run_fill32(uint32_t A, uint32_t S) {
+  const uint32_t up = ((A + S) ^ A) & A;
+  const uint32_t Ar = __brev(A), Sr = __brev(S);
+  const uint32_t dn = __brev(((Ar + Sr) ^ Ar) & Ar);
+  return up | dn | S;
+}
+
+STDIC_DEV void bwselect_warp_bits32(const uint8_t* allow, uint8_t* sel, int m, int n, int r1, int c1,
+                                    int conn) {
+  const int lane = threadIdx.x & 31;
+  uint32_t A = 0, S = 0;
+  if (lane < n) {
+    const uint8_t* col = allow + lane * m;
+    for (int i = 0; i < m; ++i) A |= (uint32_t)(col[i] != 0) << i;
+  }
+  if (r1 >= 1 && r1 <= m && c1 >= 1 && c1 <= n && lane == c1 - 1) S = A & (1u << (r1 - 1));
+  S = run_fill32(A, S);
+  for (;;) {
+    const uint32_t L = __shfl_up_sync(0xffffffffu, S, 1), R = __shfl_down_sync(0xffffffffu, S, 1);
+    uint32_t nb = (lane > 0 ? L : 0u) | (lane < 31 ? R : 0u);
+    if (conn == 8) nb |= (nb << 1) | (nb >> 1);
+    const uint32_t t = S | (nb & A);
+    const uint32_t f = t != S ? run_fill32(A, t) : t;
+    const bool changed = f != S;
+    S = f;
+    if (!__any_sync(0xffffffffu, changed)) break;
+  }
+  if (lane < n) {
+    uint8_t* col = sel + lane * m;
+    for (int i = 0; i < m; ++i) col[i] = (uint8_t)((S >> i) & 1u);
+  }
+  __syncwarp();
+}
+
+// flood fill of bwselect restricted to a team (see bwselect_block): tiles up
+// to 64 x 96 by the first warp of the team with bitmaps, larger ones by
+// alternating sweeps of the whole team
 template <int TW>
 STDIC_DEV void bwselect_team(const Team<TW>& tm, const uint8_t* allow, uint8_t* sel_, int m, int n,
                              int r1, int c1, int conn, int* iscr) {
-  if constexpr (TW == 1) {
-    if (m <= 64 && n <= 96) {
-      __syncwarp();
-      bwselect_warp_bits(allow, sel_, m, n, r1, c1, conn);
-      return;
+  if (m <= 64 && n <= 96) {
+    tm.sync();
+    if (tm.tl < 32) {
+      if (m <= 32 && n <= 32) bwselect_warp_bits32(allow, sel_, m, n, r1, c1, conn);
+      else bwselect_warp_bits(allow, sel_, m, n, r1, c1, conn);
     }
+    tm.sync();
+    return;
   }
   volatile uint8_t* sel = sel_;
   const int npx = m * n;
@@ -405,40 +444,85 @@ STDIC_DEV float dot_df(const float* hh, const float* hl, const float* x) {
   return __fadd_rn(S, E);
 }
 
+// Team slot layout: per-pixel arrays, the staged g footprint, the control
+// block and the reduction scratch.
+__host__ __device__ __forceinline__ size_t tiles_bytes(int px, bool two) {
+  return ((size_t)px * (two ? 8 : 4) + 5 * (size_t)px + 15) / 16 * 16;
+}
+// Bytes of one warp's global scratch slice (the per-pixel arrays for npx_max
+// pixels), a multiple of 16 so that every slice keeps the alignment of the
+// buffer for its float arrays.
+__host__ __device__ __forceinline__ size_t slice_bytes(int npx_max, bool two) {
+  return ((size_t)npx_max * (two ? 8 : 4) + 5 * (size_t)npx_max + 15) / 16 * 16;
+}
+__host__ __device__ __forceinline__ size_t gtile_bytes(int gt) {
+  return ((size_t)(gt > 0 ? gt : 0) * 4 + 15) / 16 * 16;
+}
+__host__ __device__ __forceinline__ size_t team_bytes(int px, bool two, int tw, int gt) {
+  return tiles_bytes(px, two) + gtile_bytes(gt) + sizeof(TeamCtl) + sizeof(float) * 32 * tw + 16 * tw + 64;
+}
+
+// Asynchronous 4-byte global -> shared copy (no register staging) and the
+// wait for all of this thread's copies.
+STDIC_DEV void cp_async4(float* smem, const float* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+STDIC_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// cubic32 reading its 16 taps from a staged tile of g whose first element is
+// image element (gx0, gy0) (0-based) and whose rows are gtw floats: the same
+// taps and arithmetic as cubic32, so the same result.  Local indices are
+// clamped to the tile, so a read never leaves it.
+STDIC_DEV float cubic_tile(const float* __restrict__ gt, int gtw, int gth, int gx0, int gy0, int W,
+                           int H, int iu, float su, int iv, float sv) {
+  const float fu = floorf(su), fv = floorf(sv);
+  const float dx = su - fu, dy = sv - fv;
+  const int xb = min(max(iu + (int)fu - 2, 0), W - 4);
+  const int yb = min(max(iv + (int)fv - 2, 0), H - 4);
+  const int lx = min(max(xb - gx0, 0), gtw - 4), ly = min(max(yb - gy0, 0), gth - 4);
+  const float dx2 = dx * dx, dx3 = dx2 * dx, dy2 = dy * dy, dy3 = dy2 * dy;
+  const float wx0 = 0.5f * (-dx + 2.f * dx2 - dx3), wx1 = 0.5f * (2.f - 5.f * dx2 + 3.f * dx3);
+  const float wx2 = 0.5f * (dx + 4.f * dx2 - 3.f * dx3), wx3 = 0.5f * (-dx2 + dx3);
+  const float wy0 = 0.5f * (-dy + 2.f * dy2 - dy3), wy1 = 0.5f * (2.f - 5.f * dy2 + 3.f * dy3);
+  const float wy2 = 0.5f * (dy + 4.f * dy2 - 3.f * dy3), wy3 = 0.5f * (-dy2 + dy3);
+  const float* r = gt + ly * gtw + lx;
+  const float s0 = wx0 * r[0] + wx1 * r[1] + wx2 * r[2] + wx3 * r[3];
+  r += gtw;
+  const float s1 = wx0 * r[0] + wx1 * r[1] + wx2 * r[2] + wx3 * r[3];
+  r += gtw;
+  const float s2 = wx0 * r[0] + wx1 * r[1] + wx2 * r[2] + wx3 * r[3];
+  r += gtw;
+  const float s3 = wx0 * r[0] + wx1 * r[1] + wx2 * r[2] + wx3 * r[3];
+  return wy0 * s0 + wy1 * s1 + wy2 * s2 + wy3 * s3;
+}
+
 }  // namespace
 
-size_t batched_team_bytes(int sm_px, bool two, int tw) {
-  return ((size_t)sm_px * (two ? 8 : 4) + 4 * (size_t)sm_px + 15) / 16 * 16 + sizeof(TeamCtl) +
-         sizeof(float) * 32 * tw + 16 * tw + 64;
+size_t batched_team_bytes(int sm_px, bool two, int tw, int gtile) {
+  return team_bytes(sm_px, two, tw, gtile);
 }
 
 size_t batched_scratch_bytes(int npx_max, bool two, long long warps) {
-  return ((size_t)npx_max * (two ? 8 : 4) + 4 * (size_t)npx_max) * (size_t)warps + 256;
+  return slice_bytes(npx_max, two) * (size_t)warps + 256;
 }
 
-int batched_small_px(int sm_px, bool two, int tw) {
-  const size_t sub = (batched_team_bytes(sm_px, two, tw) / tw) & ~(size_t)15;
-  const long long fixed = (long long)(sizeof(TeamCtl) + sizeof(float) * 32 + 16 + 64 + 15);
+int batched_small_px(int sm_px, bool two, int tw, int gtile) {
+  const size_t sub = (team_bytes(sm_px, two, tw, gtile) / tw) & ~(size_t)15;
+  const int gs = gtile / tw;
+  const long long fixed = (long long)(gtile_bytes(gs) + sizeof(TeamCtl) + sizeof(float) * 32 + 16 + 64 + 15);
   long long px = ((long long)sub - fixed) / (two ? 12 : 8);
-  while (px > 0 && batched_team_bytes((int)px, two, 1) > sub) --px;
+  while (px > 0 && team_bytes((int)px, two, 1, gs) > sub) --px;
   return (int)(px > 0 ? px : 0);
 }
 
-// Shared memory per team: smem_px floats (tempg) [+ smem_px floats (tempf,
-// 2-DOF)] + 4 smem_px bytes of bitmaps, then the control block and reduction
-// scratch.  Global scratch per team: the same layout for npx_max pixels.
-//
-// Stages (B.stage): 0 runs the 2-DOF form fused; for the 6-DOF form stage 1
-// does the per-subset set-up (window, masks, f statistics, FP32 Hessian) and
-// stage 2 the iterations with the inverse Hessian the factor kernel produced
-// in FP64 between them.  Every warp of a team holds the team totals after each
-// reduction and runs the same FP64 update on them, so all warps carry
-// bit-identical P without a shared-memory broadcast.
 // One subset on one team: set-up, iterations and outputs.  base/ctl/fscr/iscr
-// are the team's shared slot of smpx tile pixels, gbase its global slice.
+// are the team's shared slot of smpx tile pixels, gt its staging area of gcap
+// floats for the warped g footprint, gbase its global slice.
 template <int TW, bool TWO, int STAGE>
 STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, unsigned char* base,
-                          TeamCtl* ctl, float* fscr, int* iscr, unsigned char* gbase, int smpx) {
+                          TeamCtl* ctl, float* fscr, int* iscr, unsigned char* gbase, int smpx,
+                          float* gt, int gcap) {
   const IcgnArgs& a = B.a;
   const int lane = threadIdx.x & 31;
   constexpr int stage = STAGE;
@@ -480,7 +564,8 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
   int4 pstart = make_int4(0, 0, 0, 0);  // PixIter start of this thread for the tile
   float* tg = nullptr;
   float* tf = nullptr;
-  uint8_t *mtile = nullptr, *bwf = nullptr, *bwg = nullptr, *tmp = nullptr;
+  uint8_t *mtile = nullptr, *bwf = nullptr, *bwg = nullptr, *tmp = nullptr, *bwm8 = nullptr;
+  bool have_m8 = false;  // bwm8 holds the 8-connected selection of the mask tile
   bool has_masked = false;
   bool decided = false;  // outputs of this subset already written by the set-up stage
   const double npx0 = (double)(wx + 1) * (double)(wy + 1);
@@ -552,6 +637,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     bwf = mtile + cap;
     bwg = bwf + cap;
     tmp = bwg + cap;
+    bwm8 = tmp + cap;
     int z = 0;
     PixIter it(pstart, mx);
     for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
@@ -722,9 +808,20 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         // when the count of selected g pixels changes)
         int nws = last_nws;
         if (cg != last_cg) {
-          const double r = sqrt((double)((ws0 + 1) * (ws0 + 1)) / (double)cg) * wx / 2;
-          if (!isfinite(r)) { err = true; break; }
-          nws = 2 * (int)ceil(r);
+          // nws = 2 ceil(r), r = sqrt((ws0+1)^2 / cg) wx / 2, decided in
+          // integers: ceil(r) is the least k with 4 k^2 cg >= (ws0+1)^2 wx^2.
+          // When r is not an integer it lies at least 1/(8 cg k) from one,
+          // far beyond the FP64 rounding of the reference's expression, so
+          // both give the same k; an integer r takes the FP64 value itself.
+          if (cg <= 0) { err = true; break; }
+          const long long A = (long long)(ws0 + 1) * (ws0 + 1);
+          const long long rhs = A * (long long)wx * (long long)wx;
+          long long k = (long long)ceilf(sqrtf((float)A / (float)cg) * (float)wx * 0.5f);
+          if (k < 0) k = 0;
+          while (k > 0 && 4 * (k - 1) * (k - 1) * cg >= rhs) --k;
+          while (4 * k * k * cg < rhs) ++k;
+          if (4 * k * k * cg == rhs) k = (long long)ceil(sqrt((double)A / (double)cg) * wx / 2);
+          nws = 2 * (int)k;
           last_cg = cg;
           last_nws = nws;
         }
@@ -768,8 +865,47 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
 #pragma unroll
         for (int k = 0; k < NQ; ++k) kg[k].add(J[k] * t);
       };
+      // Stage the warped footprint of g in shared memory when it fits: the
+      // tap range follows from the four corners (the warp is affine), with a
+      // one-pixel margin, clipped to the image.
+      int gx0 = 0, gy0 = 0, gtw = 0, gth = 0;
+      bool staged = false;
+      if (gcap > 0) {
+        const float xa = dx0, xb2 = dx0 + (float)(mx - 1), ya = dy0, yb2 = dy0 + (float)(my - 1);
+        const float u00 = fu + p0 * xa + p2 * ya, u10 = fu + p0 * xb2 + p2 * ya;
+        const float u01 = fu + p0 * xa + p2 * yb2, u11 = fu + p0 * xb2 + p2 * yb2;
+        const float v00 = fv0 + p1 * xa + p3 * ya, v10 = fv0 + p1 * xb2 + p3 * ya;
+        const float v01 = fv0 + p1 * xa + p3 * yb2, v11 = fv0 + p1 * xb2 + p3 * yb2;
+        const float umin = fminf(fminf(u00, u10), fminf(u01, u11)), umax = fmaxf(fmaxf(u00, u10), fmaxf(u01, u11));
+        const float vmin = fminf(fminf(v00, v10), fminf(v01, v11)), vmax = fmaxf(fmaxf(v00, v10), fmaxf(v01, v11));
+        if (umin >= -1e6f && umax <= 1e6f && vmin >= -1e6f && vmax <= 1e6f) {
+          const long long ax0 = (long long)iu + (long long)floorf(umin) - 3;
+          const long long ax1 = (long long)iu + (long long)floorf(umax) + 2;
+          const long long ay0 = (long long)iv + (long long)floorf(vmin) - 3;
+          const long long ay1 = (long long)iv + (long long)floorf(vmax) + 2;
+          const long long cx0 = ax0 < 0 ? 0 : ax0, cx1 = ax1 > fr.W - 1 ? fr.W - 1 : ax1;
+          const long long cy0 = ay0 < 0 ? 0 : ay0, cy1 = ay1 > fr.H - 1 ? fr.H - 1 : ay1;
+          const long long w_ = cx1 - cx0 + 1, h_ = cy1 - cy0 + 1;
+          if (w_ >= 4 && h_ >= 4 && w_ <= gcap && h_ <= gcap && w_ * h_ <= gcap) {
+            gx0 = (int)cx0; gy0 = (int)cy0; gtw = (int)w_; gth = (int)h_;
+            staged = true;
+          }
+        }
+      }
+      if (staged) {
+        PixIter ti(tm.tl, tm.TT, gtw);
+        const int ng_ = gtw * gth;
+        for (int k = tm.tl; k < ng_; k += tm.TT, ti.next())
+          cp_async4(gt + k, fr.g + (long long)(gy0 + ti.j) * fr.W + gx0 + ti.i);
+        cp_async_wait_all();
+        tm.sync();
+      }
+      auto sample = [&](float su, float sv) {
+        return staged ? cubic_tile(gt, gtw, gth, gx0, gy0, fr.W, fr.H, iu, su, iv, sv)
+                      : cubic32(fr.g, fr.W, fr.H, iu, su, iv, sv);
+      };
       int p = tm.tl;
-      // two pixels per trip so that both pixels' 16 taps are in flight together
+      // two pixels per trip so that both pixels' taps are in flight together
       for (; p + tm.TT < npx; p += 2 * tm.TT) {
         const int ia = it.i, ja = it.j;
         it.next();
@@ -777,14 +913,14 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         it.next();
         const float dxa = dx0 + (float)ia, dya = dy0 + (float)ja;
         const float dxb = dx0 + (float)ib, dyb = dy0 + (float)jb;
-        const float ta = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dxa + p2 * dya, iv, fv0 + p1 * dxa + p3 * dya);
-        const float tb2 = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dxb + p2 * dyb, iv, fv0 + p1 * dxb + p3 * dyb);
+        const float ta = sample(fu + p0 * dxa + p2 * dya, fv0 + p1 * dxa + p3 * dya);
+        const float tb2 = sample(fu + p0 * dxb + p2 * dyb, fv0 + p1 * dxb + p3 * dyb);
         one(p, ia, ja, ta);
         one(p + tm.TT, ib, jb, tb2);
       }
       if (p < npx) {
         const float dx = dx0 + (float)it.i, dy = dy0 + (float)it.j;
-        const float t = cubic32(fr.g, fr.W, fr.H, iu, fu + p0 * dx + p2 * dy, iv, fv0 + p1 * dx + p3 * dy);
+        const float t = sample(fu + p0 * dx + p2 * dy, fv0 + p1 * dx + p3 * dy);
         one(p, it.i, it.j, t);
       }
       red[0] = (float)zg; red[1] = (float)nang;
@@ -800,38 +936,91 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
       bwselect_team(tm, tmp, bwg, mx, my, sr, sc, TWO ? 4 : 8, iscr);
       int anyzero = 0;
       for (int p = tm.tl; p < npx; p += tm.TT) anyzero |= !bwg[p];
-      if (!tm.any(anyzero, iscr)) bwselect_team(tm, mtile, bwg, mx, my, sr, sc, 8, iscr);
+      if (!tm.any(anyzero, iscr)) {
+        // the 8-connected selection of the mask tile does not change between
+        // iterations: filled once per subset, then copied
+        if (!have_m8) {
+          bwselect_team(tm, mtile, bwm8, mx, my, sr, sc, 8, iscr);
+          have_m8 = true;
+        }
+        for (int p = tm.tl; p < npx; p += tm.TT) bwg[p] = bwm8[p];
+        tm.sync();
+      }
       if constexpr (TWO) {
         bw = bwg;
         f_side();
         ibf = 1.f / bottomf;
       }
-      // the g tile restricted to its selection, and its sums again
-      int cnt = 0;
-      Kahan sg, qg, kg[NQ];
-      float ng = 0.f;
-      PixIter it(pstart, mx);
-      for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
-        const float t = tg[p] * (float)bwg[p];
-        tg[p] = t;
-        cnt += bwg[p];
-        if (fabsf(t) > 1e-10f) {
-          const float d = t - shift;
-          sg.add(d);
-          qg.add(d * d);
-          ng += 1.f;
+      if constexpr (!TWO) {
+        // The g tile restricted to its selection.  J depends only on the fixed
+        // f selection here, so the sums of the first pass stay valid for the
+        // kept pixels: only the removed pixels' parts are summed and taken off.
+        int cnt = 0, rem = 0;
+        Kahan rsg, rqg, rkg[NQ];
+        float rng = 0.f;
+        PixIter it(pstart, mx);
+        for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+          const int keep = bwg[p];
+          cnt += keep;
+          if (!keep) {
+            const float t = tg[p];
+            if (t != 0.f) {
+              rem = 1;
+              tg[p] = 0.f;
+              if (fabsf(t) > 1e-10f) {
+                const float d = t - shift;
+                rsg.add(d);
+                rqg.add(d * d);
+                rng += 1.f;
+              }
+              float J[NQ];
+              jac(it.i, it.j, bw ? (float)bw[p] : 1.f, J);
+#pragma unroll
+              for (int k = 0; k < NQ; ++k) rkg[k].add(J[k] * t);
+            }
+          }
         }
-        float J[NQ];
-        jac(it.i, it.j, bw ? (float)bw[p] : 1.f, J);
+        cg = tm.sum_int(cnt, iscr);
+        if (tm.any(rem, iscr)) {
+          float rr[NR];
+          rr[0] = 0.f; rr[1] = 0.f;
+          rr[2] = rsg.s; rr[3] = -rsg.c; rr[4] = rqg.s; rr[5] = -rqg.c; rr[6] = rng;
 #pragma unroll
-        for (int k = 0; k < NQ; ++k) kg[k].add(J[k] * t);
+          for (int k = 0; k < NQ; ++k) { rr[7 + 2 * k] = rkg[k].s; rr[8 + 2 * k] = -rkg[k].c; }
+          tm.template sumf<NR>(rr, fscr);
+#pragma unroll
+          for (int k = 2; k < NR; ++k) red[k] -= rr[k];
+        }
+        red[0] = (float)cg;
+      } else {
+        // the g tile restricted to its selection, and its sums again (the f
+        // selection, and with it J, follows the g selection in this form)
+        int cnt = 0;
+        Kahan sg, qg, kg[NQ];
+        float ng = 0.f;
+        PixIter it(pstart, mx);
+        for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+          const float t = tg[p] * (float)bwg[p];
+          tg[p] = t;
+          cnt += bwg[p];
+          if (fabsf(t) > 1e-10f) {
+            const float d = t - shift;
+            sg.add(d);
+            qg.add(d * d);
+            ng += 1.f;
+          }
+          float J[NQ];
+          jac(it.i, it.j, bw ? (float)bw[p] : 1.f, J);
+#pragma unroll
+          for (int k = 0; k < NQ; ++k) kg[k].add(J[k] * t);
+        }
+        red[0] = (float)cnt; red[1] = 0.f;
+        red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) { red[7 + 2 * k] = kg[k].s; red[8 + 2 * k] = -kg[k].c; }
+        tm.template sumf<NR>(red, fscr);
+        cg = (int)red[0];
       }
-      red[0] = (float)cnt; red[1] = 0.f;
-      red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
-#pragma unroll
-      for (int k = 0; k < NQ; ++k) { red[7 + 2 * k] = kg[k].s; red[8 + 2 * k] = -kg[k].c; }
-      tm.template sumf<NR>(red, fscr);
-      cg = (int)red[0];
     }
     // g statistics from the shifted one-pass sums: mean and
     // sqrt((n-1) var) = sqrt(max(s2 - s1^2/n, 0)) (NaN for n = 0, 0 for n = 1)
@@ -856,7 +1045,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
       const float jg = red[7 + 2 * k] + red[8 + 2 * k];
       b2[k] = jf[k] * ibf - (jg - meang * j1[k]) * ibg;
     }
-    // convergence test (FP32) and the FP64 update, identical on every warp
+    // convergence test (FP32) and the update, identical on every lane
     int done = 0;
     float nb = 0.f;
     float D[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -934,9 +1123,10 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
 // Frames are interleaved so that every frame's largest subsets start first.
 template <int TW, bool TWO, int STAGE>
 STDIC_DEV void team_loop(const BatchedArgs& B, const Team<TW>& tm, int* head, int lo, int hi,
-                         unsigned char* base, int smpx, unsigned char* gbase) {
-  const size_t tiles_b = ((size_t)smpx * (TWO ? 8 : 4) + 4 * (size_t)smpx + 15) / 16 * 16;
-  TeamCtl* ctl = (TeamCtl*)(base + tiles_b);
+                         unsigned char* base, int smpx, int gcap, unsigned char* gbase) {
+  const size_t tiles_b = tiles_bytes(smpx, TWO);
+  float* gt = (float*)(base + tiles_b);
+  TeamCtl* ctl = (TeamCtl*)(base + tiles_b + gtile_bytes(gcap));
   float* fscr = (float*)(ctl + 1);
   int* iscr = (int*)(fscr + 32 * TW);
   const int nf = B.frames > 0 ? B.frames : 1;
@@ -949,7 +1139,7 @@ STDIC_DEV void team_loop(const BatchedArgs& B, const Team<TW>& tm, int* head, in
     const int item = ctl->item;
     tm.sync();
     if (item < 0) break;
-    run_subset<TW, TWO, STAGE>(B, tm, item, base, ctl, fscr, iscr, gbase, smpx);
+    run_subset<TW, TWO, STAGE>(B, tm, item, base, ctl, fscr, iscr, gbase, smpx, gt, gcap);
   }
 }
 
@@ -962,34 +1152,32 @@ STDIC_DEV void team_loop(const BatchedArgs& B, const Team<TW>& tm, int* head, in
 // first and get the widest teams, and no warp idles while small work is left.
 //
 // Shared memory per team: smem_px floats (tempg) [+ smem_px floats (tempf,
-// 2-DOF)] + 4 smem_px bytes of bitmaps, then the control block and reduction
-// scratch.  Global scratch: one slice of the same layout for npx_max pixels
+// 2-DOF)] + 5 smem_px bytes of bitmaps, the staged g footprint, then the
+// control block and reduction scratch.  Global scratch: one slice of the same layout for npx_max pixels
 // per warp (a team uses the slice of its first warp).
 //
 // Stages (B.stage): 0 runs the 2-DOF form fused; for the 6-DOF form stage 1
 // does the per-subset set-up (window, masks, f statistics, FP32 Hessian) and
 // stage 2 the iterations with the inverse Hessian the factor kernel produced
-// in FP64 between them.  Every warp of a team holds the team totals after each
-// reduction and runs the same FP64 update on them, so all warps carry
-// bit-identical P without a shared-memory broadcast.
+// in FP64 between them.  Every lane of a team holds the team totals after each
+// reduction and runs the same update on them, so all warps carry bit-identical
+// P without a shared-memory broadcast.
 template <int TW, bool TWO, int STAGE>
 __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
   extern __shared__ __align__(16) unsigned char dsm[];
   const int nf = B.frames > 0 ? B.frames : 1;
   const int Ntot = B.a.N * nf;
   const int warp = threadIdx.x >> 5;
-  const size_t gstride = (size_t)B.a.npx_max * (TWO ? 8 : 4) + 4 * (size_t)B.a.npx_max;
+  const size_t gstride = slice_bytes(B.a.npx_max, TWO);
   const long long gwarp0 = (long long)blockIdx.x * (blockDim.x >> 5);
-  // team slot bytes (the layout of batched_team_bytes)
-  const size_t tb = ((size_t)B.smem_px * (TWO ? 8 : 4) + 4 * (size_t)B.smem_px + 15) / 16 * 16 +
-                    sizeof(TeamCtl) + sizeof(float) * 32 * TW + 16 * TW + 64;
+  const size_t tb = team_bytes(B.smem_px, TWO, TW, B.gtile);
   Team<TW> tm;
   tm.id = threadIdx.x / Team<TW>::TT;
   tm.tl = threadIdx.x % Team<TW>::TT;
   unsigned char* tbase = dsm + tb * tm.id;
   const bool split = TW > 1 && B.split;
   const int split_q = split ? min(*B.n_big * nf, Ntot) : Ntot;
-  team_loop<TW, TWO, STAGE>(B, tm, B.queue_head, 0, split_q, tbase, B.smem_px,
+  team_loop<TW, TWO, STAGE>(B, tm, B.queue_head, 0, split_q, tbase, B.smem_px, B.gtile,
                             B.scratch + gstride * (gwarp0 + (long long)tm.id * TW));
   if constexpr (TW > 1) {
     if (split) {
@@ -998,7 +1186,7 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
       t1.tl = threadIdx.x & 31;
       const size_t sub = (tb / TW) & ~(size_t)15;
       team_loop<1, TWO, STAGE>(B, t1, B.queue_head + 1, split_q, Ntot,
-                               tbase + sub * (warp % TW), B.smem_px_small,
+                               tbase + sub * (warp % TW), B.smem_px_small, B.gtile_small,
                                B.scratch + gstride * (gwarp0 + warp));
     }
   }
@@ -1072,10 +1260,46 @@ cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hin
   return cudaGetLastError();
 }
 
+// Work queue of the iteration stage from the set-up results: subsets still to
+// iterate that are masked (their selections are refilled every iteration) or
+// at least big_ws pixels a side go first, largest first, to the wide teams;
+// the rest follow smallest first; subsets the set-up already decided go last.
+// n_big receives the number of the first group.
+__global__ void __launch_bounds__(1024) build_queue6_kernel(const SubsetState6* __restrict__ st, int N,
+                                                            int big_ws, int32_t* order, int* n_big) {
+  __shared__ int hist[512];
+  __shared__ int start[512];
+  for (int b = threadIdx.x; b < 512; b += blockDim.x) hist[b] = 0;
+  __syncthreads();
+  auto key = [&](int k) {
+    const SubsetState6 s = st[k];
+    if (s.code != 0) return 511;
+    const int w = min(max(s.ws, 0), 255);
+    const bool big = s.cntf > 0 || s.masked != 0 || w >= big_ws;
+    return big ? 255 - w : 256 + min(w, 254);
+  };
+  for (int k = threadIdx.x; k < N; k += blockDim.x) atomicAdd(&hist[key(k)], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int b = 0; b < 512; ++b) { start[b] = acc; acc += hist[b]; }
+    *n_big = start[256];
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < N; k += blockDim.x) order[atomicAdd(&start[key(k)], 1)] = k;
+}
+
+cudaError_t launch_build_queue6(const SubsetState6* st, int N, int big_ws, int32_t* order, int* n_big,
+                                cudaStream_t s) {
+  if (N <= 0) return cudaSuccess;
+  build_queue6_kernel<<<1, 1024, 0, s>>>(st, N, big_ws, order, n_big);
+  return cudaGetLastError();
+}
+
 template <int TW, bool TWO, int STAGE>
 static cudaError_t launch_tw(const BatchedArgs& b, int blocks, int threads, cudaStream_t s) {
   const int teams = threads / (TW * 32);
-  const size_t smem = batched_team_bytes(b.smem_px, TWO, TW) * teams;
+  const size_t smem = batched_team_bytes(b.smem_px, TWO, TW, b.gtile) * teams;
   if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
   cudaError_t e = cudaFuncSetAttribute(icgn_batched_kernel<TW, TWO, STAGE>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1103,9 +1327,9 @@ cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, c
 
 // Resident blocks per SM of one configuration (for grid sizing and the
 // autotuner); the iteration stage (or the fused 2-DOF form) is the reference.
-int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px) {
+int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px, int gtile) {
   const int teams = threads / (tw * 32);
-  const size_t smem = batched_team_bytes(smem_px, two, tw) * teams;
+  const size_t smem = batched_team_bytes(smem_px, two, tw, gtile) * teams;
   if (smem > 227 * 1024) return 0;
   int nb = 0;
   cudaError_t e = cudaSuccess;

@@ -56,6 +56,8 @@ struct BatchedArgs {
   const int* n_big;       // split: number of queue entries of the team phase (device)
   int split;              // 1: large subsets on teams of warps_per_subset, the rest on single warps
   int smem_px_small;      // split: tile pixels of a single warp's share of the team slot
+  int gtile;              // floats of the staged g footprint per team (0: gather from global)
+  int gtile_small;        // split: the same for a single warp's share
   int warps_per_subset;
   int two_dof;
   int frames;             // number of frame pairs stacked in g32 (multi-frame)
@@ -84,11 +86,14 @@ struct SubsetState6 {
 
 cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hinv6, int n,
                            cudaStream_t s);
+// Queue of the 6-DOF iteration stage from the set-up results (split form).
+cudaError_t launch_build_queue6(const SubsetState6* st, int N, int big_ws, int32_t* order, int* n_big,
+                                cudaStream_t s);
 
 // Size of one team's shared slot / global slice of the batched kernel.
-size_t batched_team_bytes(int sm_px, bool two, int tw);
+size_t batched_team_bytes(int sm_px, bool two, int tw, int gtile);
 size_t batched_scratch_bytes(int npx_max, bool two, long long warps);
-int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px);
+int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px, int gtile);
 
 cudaError_t launch_interp(const void* F, long long M, long long N, long long P, const void* X,
                           const void* Y, long long n, void* out, int dtype, cudaStream_t s);
@@ -111,7 +116,7 @@ cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int 
                                int32_t* order, int* n_big, cudaStream_t s, int ascending = 0,
                                int big_ws = 0);
 // Largest tile of a single warp's share of a split team slot.
-int batched_small_px(int sm_px, bool two, int tw);
+int batched_small_px(int sm_px, bool two, int tw, int gtile);
 cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, cudaStream_t s);
 
 // Subpb2 (FEM).  All pointers are device pointers.

@@ -13,7 +13,7 @@
  *   stdic_subpb1           func_quadtree/Subpb1Quadtree.m:1-191
  *   stdic_subpb2           func_quadtree/Subpb2Quadtree.m:1-413
  *   stdic_icgn_adjoint     no counterpart in the reference (gradient of the
- *                          summed ZNSSD cost of the IC-GN subsets)
+ *                          ZNSSD cost of the IC-GN subsets)
  *
  * Conventions (MATLAB's):
  *   - arrays are column-major, first index contiguous; an image is W x H with
@@ -181,6 +181,30 @@ int stdic_subpb2(stdic_ctx* ctx, const double* coords, int N, const int32_t* ele
                  int gauss_order, double beta, double mu, const double* U, const double* F,
                  double alpha, double winstepsize, double tol, int maxit, double* Uhat,
                  int* iters);
+
+/* modes of stdic_icgn_adjoint */
+enum {
+  STDIC_ADJ_RECOMPUTE = 0, /* interpolate each subset again in the backward pass */
+  STDIC_ADJ_STORE = 1      /* keep it in shared memory between the two passes */
+};
+
+/* No reference counterpart: the gradient of the subset ZNSSD cost, the
+ * criterion funICGNQuadtree.m minimises.  For node n, with P = [F11 F21 F12
+ * F22 u v] taken from F (4N) and U (2N) and the (ws+1)^2 window around
+ * round(coords_n) (pixels with mask 0 or outside the image left out):
+ *   C_n = sum_i (a_i - b_i)^2,  a = (f - fbar)/|f - fbar|,  b = (t - tbar)/|t - tbar|,
+ *   t = bicubic of ImgDef (as ba_interp2) at the warp of funICGNQuadtree.m:151-152.
+ * Outputs (each may be NULL): cost = sum of the finite C_n; cost_n (N; NaN
+ * for a window with fewer than 2 pixels or a constant f or t); dU (2N) and dF
+ * (4N), the gradients of C_n with respect to the node's U and F; dg (W x H),
+ * the gradient of the total cost with respect to ImgDef.  fr->dfdx/dfdy are
+ * not used and mask may be NULL.  precision STDIC_PLAIN_F64 computes in FP64
+ * (double frame, double dg); STDIC_BATCHED_F32 in FP32 (dg is float).  mode is
+ * STDIC_ADJ_RECOMPUTE or STDIC_ADJ_STORE. */
+int stdic_icgn_adjoint(stdic_ctx* ctx, const stdic_frame* fr, const double* coords, int N,
+                       int winsize, const int32_t* ws_list, const double* U, const double* F,
+                       double* cost, double* cost_n, double* dU, double* dF, void* dg, int mode,
+                       int precision);
 
 /* No reference counterpart.  stdic_subpb2 without a context and without any
  * device allocation, for callers that cannot allocate when the global step

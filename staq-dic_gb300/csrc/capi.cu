@@ -732,6 +732,91 @@ static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, 
   return filter ? deliver_int(c, c->scal + 1, badnum) : STDIC_OK;
 }
 
+int stdic_icgn_adjoint(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N, int winsize,
+                       const int32_t* ws_list, const double* U, const double* F, double* cost,
+                       double* cost_n, double* dU, double* dF, void* dg, int mode, int precision) {
+  if (!c) return STDIC_E_ARG;
+  if (!fr || !fr->f || !fr->g || fr->W < 4 || fr->H < 4 || (fr->dtype != STDIC_F64 && fr->dtype != STDIC_F32))
+    return fail(c, STDIC_E_ARG, "adjoint: bad frame (f, g and W, H >= 4 are needed)");
+  if (N < 0 || (N > 0 && (!coords || !U || !F)) || (mode != STDIC_ADJ_RECOMPUTE && mode != STDIC_ADJ_STORE))
+    return fail(c, STDIC_E_ARG, "adjoint: bad arguments");
+  if (precision != STDIC_PLAIN_F64 && precision != STDIC_BATCHED_F32)
+    return fail(c, STDIC_E_ARG, "unknown precision");
+  if (precision == STDIC_PLAIN_F64 && fr->dtype != STDIC_F64)
+    return fail(c, STDIC_E_ARG, "adjoint: FP64 precision needs double images");
+  if (!ws_list && (winsize < 0 || (winsize & 1)))
+    return fail(c, STDIC_E_ARG, "adjoint: winsize must be even and >= 0");
+  cudaSetDevice(c->device);
+  const bool f64 = precision == STDIC_PLAIN_F64;
+  // largest subset size (read on the host; the list is small)
+  int ws_max = winsize;
+  if (ws_list && N > 0) {
+    std::vector<int32_t> wl((size_t)N);
+    if (is_device_ptr(ws_list)) {
+      cudaError_t e = cudaMemcpyAsync(wl.data(), ws_list, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "adjoint: subset sizes");
+    } else {
+      std::memcpy(wl.data(), ws_list, sizeof(int32_t) * N);
+    }
+    ws_max = 0;
+    for (int32_t w : wl) {
+      if (w < 0 || (w & 1) || w > 1024) return fail(c, STDIC_E_ARG, "adjoint: subset sizes must be even, 0..1024");
+      ws_max = std::max(ws_max, (int)w);
+    }
+  }
+  if (ws_max > 1024) return fail(c, STDIC_E_ARG, "adjoint: subset size above 1024");
+  const size_t np = (size_t)fr->W * fr->H;
+  const size_t es_in = fr->dtype == STDIC_F64 ? 8 : 4, es = f64 ? 8 : 4;
+  Plan pl;
+  stdic::AdjointArgs a{};
+  const unsigned char *fin = nullptr, *gin = nullptr;
+  pl.in((const unsigned char*)fr->f, es_in * np, (unsigned char**)&fin);
+  pl.in((const unsigned char*)fr->g, es_in * np, (unsigned char**)&gin);
+  pl.in(fr->mask, fr->mask ? np : 0, (uint8_t**)&a.mask);
+  pl.in(coords, 2 * (size_t)N, (double**)&a.coords);
+  pl.in(U, 2 * (size_t)N, (double**)&a.U);
+  pl.in(F, 4 * (size_t)N, (double**)&a.F);
+  pl.in(ws_list, (size_t)N, (int32_t**)&a.ws_list);
+  pl.out_opt(cost_n, (size_t)std::max(N, 1), &a.cost_n);
+  pl.out(cost, 1, &a.cost);
+  pl.out(dU, 2 * (size_t)N, &a.dU);
+  pl.out(dF, 4 * (size_t)N, &a.dF);
+  unsigned char* dgp = nullptr;
+  pl.out((unsigned char*)dg, dg ? es * np : 0, &dgp);
+  float *f32 = nullptr, *g32 = nullptr;
+  const bool convert = !f64 && fr->dtype == STDIC_F64;
+  if (convert) {
+    pl.scratch(np, &f32);
+    pl.scratch(np, &g32);
+  }
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  if (convert) {
+    rc = check_launch(c, stdic::launch_to_f32((const double*)fin, f32, (long long)np, c->stream), "to_f32");
+    if (!rc) rc = check_launch(c, stdic::launch_to_f32((const double*)gin, g32, (long long)np, c->stream), "to_f32");
+    if (rc) return rc;
+    a.f = f32; a.g = g32;
+  } else {
+    a.f = fin; a.g = gin;
+  }
+  a.W = fr->W; a.H = fr->H; a.N = N;
+  a.ws_all = winsize; a.ws_max = ws_max;
+  a.dg = dgp;
+  a.head = c->scal + 7;
+  a.f64 = f64 ? 1 : 0;
+  a.store = mode == STDIC_ADJ_STORE ? 1 : 0;
+  a.nsm = c->nsm;
+  long long nl = 0;
+  cudaEventRecord(c->es0, c->stream);
+  cudaError_t e = stdic::launch_adjoint(a, c->stream, &nl);
+  cudaEventRecord(c->es1, c->stream);
+  c->launches += nl;
+  if (e != cudaSuccess) return cuda_fail(c, e, "adjoint");
+  c->solver_timed = true;
+  return pl.finish(c);
+}
+
 int stdic_subpb2(stdic_ctx* c, const double* coords, int N, const int32_t* elems, int E,
                  const int32_t* dirichlet, int nd, const double* neumann, int nn, int gauss_order,
                  double beta, double mu, const double* U, const double* F, double alpha, double winstepsize,

@@ -119,6 +119,31 @@ cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int 
 int batched_small_px(int sm_px, bool two, int tw, int gtile);
 cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, cudaStream_t s);
 
+// Adjoint of the subset ZNSSD cost (device pointers; f, g in FP64 when f64,
+// else FP32; dg of the same type; mask, dU, dF, dg, cost may be null).
+struct AdjointArgs {
+  const void* f;
+  const void* g;
+  const uint8_t* mask;
+  int W, H, N;
+  const double* coords;
+  const double* U;
+  const double* F;
+  int ws_all;
+  const int32_t* ws_list;
+  int ws_max;
+  double* cost_n;  // N
+  double* cost;    // 1: sum of the finite subset costs
+  double* dU;
+  double* dF;
+  void* dg;
+  int* head;       // work counter (scratch)
+  int f64;
+  int store;       // 1: keep interpolated subsets in shared memory between the passes
+  int nsm;
+};
+cudaError_t launch_adjoint(const AdjointArgs& a, cudaStream_t s, long long* launches);
+
 // Subpb2 (FEM).  All pointers are device pointers.
 struct Subpb2Args {
   const double* coords;

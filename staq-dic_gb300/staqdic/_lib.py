@@ -23,6 +23,8 @@ STDIC_E_TIMEOUT = -5
 STDIC_E_NOTCONV = -6
 STDIC_F64 = 0
 STDIC_F32 = 1
+STDIC_ADJ_RECOMPUTE = 0
+STDIC_ADJ_STORE = 1
 STDIC_PLAIN_F64 = 0
 STDIC_BATCHED_F32 = 1
 
@@ -31,6 +33,7 @@ EXPORTS = [
     "stdic_kernel_launches", "stdic_last_solver_ms", "stdic_interp_bicubic", "stdic_img_gradient",
     "stdic_integer_search_grid", "stdic_integer_search", "stdic_icgn_subsets", "stdic_icgn_local",
     "stdic_subpb1_subsets", "stdic_subpb1", "stdic_subpb2", "stdic_subpb2_noalloc",
+    "stdic_icgn_adjoint",
 ]
 
 
@@ -90,6 +93,8 @@ def load(build_if_missing=True):
     L.stdic_subpb2.argtypes = [_vp, _vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int,
                                _c.c_int, _c.c_double, _c.c_double, _vp, _vp, _c.c_double,
                                _c.c_double, _c.c_double, _c.c_int, _vp, _vp]
+    L.stdic_icgn_adjoint.argtypes = [_vp, _c.POINTER(Frame), _vp, _c.c_int, _c.c_int, _vp, _vp, _vp,
+                                     _vp, _vp, _vp, _vp, _vp, _c.c_int, _c.c_int]
     L.stdic_subpb2_noalloc.argtypes = [_vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int,
                                        _c.c_int, _c.c_double, _c.c_double, _vp, _vp, _c.c_double,
                                        _c.c_double, _c.c_double, _c.c_int, _vp, _vp, _vp, _c.c_char_p,

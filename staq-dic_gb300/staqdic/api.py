@@ -347,3 +347,44 @@ def Subpb2Quadtree(DICmesh, GaussPtOrder, beta, mu, U, F, udual, vdual, alpha, w
     if return_iters:
         return Uhat, int(iters.value)
     return Uhat
+
+
+ADJ_MODES = {"recompute": _lib.STDIC_ADJ_RECOMPUTE, "store": _lib.STDIC_ADJ_STORE}
+
+
+def icgn_adjoint(U, F, coordinatesFEM, ImgRef, ImgDef, winsize, ImgRefMask=None, ws_list=None,
+                 precision="plain", mode="recompute", want_dg=True, size=None, ctx=None):
+    """ZNSSD subset costs and their gradients (stdic_icgn_adjoint; no reference
+    counterpart): returns (cost, cost_n, dU, dF, dg).  cost is the sum of the
+    finite subset costs, dg the gradient of cost with respect to ImgDef (None
+    unless want_dg).  size = (W, H) is needed for torch image buffers."""
+    c = _ctx(ctx)
+    prec = PRECISIONS[precision]
+    dtype = _data_dtype(prec, ImgRef)
+    N = _nodes(coordinatesFEM)
+    W, H = size if size is not None else _shape2(ImgRef)
+    b = _Bufs()
+    fr = Frame()
+    fr.f = b.ptr(ImgRef, dtype)
+    fr.g = b.ptr(ImgDef, dtype)
+    fr.mask = b.ptr(ImgRefMask, np.uint8)
+    fr.dfdx = None
+    fr.dfdy = None
+    fr.W, fr.H = int(W), int(H)
+    fr.dtype = _lib.STDIC_F32 if dtype == np.float32 else _lib.STDIC_F64
+    like = U if _is_torch(U) else None
+    cost, pcost = b.out(like, (1,), np.float64)
+    cost_n, pcn = b.out(like, (N,), np.float64)
+    dU, pdU = b.out(like, (2 * N,), np.float64)
+    dF, pdF = b.out(like, (4 * N,), np.float64)
+    dg, pdg = (None, None)
+    if want_dg:
+        gdt = np.float64 if prec == _lib.STDIC_PLAIN_F64 else np.float32
+        dg, pdg = b.out(like, (int(W), int(H)), gdt)
+    ws0 = int(winsize) if ws_list is None else int(max(int(winsize), int(np.max(ws_list))))
+    c.check(c.L.stdic_icgn_adjoint(c.h, _lib._c.byref(fr), b.ptr(coordinatesFEM, np.float64), N, ws0,
+                                   b.ptr(ws_list, np.int32) if ws_list is not None else None,
+                                   b.ptr(U, np.float64), b.ptr(F, np.float64), pcost, pcn, pdU, pdF, pdg,
+                                   ADJ_MODES[mode] if isinstance(mode, str) else int(mode), prec),
+            "icgn_adjoint")
+    return (cost[0] if not _is_torch(cost) else cost), cost_n, dU, dF, dg

@@ -137,3 +137,43 @@ def test_bad_point_rules(oracle):
     assert set(bad.tolist()) >= {3, 4, 5, 6, 8}
     bad2, badnum2 = oracle.bad_points_subpb1(conv)
     assert badnum2 == 3 and 8 in bad2.tolist()
+
+
+def test_oracle_adjoint_matches_finite_differences(oracle):
+    """The oracle's adjoint (no reference counterpart) is pinned by central
+    differences of its own cost: h = 1e-4 px keeps the O(h^2) error of the
+    piecewise-cubic interpolant well below 1e-4 relative (norm-wise)."""
+    from staqdic import workloads
+    w = workloads.bumps4096(seed=3, size=128)
+    f = w["f"].astype(np.float64)
+    g = w["g"].astype(np.float64)
+    c = w["coordinatesFEM"]
+    N = c.shape[0]
+    rng = np.random.default_rng(1)
+    U = w["Utrue"] + rng.normal(0, 0.3, 2 * N)
+    F = rng.normal(0, 0.01, 4 * N)
+    cost, dU, dF, dg = oracle.icgn_adjoint(f, g, None, c, 32, U, F)
+    h = 1e-4
+    G = np.zeros((N, 6))
+    for k in range(6):
+        if k < 4:
+            Fp, Fm = F.copy(), F.copy()
+            Fp[k::4] += h
+            Fm[k::4] -= h
+            G[:, k] = (oracle.icgn_adjoint(f, g, None, c, 32, U, Fp, False)[0] -
+                       oracle.icgn_adjoint(f, g, None, c, 32, U, Fm, False)[0]) / (2 * h)
+        else:
+            Up, Um = U.copy(), U.copy()
+            Up[k - 4::2] += h
+            Um[k - 4::2] -= h
+            G[:, k] = (oracle.icgn_adjoint(f, g, None, c, 32, Up, F, False)[0] -
+                       oracle.icgn_adjoint(f, g, None, c, 32, Um, F, False)[0]) / (2 * h)
+    A = np.concatenate([dF.reshape(-1, 4), dU.reshape(-1, 2)], 1)
+    assert np.linalg.norm(G - A) / np.linalg.norm(A) < 1e-4
+    for x, y in ((40, 40), (60, 90), (100, 30)):
+        gp, gm = g.copy(), g.copy()
+        gp[x, y] += h
+        gm[x, y] -= h
+        fd = (np.nansum(oracle.icgn_adjoint(f, gp, None, c, 32, U, F, False)[0]) -
+              np.nansum(oracle.icgn_adjoint(f, gm, None, c, 32, U, F, False)[0])) / (2 * h)
+        assert abs(fd - dg[x, y]) <= 1e-4 * max(abs(fd), 1e-8)

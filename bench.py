@@ -11,6 +11,11 @@ uneven subsets 8..64 px).  Inputs are resident in HBM (`value`); the same call
 with pinned host buffers, copies inside the timed region, gives `e2e`.  The L2
 is flushed (256 MiB write) between timed steps.
 
+Beside the headline the line carries, on one GPU, the 2048^2 quadtree pass
+(config C3, ``c3``: batched vs plain FP64 vs the host CPU) and the timing of
+the adjoint on the 4096^2 bumps pair (config C4, ``adjoint_c4``); --no-extras
+skips them.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 N > 1 runs one replica per GPU (the path has no data-path collective);
@@ -45,10 +50,10 @@ def log(*a):
 
 
 # ----------------------------------------------------------------------------
-def make_workload(name):
+def make_workload(name, **kw):
     from staqdic import workloads
     t = time.time()
-    w = workloads.WORKLOADS[name]()
+    w = workloads.WORKLOADS[name](**kw)
     log("workload %s: %d nodes, generated in %.1fs" % (name, w["coordinatesFEM"].shape[0], time.time() - t))
     return w
 
@@ -208,6 +213,144 @@ def run_reference(args, world, rank):
 
 
 # ----------------------------------------------------------------------------
+class LocalRun:
+    """Device-resident frame, gradients and outputs of one LocalICGNQuadtree
+    workload, and the call through the C ABI."""
+
+    def __init__(self, ctx, w):
+        import ctypes
+        import torch
+        from staqdic import _lib
+        self.ctx, self.w = ctx, w
+        L = ctx.L
+        W, H = w["f"].shape
+        N = int(w["coordinatesFEM"].shape[0])
+        self.W, self.H, self.N = W, H, N
+        self.ws_list = np.ascontiguousarray(w["winsize_list"], dtype=np.int32)
+
+        def dev(a, dt):
+            return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dt).ravel(order="F"))).cuda()
+
+        f32, g32 = dev(w["f"], np.float32), dev(w["g"], np.float32)
+        mask = dev(w["maskf"], np.uint8)
+        self.coords = dev(w["coordinatesFEM"], np.float64)
+        self.U0 = dev(w["U0"], np.float64)
+        self.wsl = dev(self.ws_list, np.int32)
+        gx32 = torch.empty((W - 6) * (H - 6), dtype=torch.float32, device="cuda")
+        gy32 = torch.empty_like(gx32)
+        ctx.check(L.stdic_img_gradient(ctx.h, f32.data_ptr(), mask.data_ptr(), W, H, gx32.data_ptr(),
+                                       gy32.data_ptr(), _lib.STDIC_F32), "gradient")
+        f64, g64 = f32.double(), g32.double()
+        gx64 = torch.empty((W - 6) * (H - 6), dtype=torch.float64, device="cuda")
+        gy64 = torch.empty_like(gx64)
+        ctx.check(L.stdic_img_gradient(ctx.h, f64.data_ptr(), mask.data_ptr(), W, H, gx64.data_ptr(),
+                                       gy64.data_ptr(), _lib.STDIC_F64), "gradient64")
+        self.keep = (f32, g32, mask, f64, g64, gx64, gy64)
+        self.gx32, self.gy32 = gx32, gy32
+
+        def frame(f, g, gx, gy, dtype):
+            fr = _lib.Frame()
+            fr.f, fr.g, fr.mask, fr.dfdx, fr.dfdy = f.data_ptr(), g.data_ptr(), mask.data_ptr(), gx.data_ptr(), gy.data_ptr()
+            fr.W, fr.H, fr.dtype = W, H, dtype
+            return fr
+
+        self.fr32 = frame(f32, g32, gx32, gy32, _lib.STDIC_F32)
+        self.fr64 = frame(f64, g64, gx64, gy64, _lib.STDIC_F64)
+        self.U = torch.empty(2 * N, dtype=torch.float64, device="cuda")
+        self.F = torch.empty(4 * N, dtype=torch.float64, device="cuda")
+        self.Hp = torch.empty(21 * N, dtype=torch.float64, device="cuda")
+        self.conv = torch.empty(N, dtype=torch.int32, device="cuda")
+        self.mark = torch.empty(N, dtype=torch.uint8, device="cuda")
+        self.badnum = torch.zeros(1, dtype=torch.int32, device="cuda")
+        ws_max = int(self.ws_list.max())
+
+        def solve(fr, prec):
+            ctx.check(L.stdic_icgn_local(ctx.h, ctypes.byref(fr), self.U0.data_ptr(), self.coords.data_ptr(), N,
+                                         ws_max, self.wsl.data_ptr(), TOL, self.U.data_ptr(), self.F.data_ptr(),
+                                         self.Hp.data_ptr(), self.conv.data_ptr(), self.mark.data_ptr(),
+                                         self.badnum.data_ptr(), prec), "icgn_local")
+
+        self.solve = solve
+
+
+def converged_within(Ub, cb, Up):
+    """Converged subsets of a batched result within TOLPX of the plain FP64 one."""
+    dU = np.abs(Ub - Up).reshape(-1, 2).max(axis=1)
+    return (cb >= 1) & (cb <= 100) & ~np.isnan(Ub[0::2]) & ~np.isnan(Up[0::2]) & (dU <= TOLPX)
+
+
+def measure_c3(ctx, torch, flush, steps=5):
+    """The 2048^2 quadtree with hole (config C3): one LocalICGNQuadtree pass,
+    batched FP32 against the plain FP64 drop-in and the host CPU."""
+    from staqdic import _lib
+    w = make_workload("hole2048")
+    run = LocalRun(ctx, w)
+
+    def timed(fr, prec, k):
+        ms = []
+        for i in range(k):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            run.solve(fr, prec)
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.mean(ms))
+
+    run.solve(run.fr64, _lib.STDIC_PLAIN_F64)
+    torch.cuda.synchronize()
+    Up, cp = run.U.cpu().numpy(), run.conv.cpu().numpy()
+    plain_ms = timed(run.fr64, _lib.STDIC_PLAIN_F64, 2)
+    plain_conv = int(((cp >= 1) & (cp <= 100) & ~np.isnan(Up[0::2])).sum())
+    for _ in range(3):
+        run.solve(run.fr32, _lib.STDIC_BATCHED_F32)
+    bat_ms = timed(run.fr32, _lib.STDIC_BATCHED_F32, steps)
+    Ub, cb = run.U.cpu().numpy(), run.conv.cpu().numpy()
+    n_conv = int(converged_within(Ub, cb, Up).sum())
+    out = {"workload": "hole2048: 2048x2048 plate with hole, Kirsch 2%% strain, quadtree, %d nodes" % run.N,
+           "value": n_conv / (bat_ms * 1e-3), "ms_per_step": bat_ms, "unit": UNIT,
+           "plain_fp64": {"value": plain_conv / (plain_ms * 1e-3), "ms_per_step": plain_ms},
+           "codes_equal_frac": float(np.mean(cb == cp))}
+    out["batched_over_plain"] = out["value"] / out["plain_fp64"]["value"]
+    cpu = cpu_baseline(w, "hole2048")
+    if cpu and cpu.get("value"):
+        out["cpu_baseline"] = cpu
+        out["batched_over_cpu"] = out["value"] / cpu["value"]
+    return out
+
+
+def measure_adjoint(ctx, torch, size=4096):
+    """Adjoint of the subset ZNSSD cost on the bumps field (config C4: 4096^2,
+    ws 32, step 16), FP32, both modes, with dg."""
+    import staqdic
+    w = make_workload("bumps4096", size=size)
+    c = w["coordinatesFEM"]
+    N = c.shape[0]
+    rng = np.random.default_rng(0)
+    dev = lambda a, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dt).ravel(order="F"))).cuda()
+    U = dev(w["Utrue"] + rng.normal(0, 0.2, 2 * N), np.float64)
+    F = dev(rng.normal(0, 0.005, 4 * N), np.float64)
+    f, g, ct = dev(w["f"], np.float32), dev(w["g"], np.float32), dev(c, np.float64)
+    W, H = w["f"].shape
+    out = {"workload": "bumps4096: %dx%d speckle, 8 Gaussian displacement bumps, %d subsets of 32 px" % (W, H, N)}
+    for mode in ("recompute", "store"):
+        for _ in range(2):
+            staqdic.icgn_adjoint(U, F, ct, f, g, 32, precision="batched", mode=mode, size=(W, H), ctx=ctx)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            staqdic.icgn_adjoint(U, F, ct, f, g, 32, precision="batched", mode=mode, size=(W, H), ctx=ctx)
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        out[mode] = {"ms": float(np.mean(ms)), "subsets_per_s": N / (np.mean(ms) * 1e-3)}
+    return out
+
+
+# ----------------------------------------------------------------------------
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -216,6 +359,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hole1024")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the 2048^2 (C3) pass and the 4096^2 adjoint (C4) timing")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -243,49 +388,12 @@ def main():
     ctx.set_stream(stream.cuda_stream)
     L = ctx.L
     w = make_workload(args.workload)
-    W, H = w["f"].shape
-    N = int(w["coordinatesFEM"].shape[0])
-    ws_list = np.ascontiguousarray(w["winsize_list"], dtype=np.int32)
-
-    def dev(a, dt):
-        return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dt).ravel(order="F"))).cuda()
-
-    f32, g32 = dev(w["f"], np.float32), dev(w["g"], np.float32)
-    mask = dev(w["maskf"], np.uint8)
-    coords = dev(w["coordinatesFEM"], np.float64)
-    U0 = dev(w["U0"], np.float64)
-    wsl = dev(ws_list, np.int32)
-    gx32 = torch.empty((W - 6) * (H - 6), dtype=torch.float32, device="cuda")
-    gy32 = torch.empty_like(gx32)
-    ctx.check(L.stdic_img_gradient(ctx.h, f32.data_ptr(), mask.data_ptr(), W, H, gx32.data_ptr(),
-                                   gy32.data_ptr(), _lib.STDIC_F32), "gradient")
-    f64, g64 = f32.double(), g32.double()
-    gx64 = torch.empty((W - 6) * (H - 6), dtype=torch.float64, device="cuda")
-    gy64 = torch.empty_like(gx64)
-    ctx.check(L.stdic_img_gradient(ctx.h, f64.data_ptr(), mask.data_ptr(), W, H, gx64.data_ptr(),
-                                   gy64.data_ptr(), _lib.STDIC_F64), "gradient64")
-
-    def frame(f, g, gx, gy, dtype):
-        fr = _lib.Frame()
-        fr.f, fr.g, fr.mask, fr.dfdx, fr.dfdy = f.data_ptr(), g.data_ptr(), mask.data_ptr(), gx.data_ptr(), gy.data_ptr()
-        fr.W, fr.H, fr.dtype = W, H, dtype
-        return fr
-
-    fr32 = frame(f32, g32, gx32, gy32, _lib.STDIC_F32)
-    fr64 = frame(f64, g64, gx64, gy64, _lib.STDIC_F64)
-    U = torch.empty(2 * N, dtype=torch.float64, device="cuda")
-    F = torch.empty(4 * N, dtype=torch.float64, device="cuda")
-    Hp = torch.empty(21 * N, dtype=torch.float64, device="cuda")
-    conv = torch.empty(N, dtype=torch.int32, device="cuda")
-    mark = torch.empty(N, dtype=torch.uint8, device="cuda")
-    badnum = torch.zeros(1, dtype=torch.int32, device="cuda")
+    run = LocalRun(ctx, w)
+    W, H, N, ws_list = run.W, run.H, run.N, run.ws_list
+    fr32, fr64, solve = run.fr32, run.fr64, run.solve
+    U, F, conv = run.U, run.F, run.conv
+    gx32, gy32 = run.gx32, run.gy32
     import ctypes
-
-    def solve(fr, prec, outs=(U, F, Hp, conv, mark, badnum)):
-        u, f_, h, c, m, b = outs
-        ctx.check(L.stdic_icgn_local(ctx.h, ctypes.byref(fr), U0.data_ptr(), coords.data_ptr(), N, WS_MAX,
-                                     wsl.data_ptr(), TOL, u.data_ptr(), f_.data_ptr(), h.data_ptr(),
-                                     c.data_ptr(), m.data_ptr(), b.data_ptr(), prec), "icgn_local")
 
     # ---- plain FP64 drop-in: accuracy reference and the 'plain' throughput
     solve(fr64, _lib.STDIC_PLAIN_F64)
@@ -460,6 +568,10 @@ def main():
            "wall_s_timed": t_wall}
     if cpu:
         out["cpu_baseline"] = cpu
+        out["batched_over_cpu"] = value / cpu["value"] if cpu.get("value") else None
+    if world == 1 and not args.no_extras:
+        out["c3"] = measure_c3(ctx, torch, flush)
+        out["adjoint_c4"] = measure_adjoint(ctx, torch)
     print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()

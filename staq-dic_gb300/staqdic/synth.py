@@ -17,6 +17,8 @@ Deformation fields used by the workloads:
   * rotation about the centre composed with a straight crack opening.
 """
 import math
+import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -50,18 +52,43 @@ def _render(sp, W, H, X, Y, fwd_x, fwd_y, grow=1.0):
     amp = sp.amp[keep]
     Xf = X.ravel(order="F")
     Yf = Y.ravel(order="F")
-    for dy in range(-R, R + 1):
-        yi = py + dy
-        oky = (yi >= 0) & (yi < H)
-        for dx in range(-R, R + 1):
-            xi = px + dx
-            ok = oky & (xi >= 0) & (xi < W)
-            if not ok.any():
-                continue
-            lin = xi[ok] + yi[ok] * W
-            d2 = (Xf[lin] - cx[ok]) ** 2 + (Yf[lin] - cy[ok]) ** 2
-            img += np.bincount(lin, weights=amp[ok] * np.exp(-d2 * inv2s2[ok]), minlength=W * H)
+    offs = [(dx, dy) for dy in range(-R, R + 1) for dx in range(-R, R + 1)]
+
+    def part(chunk):
+        # one bincount per group of window offsets (the full-image pass of a
+        # bincount dominates), summed into this worker's own image
+        out = np.zeros(W * H)
+        group = 8
+        for g0 in range(0, len(chunk), group):
+            lins, wts = [], []
+            for dx, dy in chunk[g0:g0 + group]:
+                yi = py + dy
+                xi = px + dx
+                ok = (yi >= 0) & (yi < H) & (xi >= 0) & (xi < W)
+                if not ok.any():
+                    continue
+                lin = xi[ok] + yi[ok] * W
+                d2 = (Xf[lin] - cx[ok]) ** 2 + (Yf[lin] - cy[ok]) ** 2
+                lins.append(lin)
+                wts.append(amp[ok] * np.exp(-d2 * inv2s2[ok]))
+            if lins:
+                out += np.bincount(np.concatenate(lins), weights=np.concatenate(wts), minlength=W * H)
+        return out
+
+    # numpy releases the GIL in these loops: split the offsets over host threads
+    nw = max(1, min(_threads(), len(offs) // 16))
+    chunks = [offs[k::nw] for k in range(nw)]
+    if nw == 1:
+        img = part(offs)
+    else:
+        with ThreadPoolExecutor(nw) as ex:
+            for p in ex.map(part, chunks):
+                img += p
     return img.reshape((W, H), order="F")
+
+
+def _threads():
+    return min(16, os.cpu_count() or 1)
 
 
 def pixel_grid(W, H):
@@ -71,13 +98,27 @@ def pixel_grid(W, H):
 
 
 def invert_map(ufun, xs, ys, iters=30):
-    """Solve X + u(X) = x by fixed-point iteration (|grad u| << 1)."""
-    X, Y = xs.copy(), ys.copy()
-    for _ in range(iters):
-        ux, uy = ufun(X, Y)
-        X = xs - ux
-        Y = ys - uy
-    return X, Y
+    """Solve X + u(X) = x by fixed-point iteration (|grad u| << 1), in row
+    blocks over host threads (each pixel iterates independently)."""
+    W = xs.shape[0]
+    nw = max(1, min(_threads(), W // 64))
+    bounds = np.linspace(0, W, nw + 1).astype(int)
+
+    def block(k):
+        a, b = bounds[k], bounds[k + 1]
+        x0, y0 = xs[a:b], ys[a:b]
+        X, Y = x0.copy(), y0.copy()
+        for _ in range(iters):
+            ux, uy = ufun(X, Y)
+            X = x0 - ux
+            Y = y0 - uy
+        return X, Y
+
+    if nw == 1:
+        return block(0)
+    with ThreadPoolExecutor(nw) as ex:
+        parts = list(ex.map(block, range(nw)))
+    return np.concatenate([p[0] for p in parts], 0), np.concatenate([p[1] for p in parts], 0)
 
 
 def render_pair(W, H, sp, ufun, noise=0.01, rng=None, inv=None):

@@ -22,7 +22,8 @@ struct stdic_ctx {
   cudaStream_t stream = nullptr;
   void* ws = nullptr;
   size_t ws_size = 0;
-  int* scal = nullptr;  // device scalars: [1] badnum, [2] iters, [3] status, [4..5] queue heads, [6] queue split
+  int* scal = nullptr;  // device scalars: [1] badnum, [2] iters, [3] status, [4..5] queue heads, [6] queue split,
+                        // [7] adjoint queue head, [8..9] iteration-list counts
   double* scald = nullptr;  // device double scalars: [0] residual
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t es0 = nullptr, es1 = nullptr;  // around the last IC-GN solver kernel
@@ -450,6 +451,16 @@ bool tune_log() {
   return on;
 }
 
+// STDIC_TUNE_PICK=<k> takes launch shape k of batched_candidates without
+// timing the others (for profiling one fixed configuration).
+int tune_pick() {
+  static const int k = [] {
+    const char* e = std::getenv("STDIC_TUNE_PICK");
+    return e && *e ? std::atoi(e) : -1;
+  }();
+  return k;
+}
+
 // Subset sizes the work queue is sorted by (one of ws_list, wsl2, ws_all).
 struct QueueKeys {
   const int32_t* ws_list;
@@ -480,6 +491,12 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
     if (rc) return rc;
     // 2-DOF: one fused pass; 6-DOF: set-up, FP64 factorisation, iterations
     const int stages[2] = {two ? 0 : 1, 2};
+    b.split_ws = cd.split;
+    b.n2 = c->scal + 8;
+    if (!two) {
+      cudaError_t e = cudaMemsetAsync(b.n2, 0, 2 * sizeof(int), c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "list reset");
+    }
     for (int k = 0; k < (two ? 1 : 2); ++k) {
       cudaError_t e = cudaMemsetAsync(b.queue_head, 0, 2 * sizeof(int), c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "queue reset");
@@ -490,14 +507,7 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
         rc = check_launch(c, stdic::launch_factor6((const stdic::SubsetState6*)b.st6, b.H6, b.Hinv6, Ntot, c->stream),
                           "Hessian factorisation");
         if (rc) return rc;
-        if (cd.split && b.frames <= 1) {
-          // masked subsets refill their selections every iteration: they join
-          // the large ones on the wide teams in the iteration stage
-          rc = check_launch(c, stdic::launch_build_queue6((const stdic::SubsetState6*)b.st6, b.a.N, cd.split,
-                                                          (int32_t*)b.order, c->scal + 6, c->stream),
-                            "queue");
-          if (rc) return rc;
-        }
+
       }
     }
     return STDIC_OK;
@@ -507,7 +517,10 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
   auto it = c->tune.find(key);
   if (it == c->tune.end()) {
     int best = 0;
-    if (c->tuning && Ntot > 0 && cands.size() > 1) {
+    const int pick = tune_pick();
+    if (pick >= 0) {
+      best = std::min(pick, (int)cands.size() - 1);
+    } else if (c->tuning && Ntot > 0 && cands.size() > 1) {
       float bt = 1e30f;
       for (auto& cd : cands) {
         cudaEventRecord(c->ev0, c->stream);
@@ -567,6 +580,7 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
   std::vector<BatchedCand> cands;
   stdic::SubsetState6* st6 = nullptr;
   double *H6 = nullptr, *Hinv6 = nullptr;
+  int32_t* order2 = nullptr;
   if (batched) {
     cands = batched_candidates(c, false, npx_max, N);
     pl.scratch((size_t)std::max(N, 1), &order);
@@ -574,6 +588,7 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
     pl.scratch((size_t)std::max(N, 1), &st6);
     pl.scratch(21 * (size_t)std::max(N, 1), &H6);
     pl.scratch(36 * (size_t)std::max(N, 1), &Hinv6);
+    pl.scratch(2 * (size_t)std::max(N, 1), &order2);
   }
   int rc = pl.commit(c);
   if (rc) return rc;
@@ -595,7 +610,7 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
         b.f32 = d.f32; b.g32 = d.g32; b.dfdx32 = d.dfdx32; b.dfdy32 = d.dfdy32;
         b.order = order; b.two_dof = 0; b.frames = 1; b.g_stride = 0;
         b.scratch = bscr;
-        b.st6 = st6; b.H6 = H6; b.Hinv6 = Hinv6;
+        b.st6 = st6; b.H6 = H6; b.Hinv6 = Hinv6; b.order2 = order2;
         rc = run_batched(c, b, N, cands, QueueKeys{a.ws_list, nullptr, winsize});
       }
     }

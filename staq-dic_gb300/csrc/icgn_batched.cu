@@ -363,51 +363,6 @@ struct PixIter {
   }
 };
 
-// Packed lower-triangular Cholesky of a 6x6 SPD matrix in registers.
-struct Chol6 {
-  double l[21];  // row-major packed: l[r*(r+1)/2 + c], c <= r
-  bool ok;
-};
-
-STDIC_DEV void chol6_factor(const double H[21], Chol6& C) {
-  C.ok = true;
-#pragma unroll
-  for (int j = 0; j < 6; ++j) {
-    double d = H[j * (j + 1) / 2 + j];
-#pragma unroll
-    for (int k = 0; k < j; ++k) d -= C.l[j * (j + 1) / 2 + k] * C.l[j * (j + 1) / 2 + k];
-    C.ok = C.ok && (d > 0);
-    const double ljj = sqrt(d > 0 ? d : 1.0);
-    C.l[j * (j + 1) / 2 + j] = ljj;
-    const double inv = 1.0 / ljj;
-#pragma unroll
-    for (int i = j + 1; i < 6; ++i) {
-      double s = H[i * (i + 1) / 2 + j];
-#pragma unroll
-      for (int k = 0; k < j; ++k) s -= C.l[i * (i + 1) / 2 + k] * C.l[j * (j + 1) / 2 + k];
-      C.l[i * (i + 1) / 2 + j] = s * inv;
-    }
-  }
-}
-
-STDIC_DEV void chol6_solve(const Chol6& C, const double b[6], double x[6]) {
-  double y[6];
-#pragma unroll
-  for (int i = 0; i < 6; ++i) {
-    double s = b[i];
-#pragma unroll
-    for (int k = 0; k < i; ++k) s -= C.l[i * (i + 1) / 2 + k] * y[k];
-    y[i] = s / C.l[i * (i + 1) / 2 + i];
-  }
-#pragma unroll
-  for (int i = 5; i >= 0; --i) {
-    double s = y[i];
-#pragma unroll
-    for (int k = i + 1; k < 6; ++k) s -= C.l[k * (k + 1) / 2 + i] * x[k];
-    x[i] = s / C.l[i * (i + 1) / 2 + i];
-  }
-}
-
 struct TeamCtl {
   // inverse Hessian of the team's current subset (6-DOF, row-major), split
   // into FP32 pairs hh + hl that carry its FP64 value to about 2^-48
@@ -770,6 +725,13 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
 #pragma unroll
       for (int k = 0; k < 6; ++k) { s6.Jf[k] = jf[k < NQ ? k : 0]; s6.J1[k] = j1[k < NQ ? k : 0]; }
       st6[item] = s6;
+      if (B.order2 && code == 0 && !nan_out) {
+        // masked subsets refill their selections every iteration: with the
+        // large ones they go to the wide teams of the split form
+        const bool wide = B.split && (cntf > 0 || has_masked || wx >= B.split_ws);
+        const int slot = atomicAdd(&B.n2[wide ? 0 : 1], 1);
+        B.order2[(wide ? 0 : Ntot) + slot] = item;
+      }
       if (code != 0 || nan_out) {
         a.conv[item] = code;
         // decided in the set-up: P is still the initial guess, passed through in FP64
@@ -803,7 +765,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
   while (run && step <= kMaxIter && normNew > tolf && normAbs > tolf) {
     ++step;
     if constexpr (!TWO) {
-      if (step > 1 && (double)cntf > 0.0 * npx0) {
+      if (step > 1 && cntf > 0) {
         // window growth test of funICGNQuadtree.m:140 (FP64, recomputed only
         // when the count of selected g pixels changes)
         int nws = last_nws;
@@ -1123,7 +1085,8 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
 // Frames are interleaved so that every frame's largest subsets start first.
 template <int TW, bool TWO, int STAGE>
 STDIC_DEV void team_loop(const BatchedArgs& B, const Team<TW>& tm, int* head, int lo, int hi,
-                         unsigned char* base, int smpx, int gcap, unsigned char* gbase) {
+                         unsigned char* base, int smpx, int gcap, unsigned char* gbase,
+                         const int32_t* list = nullptr) {
   const size_t tiles_b = tiles_bytes(smpx, TWO);
   float* gt = (float*)(base + tiles_b);
   TeamCtl* ctl = (TeamCtl*)(base + tiles_b + gtile_bytes(gcap));
@@ -1133,7 +1096,8 @@ STDIC_DEV void team_loop(const BatchedArgs& B, const Team<TW>& tm, int* head, in
   for (;;) {
     if (tm.tl == 0) {
       const int q = lo + atomicAdd(head, 1);
-      ctl->item = q < hi ? B.order[q / nf] + (q % nf) * B.a.N : -1;
+      // list: subset ids as they are; otherwise node order with frames interleaved
+      ctl->item = q >= hi ? -1 : (list ? list[q] : B.order[q / nf] + (q % nf) * B.a.N);
     }
     tm.sync();
     const int item = ctl->item;
@@ -1176,9 +1140,31 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
   tm.tl = threadIdx.x % Team<TW>::TT;
   unsigned char* tbase = dsm + tb * tm.id;
   const bool split = TW > 1 && B.split;
+  unsigned char* const gteam = B.scratch + gstride * (gwarp0 + (long long)tm.id * TW);
+  if (STAGE == 2 && B.order2) {
+    // the lists the set-up stage left: wide teams first, then single warps
+    // (without the split every subset is in the second list)
+    const int nwide = B.n2[0], nrest = B.n2[1];
+    if (split)
+      team_loop<TW, TWO, STAGE>(B, tm, B.queue_head, 0, nwide, tbase, B.smem_px, B.gtile, gteam, B.order2);
+    else
+      team_loop<TW, TWO, STAGE>(B, tm, B.queue_head, 0, nrest, tbase, B.smem_px, B.gtile, gteam,
+                                B.order2 + Ntot);
+    if constexpr (TW > 1) {
+      if (split) {
+        Team<1> t1;
+        t1.id = warp;
+        t1.tl = threadIdx.x & 31;
+        const size_t sub = (tb / TW) & ~(size_t)15;
+        team_loop<1, TWO, STAGE>(B, t1, B.queue_head + 1, 0, nrest, tbase + sub * (warp % TW),
+                                 B.smem_px_small, B.gtile_small, B.scratch + gstride * (gwarp0 + warp),
+                                 B.order2 + Ntot);
+      }
+    }
+    return;
+  }
   const int split_q = split ? min(*B.n_big * nf, Ntot) : Ntot;
-  team_loop<TW, TWO, STAGE>(B, tm, B.queue_head, 0, split_q, tbase, B.smem_px, B.gtile,
-                            B.scratch + gstride * (gwarp0 + (long long)tm.id * TW));
+  team_loop<TW, TWO, STAGE>(B, tm, B.queue_head, 0, split_q, tbase, B.smem_px, B.gtile, gteam);
   if constexpr (TW > 1) {
     if (split) {
       Team<1> t1;
@@ -1232,24 +1218,57 @@ __global__ void __launch_bounds__(128) factor6_kernel(const SubsetState6* __rest
                                                       double* __restrict__ Hinv6, int n) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n || st[t].code != 0) return;
-  double H[21];
+  // packed lower Cholesky factor L (row-major), all indices compile-time
+  double l[21];
 #pragma unroll
-  for (int k = 0; k < 21; ++k) H[k] = H6[(size_t)t * 21 + k];
-  Chol6 C;
-  chol6_factor(H, C);
+  for (int k = 0; k < 21; ++k) l[k] = H6[(size_t)t * 21 + k];
+  bool ok = true;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    double d = l[j * (j + 1) / 2 + j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) d -= l[j * (j + 1) / 2 + k] * l[j * (j + 1) / 2 + k];
+    ok = ok && (d > 0);
+    const double ljj = sqrt(d > 0 ? d : 1.0);
+    const double inv = 1.0 / ljj;
+    l[j * (j + 1) / 2 + j] = ljj;
+#pragma unroll
+    for (int i = j + 1; i < 6; ++i) {
+      double s2 = l[i * (i + 1) / 2 + j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) s2 -= l[i * (i + 1) / 2 + k] * l[j * (j + 1) / 2 + k];
+      l[i * (i + 1) / 2 + j] = s2 * inv;
+    }
+  }
   double* out = Hinv6 + (size_t)t * 36;
-  if (!C.ok) {
+  if (!ok) {
     lu_inverse6(H6 + (size_t)t * 21, out);
     return;
   }
+  // M = L^-1 (lower, packed), then H^-1 = M^T M
+  double m[21];
 #pragma unroll
-  for (int col = 0; col < 6; ++col) {
-    double e[6], x[6];
+  for (int i = 0; i < 6; ++i) {
+    const double inv = 1.0 / l[i * (i + 1) / 2 + i];
+    m[i * (i + 1) / 2 + i] = inv;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) e[k] = k == col ? 1.0 : 0.0;
-    chol6_solve(C, e, x);
+    for (int j = 0; j < i; ++j) {
+      double s2 = 0.0;
 #pragma unroll
-    for (int r = 0; r < 6; ++r) out[r * 6 + col] = x[r];
+      for (int k = j; k < i; ++k) s2 += l[i * (i + 1) / 2 + k] * m[k * (k + 1) / 2 + j];
+      m[i * (i + 1) / 2 + j] = -s2 * inv;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 6; ++r) {
+#pragma unroll
+    for (int c2 = r; c2 < 6; ++c2) {
+      double s2 = 0.0;
+#pragma unroll
+      for (int k = c2; k < 6; ++k) s2 += m[k * (k + 1) / 2 + r] * m[k * (k + 1) / 2 + c2];
+      out[r * 6 + c2] = s2;
+      out[c2 * 6 + r] = s2;
+    }
   }
 }
 
@@ -1257,42 +1276,6 @@ cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hin
                            cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   factor6_kernel<<<(n + 127) / 128, 128, 0, s>>>(st, H6, Hinv6, n);
-  return cudaGetLastError();
-}
-
-// Work queue of the iteration stage from the set-up results: subsets still to
-// iterate that are masked (their selections are refilled every iteration) or
-// at least big_ws pixels a side go first, largest first, to the wide teams;
-// the rest follow smallest first; subsets the set-up already decided go last.
-// n_big receives the number of the first group.
-__global__ void __launch_bounds__(1024) build_queue6_kernel(const SubsetState6* __restrict__ st, int N,
-                                                            int big_ws, int32_t* order, int* n_big) {
-  __shared__ int hist[512];
-  __shared__ int start[512];
-  for (int b = threadIdx.x; b < 512; b += blockDim.x) hist[b] = 0;
-  __syncthreads();
-  auto key = [&](int k) {
-    const SubsetState6 s = st[k];
-    if (s.code != 0) return 511;
-    const int w = min(max(s.ws, 0), 255);
-    const bool big = s.cntf > 0 || s.masked != 0 || w >= big_ws;
-    return big ? 255 - w : 256 + min(w, 254);
-  };
-  for (int k = threadIdx.x; k < N; k += blockDim.x) atomicAdd(&hist[key(k)], 1);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int b = 0; b < 512; ++b) { start[b] = acc; acc += hist[b]; }
-    *n_big = start[256];
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k < N; k += blockDim.x) order[atomicAdd(&start[key(k)], 1)] = k;
-}
-
-cudaError_t launch_build_queue6(const SubsetState6* st, int N, int big_ws, int32_t* order, int* n_big,
-                                cudaStream_t s) {
-  if (N <= 0) return cudaSuccess;
-  build_queue6_kernel<<<1, 1024, 0, s>>>(st, N, big_ws, order, n_big);
   return cudaGetLastError();
 }
 

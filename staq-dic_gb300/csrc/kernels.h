@@ -56,6 +56,12 @@ struct BatchedArgs {
   const int* n_big;       // split: number of queue entries of the team phase (device)
   int split;              // 1: large subsets on teams of warps_per_subset, the rest on single warps
   int smem_px_small;      // split: tile pixels of a single warp's share of the team slot
+  // 6-DOF: the set-up stage appends every subset it leaves to the iterations
+  // to one of two lists (order2[0..) for the wide teams, order2[N..) for single
+  // warps; counts in n2[0], n2[1]), which the iteration stage then pulls
+  int32_t* order2;
+  int* n2;
+  int split_ws;           // subsets at least this size (or masked) go to the wide-team list
   int gtile;              // floats of the staged g footprint per team (0: gather from global)
   int gtile_small;        // split: the same for a single warp's share
   int warps_per_subset;
@@ -86,9 +92,7 @@ struct SubsetState6 {
 
 cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hinv6, int n,
                            cudaStream_t s);
-// Queue of the 6-DOF iteration stage from the set-up results (split form).
-cudaError_t launch_build_queue6(const SubsetState6* st, int N, int big_ws, int32_t* order, int* n_big,
-                                cudaStream_t s);
+
 
 // Size of one team's shared slot / global slice of the batched kernel.
 size_t batched_team_bytes(int sm_px, bool two, int tw, int gtile);

@@ -336,32 +336,42 @@ cudaError_t launch_icgn2_plain(const IcgnArgs& a, cudaStream_t s) {
 __global__ void __launch_bounds__(1024) badpoints_kernel(const int32_t* __restrict__ conv, int N,
                                                          double* U, double* F, int two_dof,
                                                          int* badnum) {
-  __shared__ double red[32 * 2];
-  __shared__ int ired[32];
-  double v[2] = {0, 0};
-  int nbad = 0, n102 = 0;
+  // the statistics of the good codes are integer sums, taken exactly in int64
+  __shared__ long long red[5][32];
+  __shared__ double thr_s;
+  long long sc = 0, sc2 = 0, ng = 0, nbad = 0, n102 = 0;
   for (int k = threadIdx.x; k < N; k += blockDim.x) {
-    const int c = conv[k];
+    const long long c = conv[k];
     const bool bad = c < 0 || c > kMaxIter - 1;
-    if (!bad) { v[0] += c; v[1] += 1; }
+    if (!bad) { sc += c; sc2 += c * c; ++ng; }
     nbad += bad;
     n102 += (c == kMaxIter + 2);
   }
-  block_sum<2>(v, red);
-  nbad = block_sum_int(nbad, ired);
-  n102 = block_sum_int(n102, ired);
-  const double ng = v[1];
-  const double mean = v[0] / ng;
-  double q[1] = {0};
-  for (int k = threadIdx.x; k < N; k += blockDim.x) {
-    const int c = conv[k];
-    if (!(c < 0 || c > kMaxIter - 1)) { const double d = c - mean; q[0] += d * d; }
+  long long v[5] = {sc, sc2, ng, nbad, n102};
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    if (lane == 0) red[q][warp] = v[q];
   }
-  block_sum<1>(q, red);
-  const double sd = ng > 1 ? sqrt(q[0] / (ng - 1)) : (ng == 1 ? 0.0 : nan(""));
-  const double cand = two_dof ? mean + 0.25 * sd : mean + 1.0 * sd;
-  const double floorv = two_dof ? 10.0 : 6.0;
-  const double thr = isnan(cand) ? floorv : fmax(cand, floorv);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long t[5] = {0, 0, 0, 0, 0};
+    for (int q = 0; q < 5; ++q)
+      for (int w = 0; w < nw; ++w) t[q] += red[q][w];
+    const double n = (double)t[2];
+    const double mean = (double)t[0] / n;
+    // sum (c - mean)^2 = (n sum c^2 - (sum c)^2) / n, the numerator exact in integers
+    const long long num = t[2] * t[1] - t[0] * t[0];
+    const double sd = t[2] > 1 ? sqrt((double)num / n / (n - 1.0)) : (t[2] == 1 ? 0.0 : nan(""));
+    const double cand = two_dof ? mean + 0.25 * sd : mean + 1.0 * sd;
+    const double floorv = two_dof ? 10.0 : 6.0;
+    thr_s = isnan(cand) ? floorv : fmax(cand, floorv);
+    if (badnum) *badnum = (int)(t[3] - t[4]);
+  }
+  __syncthreads();
+  const double thr = thr_s;
   for (int k = threadIdx.x; k < N; k += blockDim.x) {
     const int c = conv[k];
     if (c < 0 || c > kMaxIter - 1 || (double)c > thr) {
@@ -371,7 +381,6 @@ __global__ void __launch_bounds__(1024) badpoints_kernel(const int32_t* __restri
         for (int a = 0; a < 4; ++a) F[4 * k + a] = nan("");
     }
   }
-  if (threadIdx.x == 0 && badnum) *badnum = nbad - n102;
 }
 
 cudaError_t launch_badpoints(int32_t* conv, int N, double* U, double* F, int two_dof,
@@ -419,7 +428,24 @@ __global__ void __launch_bounds__(1024) build_queue_kernel(const int32_t* __rest
     if (ascending == 2) return b >= bw ? 255 - b : 256 - bw + b;
     return ascending ? b : 255 - b;
   };
-  for (int k = threadIdx.x; k < N; k += blockDim.x) atomicAdd(&hist[key(k)], 1);
+  // warp-aggregated counting sort: one shared atomic per distinct key of a
+  // warp; the keys of eight rounds are loaded together so their loads overlap
+  const int lane = threadIdx.x & 31;
+  const int nit = (N + blockDim.x - 1) / blockDim.x;
+  constexpr int R = 8;
+  for (int it0 = 0; it0 < nit; it0 += R) {
+    int kk[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const int k = (it0 + u) * blockDim.x + threadIdx.x;
+      kk[u] = (it0 + u < nit && k < N) ? key(k) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const unsigned grp = __match_any_sync(0xffffffffu, kk[u]);
+      if (kk[u] >= 0 && lane == __ffs(grp) - 1) atomicAdd(&hist[kk[u]], __popc(grp));
+    }
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     int acc = 0;
@@ -432,9 +458,23 @@ __global__ void __launch_bounds__(1024) build_queue_kernel(const int32_t* __rest
     }
   }
   __syncthreads();
-  for (int k = threadIdx.x; k < N; k += blockDim.x) {
-    const int pos = atomicAdd(&start[key(k)], 1);
-    order[pos] = k;
+  for (int it0 = 0; it0 < nit; it0 += R) {
+    int kk[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const int k = (it0 + u) * blockDim.x + threadIdx.x;
+      kk[u] = (it0 + u < nit && k < N) ? key(k) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const int k = (it0 + u) * blockDim.x + threadIdx.x;
+      const unsigned grp = __match_any_sync(0xffffffffu, kk[u]);
+      const int leader = __ffs(grp) - 1;
+      int base = 0;
+      if (kk[u] >= 0 && lane == leader) base = atomicAdd(&start[kk[u]], __popc(grp));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (kk[u] >= 0) order[base + __popc(grp & ((1u << lane) - 1u))] = k;
+    }
   }
 }
 

@@ -182,6 +182,19 @@ int stdic_subpb2(stdic_ctx* ctx, const double* coords, int N, const int32_t* ele
                  double alpha, double winstepsize, double tol, int maxit, double* Uhat,
                  int* iters);
 
+/* No reference counterpart (the batching of the chosen form across frame
+ * pairs): funICGNQuadtree over N nodes for `frames` deformed frames at once,
+ * all sharing the reference frame of fr (f, its gradients and mask) and one
+ * mesh, in one persistent kernel.  fr->g holds the frames' W x H images one
+ * after another.  U0, U (2N per frame), F (4N per frame) and conv (N per frame)
+ * hold the frames one after another; Hpk (optional) is (N frames) x 21.  Each
+ * frame's results are those of stdic_icgn_subsets on that frame alone, up to
+ * the FP32 summation order of the launch shape.  STDIC_BATCHED_F32 only. */
+int stdic_icgn_subsets_frames(stdic_ctx* ctx, const stdic_frame* fr, int frames, const double* U0,
+                              const double* coords, int N, int winsize, const int32_t* ws_list,
+                              double tol, double* U, double* F, double* Hpk, int32_t* conv,
+                              int precision);
+
 /* modes of stdic_icgn_adjoint */
 enum {
   STDIC_ADJ_RECOMPUTE = 0, /* interpolate each subset again in the backward pass */

@@ -551,8 +551,11 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
 static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0, const double* coords,
                            int N, int winsize, const int32_t* ws_list, double tol, double* U, double* F,
                            double* Hpk, int32_t* conv, uint8_t* mark_hole, int* badnum, int precision,
-                           bool filter) {
+                           bool filter, int frames = 1) {
   if (!c) return STDIC_E_ARG;
+  if (frames < 1 || (frames > 1 && (precision != STDIC_BATCHED_F32 || filter)))
+    return fail(c, STDIC_E_ARG, "several frames: batched precision only, frames >= 1");
+  const size_t NT = (size_t)N * frames;
   if (N < 0 || !frame_ok(fr) || (N > 0 && (!U0 || !coords || !U)) || winsize <= 0 || (winsize & 1) ||
       winsize > 96 || !(tol > 0))
     return fail(c, STDIC_E_ARG, "LocalICGNQuadtree: bad arguments (winsize even, 2..96)");
@@ -564,16 +567,16 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
   const bool batched = precision == STDIC_BATCHED_F32;
   Plan pl;
   FrameDev d;
-  stage_frame(c, pl, fr, &d, batched, 1);
+  stage_frame(c, pl, fr, &d, batched, frames);
   stdic::IcgnArgs a{};
-  pl.in(U0, 2 * (size_t)N, (double**)&a.U0);
+  pl.in(U0, 2 * NT, (double**)&a.U0);
   pl.in(coords, 2 * (size_t)N, (double**)&a.coords);
   pl.in(ws_list, (size_t)N, (int32_t**)&a.ws_list);
-  pl.out(U, 2 * (size_t)N, &a.U);
-  pl.out_opt(F, 4 * (size_t)N, &a.F);
-  pl.out(Hpk, 21 * (size_t)N, &a.Hpk);
-  pl.out_opt(conv, (size_t)N, &a.conv);
-  pl.out(mark_hole, (size_t)N, &a.mark);
+  pl.out(U, 2 * NT, &a.U);
+  pl.out_opt(F, 4 * NT, &a.F);
+  pl.out(Hpk, 21 * NT, &a.Hpk);
+  pl.out_opt(conv, NT, &a.conv);
+  pl.out(mark_hole, NT, &a.mark);
   int32_t* order = nullptr;
   unsigned char* bscr = nullptr;
   const int npx_max = stdic::grown_tile_pixels(winsize);
@@ -582,13 +585,14 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
   double *H6 = nullptr, *Hinv6 = nullptr;
   int32_t* order2 = nullptr;
   if (batched) {
-    cands = batched_candidates(c, false, npx_max, N);
+    const size_t nt = std::max(NT, (size_t)1);
+    cands = batched_candidates(c, false, npx_max, (int)NT);
     pl.scratch((size_t)std::max(N, 1), &order);
     pl.scratch(batched_scratch_need(cands), &bscr);
-    pl.scratch((size_t)std::max(N, 1), &st6);
-    pl.scratch(21 * (size_t)std::max(N, 1), &H6);
-    pl.scratch(36 * (size_t)std::max(N, 1), &Hinv6);
-    pl.scratch(2 * (size_t)std::max(N, 1), &order2);
+    pl.scratch(nt, &st6);
+    pl.scratch(21 * nt, &H6);
+    pl.scratch(36 * nt, &Hinv6);
+    pl.scratch(2 * nt, &order2);
   }
   int rc = pl.commit(c);
   if (rc) return rc;
@@ -603,15 +607,16 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
       cudaEventRecord(c->es1, c->stream);
       c->solver_timed = rc == STDIC_OK;
     } else {
-      rc = convert_frame(c, fr, &d, 1);
+      rc = convert_frame(c, fr, &d, frames);
       if (!rc) {
         stdic::BatchedArgs b{};
         b.a = a;
         b.f32 = d.f32; b.g32 = d.g32; b.dfdx32 = d.dfdx32; b.dfdy32 = d.dfdy32;
-        b.order = order; b.two_dof = 0; b.frames = 1; b.g_stride = 0;
+        b.order = order; b.two_dof = 0; b.frames = frames;
+        b.g_stride = (long long)fr->W * fr->H;
         b.scratch = bscr;
         b.st6 = st6; b.H6 = H6; b.Hinv6 = Hinv6; b.order2 = order2;
-        rc = run_batched(c, b, N, cands, QueueKeys{a.ws_list, nullptr, winsize});
+        rc = run_batched(c, b, (int)NT, cands, QueueKeys{a.ws_list, nullptr, winsize});
       }
     }
     if (rc) return rc;
@@ -641,6 +646,13 @@ int stdic_icgn_subsets(stdic_ctx* c, const stdic_frame* fr, const double* U0, co
                          precision, false);
 }
 
+int stdic_icgn_subsets_frames(stdic_ctx* c, const stdic_frame* fr, int frames, const double* U0,
+                              const double* coords, int N, int winsize, const int32_t* ws_list, double tol,
+                              double* U, double* F, double* Hpk, int32_t* conv, int precision) {
+  return icgn_local_impl(c, fr, U0, coords, N, winsize, ws_list, tol, U, F, Hpk, conv, nullptr, nullptr,
+                         precision, false, frames);
+}
+
 static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, const double* FOld,
                        const double* udual, const double* vdual, const double* coords, int N,
                        const int32_t* winsize_list, double mu, double beta, double tol, double* U,
@@ -662,7 +674,7 @@ int stdic_subpb1_subsets(stdic_ctx* c, const stdic_frame* fr, const double* UOld
 }
 
 static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, const double* FOld,
-                 const double* udual, const double* vdual, const double* coords, int N,
+                       const double* udual, const double* vdual, const double* coords, int N,
                        const int32_t* winsize_list, double mu, double beta, double tol, double* U,
                        int32_t* conv, int* badnum, int precision, bool filter) {
   (void)udual;

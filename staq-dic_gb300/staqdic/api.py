@@ -388,3 +388,29 @@ def icgn_adjoint(U, F, coordinatesFEM, ImgRef, ImgDef, winsize, ImgRefMask=None,
                                    ADJ_MODES[mode] if isinstance(mode, str) else int(mode), prec),
             "icgn_adjoint")
     return (cost[0] if not _is_torch(cost) else cost), cost_n, dU, dF, dg
+
+
+def icgn_subsets_frames(U0_list, coordinatesFEM, Df, ImgRef, ImgDef_list, winsize, tol, ws_list=None,
+                        ctx=None):
+    """funICGNQuadtree for several deformed frames sharing ImgRef and one mesh,
+    in one batched launch (stdic_icgn_subsets_frames; no reference
+    counterpart).  Returns lists of U (2N), F (4N) and ConvItPerEle (N)."""
+    c = _ctx(ctx)
+    P = len(ImgDef_list)
+    N = _nodes(coordinatesFEM)
+    dtype = np.float32
+    b = _Bufs()
+    g = np.concatenate([np.asarray(x, dtype=dtype).ravel(order="F") for x in ImgDef_list])
+    fr = _frame(b, Df, ImgRef, g, dtype)
+    U0 = np.concatenate([np.asarray(u, dtype=np.float64).ravel() for u in U0_list])
+    U = np.empty(2 * N * P)
+    F = np.empty(4 * N * P)
+    conv = np.empty(N * P, dtype=np.int32)
+    ws = int(winsize) if ws_list is None else int(max(int(winsize), int(np.max(ws_list))))
+    c.check(c.L.stdic_icgn_subsets_frames(c.h, _lib._c.byref(fr), P, b.ptr(U0, np.float64),
+                                          b.ptr(coordinatesFEM, np.float64), N, ws,
+                                          b.ptr(ws_list, np.int32) if ws_list is not None else None,
+                                          float(tol), U.ctypes.data, F.ctypes.data, None, conv.ctypes.data,
+                                          _lib.STDIC_BATCHED_F32), "funICGNQuadtree (frames)")
+    return ([U[2 * N * k:2 * N * (k + 1)] for k in range(P)], [F[4 * N * k:4 * N * (k + 1)] for k in range(P)],
+            [conv[N * k:N * (k + 1)] for k in range(P)])

@@ -210,6 +210,35 @@ def test_icgn_uneven_quadtree_batched_and_plain(sd, ctx, oracle, hole):
     _cmp_batched(conv, co, U, Uo)
 
 
+def test_multi_frame_batch_matches_each_frame(sd, ctx, oracle):
+    """Several deformed frames (rotation 2k degrees plus a crack opening) in one
+    batched launch give each frame's single-frame results: identical codes,
+    and U within 0.01 px and F within 1e-4 on subsets with equal codes (only
+    the FP32 summation order of the launch shape may differ); the FP64 oracle
+    bounds every frame as for a single frame."""
+    from staqdic import workloads
+    w = workloads.series1024(seed=4, size=256, pairs=4)
+    f = w["f"]
+    wl = np.asarray(w["winsize_list"], np.int32)
+    c = w["coordinatesFEM"]
+    f64 = f.astype(np.float64)
+    Dref = oracle.funImgGradient(f64, w["maskf"])
+    Df32 = {k: (v.astype(np.float32) if k in ("DfDx", "DfDy") else v) for k, v in Dref.items()}
+    Ul, Fl, cl = sd.icgn_subsets_frames(w["U0_list"], c, Df32, f, w["g_list"], int(wl.max()), 1e-2,
+                                        ws_list=wl, ctx=ctx)
+    for k, g in enumerate(w["g_list"]):
+        U1, F1, H1, c1 = sd.icgn_subsets(w["U0_list"][k], c, Df32, f, g, int(wl.max()), 1e-2,
+                                         precision="batched", ws_list=wl, ctx=ctx)
+        assert np.mean(cl[k] == c1) >= 0.99
+        same = (cl[k] == c1) & (c1 >= 1) & (c1 <= 100)
+        assert same.sum() > 0.5 * c1.size
+        dU = np.abs(Ul[k] - U1).reshape(-1, 2).max(axis=1)
+        dF = np.abs(Fl[k] - F1).reshape(-1, 4).max(axis=1)
+        assert dU[same].max() <= 0.01 and dF[same].max() <= 1e-4
+        Uo, Fo, Ho, co, _ = oracle.icgn6(w["U0_list"][k], c, Dref, f64, g.astype(np.float64), wl, 1e-2)
+        _cmp_batched(cl[k], co, Ul[k], Uo, Fl[k], Fo)
+
+
 # ------------------------------------------------------------------ Subpb1
 def _subpb1_inputs(oracle, golden):
     d, f, g, Dref = golden

@@ -12,9 +12,10 @@ with pinned host buffers, copies inside the timed region, gives `e2e`.  The L2
 is flushed (256 MiB write) between timed steps.
 
 Beside the headline the line carries, on one GPU, the 2048^2 quadtree pass
-(config C3, ``c3``: batched vs plain FP64 vs the host CPU) and the timing of
-the adjoint on the 4096^2 bumps pair (config C4, ``adjoint_c4``); --no-extras
-skips them.
+(config C3, ``c3``: batched vs plain FP64 vs the host CPU), the timing of
+the adjoint on the 4096^2 bumps pair (config C4, ``adjoint_c4``) and 16 frames
+in one multi-frame launch against the frames one by one (config C5, ``c5``);
+--no-extras skips them.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -213,6 +214,18 @@ def run_reference(args, world, rank):
 
 
 # ----------------------------------------------------------------------------
+def reduce_over_ranks(dist, ms, n, device):
+    """Replica aggregation: the slowest rank's time per step and the converged
+    subsets of all ranks (the path has no data-path collective; this is the
+    only exchange, outside the timed region)."""
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    k = torch.tensor([float(n)], dtype=torch.float64, device=device)
+    dist.all_reduce(k)
+    return float(t.item()), float(k.item())
+
+
 class LocalRun:
     """Device-resident frame, gradients and outputs of one LocalICGNQuadtree
     workload, and the call through the C ABI."""
@@ -318,6 +331,84 @@ def measure_c3(ctx, torch, flush, steps=5):
         out["cpu_baseline"] = cpu
         out["batched_over_cpu"] = out["value"] / cpu["value"]
     return out
+
+
+def measure_c5(ctx, torch, flush, steps=3):
+    """16 deformed frames (rotation 2k degrees plus a crack opening) of one
+    1024^2 reference frame and quadtree mesh (config C5): one multi-frame
+    batched launch against the 16 frames one by one, device-resident inputs."""
+    import ctypes
+    from staqdic import _lib
+    w = make_workload("series1024")
+    L = ctx.L
+    W, H = w["f"].shape
+    N = int(w["coordinatesFEM"].shape[0])
+    P = len(w["g_list"])
+    dev = lambda a, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dt).ravel(order="F"))).cuda()
+    f32 = dev(w["f"], np.float32)
+    g32 = torch.cat([dev(g, np.float32) for g in w["g_list"]])
+    mask = dev(w["maskf"], np.uint8)
+    wl = np.ascontiguousarray(w["winsize_list"], dtype=np.int32)
+    wsl, coords = dev(wl, np.int32), dev(w["coordinatesFEM"], np.float64)
+    U0 = torch.cat([dev(u, np.float64) for u in w["U0_list"]])
+    gx = torch.empty((W - 6) * (H - 6), dtype=torch.float32, device="cuda")
+    gy = torch.empty_like(gx)
+    ctx.check(L.stdic_img_gradient(ctx.h, f32.data_ptr(), mask.data_ptr(), W, H, gx.data_ptr(), gy.data_ptr(),
+                                   _lib.STDIC_F32), "gradient")
+    U = torch.empty(2 * N * P, dtype=torch.float64, device="cuda")
+    F = torch.empty(4 * N * P, dtype=torch.float64, device="cuda")
+    conv = torch.empty(N * P, dtype=torch.int32, device="cuda")
+    ws_max = int(wl.max())
+
+    def frame(gptr):
+        fr = _lib.Frame()
+        fr.f, fr.g, fr.mask, fr.dfdx, fr.dfdy = f32.data_ptr(), gptr, mask.data_ptr(), gx.data_ptr(), gy.data_ptr()
+        fr.W, fr.H, fr.dtype = W, H, _lib.STDIC_F32
+        return fr
+
+    fr_all = frame(g32.data_ptr())
+
+    def multi():
+        ctx.check(L.stdic_icgn_subsets_frames(ctx.h, ctypes.byref(fr_all), P, U0.data_ptr(), coords.data_ptr(), N,
+                                              ws_max, wsl.data_ptr(), TOL, U.data_ptr(), F.data_ptr(), None,
+                                              conv.data_ptr(), _lib.STDIC_BATCHED_F32), "frames")
+
+    frs = [frame(g32.data_ptr() + 4 * W * H * k) for k in range(P)]
+
+    def singles():
+        for k in range(P):
+            ctx.check(L.stdic_icgn_subsets(ctx.h, ctypes.byref(frs[k]), U0.data_ptr() + 16 * N * k,
+                                           coords.data_ptr(), N, ws_max, wsl.data_ptr(), TOL,
+                                           U.data_ptr() + 16 * N * k, F.data_ptr() + 32 * N * k, None,
+                                           conv.data_ptr() + 4 * N * k, _lib.STDIC_BATCHED_F32), "single")
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        ms = []
+        for i in range(steps):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.mean(ms))
+
+    ms_single = timed(singles)
+    c_single, U_single = conv.cpu().numpy(), U.cpu().numpy()
+    ms_multi = timed(multi)
+    c_multi, U_multi = conv.cpu().numpy(), U.cpu().numpy()
+    nconv = int(((c_multi >= 1) & (c_multi <= 100) & ~np.isnan(U_multi[0::2])).sum())
+    same = (c_multi == c_single) & (c_multi >= 1) & (c_multi <= 100)
+    dU = np.abs(U_multi - U_single).reshape(-1, 2).max(axis=1)
+    return {"workload": "series1024: %d frames of %dx%d, rotation 2k deg + crack, quadtree %d nodes" % (P, W, H, N),
+            "subsets_per_launch": N * P, "value": nconv / (ms_multi * 1e-3), "unit": UNIT,
+            "ms_per_launch": ms_multi, "frames_one_by_one": {"value": nconv / (ms_single * 1e-3),
+                                                             "ms": ms_single},
+            "codes_equal_frac": float(np.mean(c_multi == c_single)),
+            "max_abs_du_px_equal_codes": float(dU[same].max()) if same.any() else None}
 
 
 def measure_adjoint(ctx, torch, size=4096):
@@ -452,12 +543,7 @@ def main():
     total_ms = float(np.sum(step_ms))
     mean_ms = total_ms / len(step_ms)
     if dist:
-        t = torch.tensor([mean_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        mean_ms = float(t.item())
-        n = torch.tensor([n_conv], device="cuda", dtype=torch.float64)
-        dist.all_reduce(n)
-        n_conv_all = float(n.item())
+        mean_ms, n_conv_all = reduce_over_ranks(dist, mean_ms, n_conv, "cuda")
     else:
         n_conv_all = float(n_conv)
     value = n_conv_all / (mean_ms * 1e-3)
@@ -503,12 +589,7 @@ def main():
     n_conv_e2e = int(((ocn >= 1) & (ocn <= 100) & ~np.isnan(oUn[0::2]) & ~np.isnan(Up[0::2]) & (dUe <= TOLPX)).sum())
     e2e_mean = float(np.mean(e2e_ms))
     if dist:
-        t = torch.tensor([e2e_mean], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_mean = float(t.item())
-        n = torch.tensor([n_conv_e2e], device="cuda", dtype=torch.float64)
-        dist.all_reduce(n)
-        n_conv_e2e = float(n.item())
+        e2e_mean, n_conv_e2e = reduce_over_ranks(dist, e2e_mean, n_conv_e2e, "cuda")
     e2e_value = n_conv_e2e / (e2e_mean * 1e-3)
 
     if rank != 0:
@@ -572,6 +653,7 @@ def main():
     if world == 1 and not args.no_extras:
         out["c3"] = measure_c3(ctx, torch, flush)
         out["adjoint_c4"] = measure_adjoint(ctx, torch)
+        out["c5"] = measure_c5(ctx, torch, flush)
     print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -121,10 +121,11 @@ def invert_map(ufun, xs, ys, iters=30):
     return np.concatenate([p[0] for p in parts], 0), np.concatenate([p[1] for p in parts], 0)
 
 
-def render_pair(W, H, sp, ufun, noise=0.01, rng=None, inv=None):
-    """Reference and deformed images for displacement field ufun(X, Y)."""
+def render_pair(W, H, sp, ufun, noise=0.01, rng=None, inv=None, want_f=True):
+    """Reference and deformed images for displacement field ufun(X, Y)
+    (f is None when want_f is false)."""
     xs, ys = pixel_grid(W, H)
-    f = _render(sp, W, H, xs, ys, sp.cx, sp.cy)
+    f = _render(sp, W, H, xs, ys, sp.cx, sp.cy) if want_f else None
     if inv is None:
         X, Y = invert_map(ufun, xs, ys)
     else:
@@ -132,9 +133,10 @@ def render_pair(W, H, sp, ufun, noise=0.01, rng=None, inv=None):
     ux, uy = ufun(sp.cx, sp.cy)
     g = _render(sp, W, H, X, Y, sp.cx + ux, sp.cy + uy, grow=1.2)
     if noise and rng is not None:
-        f = f + rng.normal(0.0, noise, f.shape)
+        if f is not None:
+            f = f + rng.normal(0.0, noise, f.shape)
         g = g + rng.normal(0.0, noise, g.shape)
-    return np.asfortranarray(f), np.asfortranarray(g), X, Y
+    return (np.asfortranarray(f) if f is not None else None), np.asfortranarray(g), X, Y
 
 
 def normalize(img, roi=None):

@@ -154,7 +154,7 @@ def series1024(seed=4, size=1024, pairs=16):
     ws_list = np.clip(2 * hn, 8, 64).astype(np.int32)
     for k in range(pairs):
         ufun, inv = synth.crack_rotation_field(2.0 * k, centre, cy, cxm, 5.0 * size / 1024)
-        _, g, X, Y = synth.render_pair(W, H, sp, ufun, noise=0.0, inv=inv)
+        _, g, X, Y = synth.render_pair(W, H, sp, ufun, noise=0.0, inv=inv, want_f=False)
         g = g + rng.normal(0, 0.01, (W, H))
         maskg = (~((np.abs(Y - cy) <= 3) & (X < cxm)) & (X >= 1) & (X <= W) & (Y >= 1) & (Y <= H))
         gs.append(np.asfortranarray((synth.normalize(g) * maskg).astype(np.float32)))

@@ -482,11 +482,14 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
     b.gtile = cd.gtile_per_warp * cd.tw;
     b.gtile_small = cd.split ? cd.gtile_per_warp : 0;
     // Single warps take the queue smallest first, so that the small subsets
-    // that run to the iteration limit start early; split teams take the large
-    // subsets largest first, then single warps the rest smallest first.
+    // that run to the iteration limit start early.  The split form takes it
+    // largest first: its wide teams already start with the masked subsets
+    // (the long chains) in the 6-DOF iteration stage, and the single-warp
+    // list, filled in set-up order, then runs largest first too.
+    const int mode = cd.split ? (two ? 2 : 0) : (cd.tw == 1 ? 1 : 0);
     int rc = check_launch(c, stdic::launch_build_queue(qk.ws_list, qk.wsl2, qk.ws_all, b.a.N,
-                                                       (int32_t*)b.order, c->scal + 6, c->stream,
-                                                       cd.split ? 2 : (cd.tw == 1 ? 1 : 0), cd.split),
+                                                       (int32_t*)b.order, c->scal + 6, c->stream, mode,
+                                                       cd.split),
                           "queue");
     if (rc) return rc;
     // 2-DOF: one fused pass; 6-DOF: set-up, FP64 factorisation, iterations

@@ -23,7 +23,8 @@ struct stdic_ctx {
   void* ws = nullptr;
   size_t ws_size = 0;
   int* scal = nullptr;  // device scalars: [1] badnum, [2] iters, [3] status, [4..5] queue heads, [6] queue split,
-                        // [7] adjoint queue head, [8..9] iteration-list counts
+                        // [7] adjoint queue head, [8..9] iteration-list counts,
+                        // [10] gradient tile-copy time-out flag
   double* scald = nullptr;  // device double scalars: [0] residual
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t es0 = nullptr, es1 = nullptr;  // around the last IC-GN solver kernel
@@ -277,9 +278,17 @@ int stdic_img_gradient(stdic_ctx* c, const void* img, const uint8_t* mask, int W
   pl.out((unsigned char*)dfdy, es * (W - 6) * (H - 6), &dy);
   int rc = pl.commit(c);
   if (rc) return rc;
-  rc = check_launch(c, stdic::launch_gradient(di, dm, W, H, dx, dy, dtype, c->stream), "funImgGradient");
+  cudaMemsetAsync(c->scal + 10, 0, sizeof(int), c->stream);
+  rc = check_launch(c, stdic::launch_gradient(di, dm, W, H, dx, dy, dtype, c->stream, c->scal + 10),
+                    "funImgGradient");
   if (rc) return rc;
-  return pl.finish(c);
+  rc = pl.finish(c);
+  if (rc || !pl.any_host) return rc;
+  // the call has synchronised: report a tile copy whose bounded wait gave up
+  int timed_out = 0;
+  rc = read_scalar(c, c->scal + 10, &timed_out);
+  if (rc) return rc;
+  return timed_out ? fail(c, STDIC_E_TIMEOUT, "funImgGradient: a tile copy did not complete") : STDIC_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -101,8 +101,9 @@ int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px, int gtile)
 
 cudaError_t launch_interp(const void* F, long long M, long long N, long long P, const void* X,
                           const void* Y, long long n, void* out, int dtype, cudaStream_t s);
+// err (optional, device) is set to 1 when a tile copy's bounded wait gives up.
 cudaError_t launch_gradient(const void* img, const uint8_t* mask, int W, int H, void* dfdx,
-                            void* dfdy, int dtype, cudaStream_t s);
+                            void* dfdy, int dtype, cudaStream_t s, int* err = nullptr);
 cudaError_t launch_intsearch(const double* f, const double* g, int W, int H, int Sx, int Sy,
                              double gx0, double gy0, int nx, int ny, int wsx, int wsy, int stepx,
                              int stepy, double* x, double* y, double* u, double* v, double* cc,

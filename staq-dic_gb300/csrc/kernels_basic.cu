@@ -6,6 +6,11 @@
 //                      normxcorr2 restated from its published definition
 //   badpoints_kernel   LocalICGNQuadtree.m:153-177 / Subpb1Quadtree.m:173-191
 #include <cfloat>
+#include <cstdint>
+#include <mutex>
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include "device_common.cuh"
 #include "kernels.h"
@@ -92,11 +97,118 @@ __global__ void __launch_bounds__(256) gradient_kernel(const REAL* __restrict__ 
   dfdy[(long long)j * Wo + i] = sy * m;
 }
 
+// The same stencil with the input tile (32 x 8 outputs plus the 3-pixel halo,
+// 40 x 14 elements) brought into shared memory by one TMA 2-D tile copy
+// completing on an mbarrier.  The copy starts at the tile origin, whose x is a
+// multiple of 32 elements (TMA's 16-byte rule); elements beyond the image are
+// filled with zeros by the copy.  The wait is bounded: after 2^24 polls the
+// CTA sets *err and leaves its outputs unwritten.
+template <class REAL>
+__global__ void __launch_bounds__(256) gradient_tma_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                           const uint8_t* __restrict__ mask, int W,
+                                                           int H, REAL* __restrict__ dfdx,
+                                                           REAL* __restrict__ dfdy, int* err) {
+  constexpr int TX = 32, TY = 8, R = 3, BX = 40, BY = TY + 2 * R;
+  __shared__ __align__(128) REAL t[BY][BX];
+  __shared__ __align__(8) uint64_t bar;
+  const int Wo = W - 6, Ho = H - 6;
+  const int bx = blockIdx.x * TX, by = blockIdx.y * TY;
+  const unsigned sbar = (unsigned)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned bytes = (unsigned)(BX * BY * sizeof(REAL));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar), "r"(bytes) : "memory");
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(&t[0][0]);
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<unsigned long long>(&tmap)), "r"(bx), "r"(by), "r"(sbar)
+        : "memory");
+  }
+  bool ok = false;
+  for (int it = 0; it < (1 << 24) && !ok; ++it) {
+    unsigned done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done) : "r"(sbar), "r"(0u) : "memory");
+    ok = done != 0;
+  }
+  if (!ok) {
+    if (threadIdx.x == 0 && err) atomicExch(err, 1);
+    return;
+  }
+  const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
+  const int i = bx + lx, j = by + ly;
+  if (i >= Wo || j >= Ho) return;
+  const REAL h[7] = {REAL(-1.0 / 60), REAL(3.0 / 20), REAL(-3.0 / 4), REAL(0.0),
+                     REAL(3.0 / 4), REAL(-3.0 / 20), REAL(1.0 / 60)};
+  REAL sx = 0, sy = 0;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    if constexpr (sizeof(REAL) == 8) {
+      sx = da(sx, dm(h[k], t[ly + R][lx + k]));
+      sy = da(sy, dm(h[k], t[ly + k][lx + R]));
+    } else {
+      sx = __fadd_rn(sx, __fmul_rn(h[k], t[ly + R][lx + k]));
+      sy = __fadd_rn(sy, __fmul_rn(h[k], t[ly + k][lx + R]));
+    }
+  }
+  const REAL m = (REAL)mask[(long long)(j + 3) * W + (i + 3)];
+  dfdx[(long long)j * Wo + i] = sx * m;
+  dfdy[(long long)j * Wo + i] = sy * m;
+}
+
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// 2-D tensor map of a W x H image (x = dim 1 contiguous) with a 40 x 14 box;
+// false when TMA cannot describe it (pitch or base not 16-byte aligned).
+bool image_tensor_map(const void* img, int W, int H, int dtype, CUtensorMap* m) {
+  const size_t es = dtype == 0 ? 8 : 4;
+  if (((uintptr_t)img & 15) != 0 || ((size_t)W * es) % 16 != 0) return false;
+  auto enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
+  const cuuint64_t strides[1] = {(cuuint64_t)W * es};
+  const cuuint32_t box[2] = {40, 14};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, dtype == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+             const_cast<void*>(img), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace
+
 cudaError_t launch_gradient(const void* img, const uint8_t* mask, int W, int H, void* dfdx,
-                            void* dfdy, int dtype, cudaStream_t s) {
+                            void* dfdy, int dtype, cudaStream_t s, int* err) {
   const int Wo = W - 6, Ho = H - 6;
   if (Wo <= 0 || Ho <= 0) return cudaErrorInvalidValue;
   dim3 grid((Wo + 31) / 32, (Ho + 7) / 8);
+  CUtensorMap tm;
+  if (image_tensor_map(img, W, H, dtype, &tm)) {
+    if (dtype == 0)
+      gradient_tma_kernel<double><<<grid, 256, 0, s>>>(tm, mask, W, H, (double*)dfdx, (double*)dfdy, err);
+    else
+      gradient_tma_kernel<float><<<grid, 256, 0, s>>>(tm, mask, W, H, (float*)dfdx, (float*)dfdy, err);
+    return cudaGetLastError();
+  }
   if (dtype == 0)
     gradient_kernel<double><<<grid, 256, 0, s>>>((const double*)img, mask, W, H, (double*)dfdx,
                                                  (double*)dfdy);

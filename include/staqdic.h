@@ -195,6 +195,44 @@ int stdic_icgn_subsets_frames(stdic_ctx* ctx, const stdic_frame* fr, int frames,
                               double tol, double* U, double* F, double* Hpk, int32_t* conv,
                               int precision);
 
+/* The strain step of the ADMM loop (a local replacement; the active loop
+ * calls funGlobalNodalStrainRBF.m).  The Gauss-point strains DN U of every
+ * element are those of funGlobalNodalStrainQuadtree.m:80-257; each node takes
+ * the mean, over the elements containing it, of each element's Gauss point
+ * nearest to it (the reference interpolates with a natural-neighbour
+ * scatteredInterpolant).  F (4N) = [du/dx dv/dx du/dy dv/dy] per node, the
+ * order of the active loop's strain step; NaN at nodes in no element. */
+int stdic_nodal_strain(stdic_ctx* ctx, const double* coords, int N, const int32_t* elems, int E,
+                       const double* U, int gauss_order, double* F);
+
+/* The NaN fill after the local step (a local replacement of the thin-plate RBF
+ * fill of Subpb1Quadtree.m:193-259): in sweeps, every node whose U (2N,
+ * in/out) is NaN takes the mean of its finite mesh neighbours of the previous
+ * sweep, until no NaN node has a finite neighbour. */
+int stdic_fill_nans(stdic_ctx* ctx, const double* coords, int N, const int32_t* elems, int E,
+                    double* U);
+
+/* `steps` ADMM iterations of main_ALDIC_Quadtree_v2.m:337-395 on one frame:
+ *   U1 = Subpb1(U2, F2, vdual) with its bad-subset filter, NaN fill
+ *   (stdic_fill_nans) and U1(hole) = U2(hole); F1 = F2;
+ *   U2 = Subpb2(U1, F1) (GaussPtOrder 2, alpha 0, PCG tol 1e-10);
+ *   F2 = nodal strain of U2 (stdic_nodal_strain); F2(hole) = F1(hole),
+ *   U2(hole) = U1(hole); udual = F2 - F1; vdual = U2 - U1.
+ * winsize_list is N x 2; mark_hole (N, may be NULL) is markCoordHoleStrain.
+ * U2 (2N), F2 (4N), udual (4N), vdual (2N) are read and updated; U1 (2N) is
+ * the last local solution; badnum and pcg_iters (steps each) the per-step
+ * LocalICGNBadPtNum and CG counts (each may be NULL).  With use_graph the
+ * first iteration runs directly and the others replay one CUDA graph of the
+ * iteration; graph_used (may be NULL) says whether the capture succeeded.
+ * The strain and fill steps are local replacements of the reference's global
+ * ones, so the iterates follow the reference's scheme, not its exact values. */
+int stdic_admm(stdic_ctx* ctx, const stdic_frame* fr, const double* coords, int N,
+               const int32_t* elems, int E, const int32_t* dirichlet, int nd,
+               const int32_t* winsize_list, const uint8_t* mark_hole, double mu, double beta,
+               double tol, int steps, int precision, int use_graph, double* U2, double* F2,
+               double* udual, double* vdual, double* U1, int* badnum, int* pcg_iters,
+               int* graph_used);
+
 /* modes of stdic_icgn_adjoint */
 enum {
   STDIC_ADJ_RECOMPUTE = 0, /* interpolate each subset again in the backward pass */

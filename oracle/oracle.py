@@ -237,6 +237,29 @@ def icgn_adjoint(ImgRef, ImgDef, mask, coords, winsize, U, F, want_dg=True):
     return cost, dU, dF, dg
 
 
+def nodal_strain(coords, elems, U, gauss_order=2):
+    """Nodal F = [du/dx dv/dx du/dy dv/dy] per node (4N) from the element
+    Gauss-point strains (see orc_nodal_strain)."""
+    coords = _F(coords)
+    el = _F(elems, np.int32)
+    N, E = coords.shape[0], el.shape[0]
+    U = np.ascontiguousarray(U, dtype=np.float64).ravel()
+    F = np.empty(4 * N)
+    lib().orc_nodal_strain(_p(coords, _d), _L(N), _p(el, _i32), _L(E), _p(U, _d), int(gauss_order),
+                           _p(F, _d))
+    return F
+
+
+def fill_nans(coords, elems, U):
+    """U (2N) with NaN nodes filled from their mesh neighbours (see orc_fill_nans)."""
+    coords = _F(coords)
+    el = _F(elems, np.int32)
+    N, E = coords.shape[0], el.shape[0]
+    out = np.array(U, dtype=np.float64).ravel().copy()
+    lib().orc_fill_nans(_p(coords, _d), _L(N), _p(el, _i32), _L(E), _p(out, _d))
+    return out
+
+
 def bad_points_local(conv, maxIterNum=100):
     """LocalICGNQuadtree.m:153-169 -> (bad index array, LocalICGNBadPtNum)."""
     conv = np.asarray(conv)

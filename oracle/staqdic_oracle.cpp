@@ -15,6 +15,9 @@
 //                         func_quadtree/LocalICGNQuadtree.m:67-147
 //   orc_icgn2             func/funICGN_Subpb1.m:34-471 driven as in
 //                         func_quadtree/Subpb1Quadtree.m:75-169
+//   orc_nodal_strain      funGlobalNodalStrainQuadtree.m:80-257 (Gauss-point
+//                         strains); nodal recovery is a local replacement
+//   orc_fill_nans         local replacement of Subpb1Quadtree.m:193-259's fill
 //   orc_adjoint           no counterpart: gradient of the ZNSSD subset cost of
 //                         funICGNQuadtree.m:151-165 (pinned by finite differences)
 //   orc_subpb2_assemble   func_quadtree/Subpb2Quadtree.m:30-336 (element loop,
@@ -1144,6 +1147,120 @@ extern "C" void orc_adjoint(const double* f, const double* g, const uint8_t* mas
     if (dF)
       for (int k = 0; k < 4; ++k) dF[4 * n + k] = dP[k];
     if (dU) { dU[2 * n] = dP[4]; dU[2 * n + 1] = dP[5]; }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Nodal strain (local replacement of the reference's strain step).  The Gauss
+// point strains follow funGlobalNodalStrainQuadtree.m:80-257: at the Gauss
+// points of each element (GaussPtOrder^2, points ordered x-major), DN U with
+// the hanging-node shape functions gives [du/dx du/dy dv/dx dv/dy].  The
+// quadtree elements are axis-aligned rectangles, for which the routine's
+// bilinear inverse map returns ksi, eta equal to the Gauss abscissae.  The
+// reference then interpolates the Gauss-point values to the nodes with a
+// natural-neighbour scatteredInterpolant (:266-276); here every node takes the
+// mean, over the elements that contain it, of each element's Gauss point
+// nearest to it (on a regular mesh the natural-neighbour weights of those
+// points).  Components are stored as the active ADMM loop's strain step stores
+// them (funGlobalNodalStrainRBF.m:52-62): F = [du/dx dv/dx du/dy dv/dy].
+// A node in no element gets NaN.
+// ---------------------------------------------------------------------------
+extern "C" void orc_nodal_strain(const double* coords, long N, const int32_t* elems, long E,
+                                 const double* U, int gauss_order, double* F) {
+  double gpt[5], gwt[5];
+  const int ng = gauss_rule(gauss_order, gpt, gwt);
+  std::vector<double> sum(4 * (size_t)N, 0.0);
+  std::vector<int> cnt(N, 0);
+  for (long e = 0; e < E; ++e) {
+    int nd[8];
+    double px[8], py[8], uu[8], vv[8], dp[4];
+    for (int c = 0; c < 8; ++c) {
+      nd[c] = elems[c * E + e];
+      const bool ok = nd[c] >= 1 && nd[c] <= N;
+      px[c] = ok ? coords[nd[c] - 1] : 0.0;
+      py[c] = ok ? coords[N + nd[c] - 1] : 0.0;
+      uu[c] = ok ? U[2 * (nd[c] - 1)] : 0.0;
+      vv[c] = ok ? U[2 * (nd[c] - 1) + 1] : 0.0;
+    }
+    for (int c = 0; c < 4; ++c) dp[c] = nd[4 + c] != 0 ? 1.0 : 0.0;
+    const double x1 = px[0], x3 = px[2], y1 = py[0], y3 = py[2];
+    std::vector<double> gs(4 * ng * ng), gxv(ng * ng), gyv(ng * ng);
+    for (int ti = 0; ti < ng; ++ti)
+      for (int tj = 0; tj < ng; ++tj) {
+        const int g = ng * ti + tj;
+        const double ksi = gpt[ti], eta = gpt[tj];
+        gxv[g] = gpt[ti] * 0.5 * (x3 - x1) + 0.5 * (x3 + x1);
+        gyv[g] = gpt[tj] * 0.5 * (y3 - y1) + 0.5 * (y3 + y1);
+        double dk[8], de[8];
+        shape_derivs(ksi, eta, dp, dk, de);
+        double J11 = 0, J12 = 0, J21 = 0, J22 = 0;
+        for (int c = 0; c < 8; ++c) {
+          J11 += dk[c] * px[c]; J12 += dk[c] * py[c];
+          J21 += de[c] * px[c]; J22 += de[c] * py[c];
+        }
+        const double det = J11 * J22 - J12 * J21;
+        const double i11 = J22 / det, i12 = -J12 / det, i21 = -J21 / det, i22 = J11 / det;
+        double dudx = 0, dudy = 0, dvdx = 0, dvdy = 0;
+        for (int c = 0; c < 8; ++c) {
+          const double gx = i11 * dk[c] + i12 * de[c], gy = i21 * dk[c] + i22 * de[c];
+          dudx += gx * uu[c]; dudy += gy * uu[c];
+          dvdx += gx * vv[c]; dvdy += gy * vv[c];
+        }
+        gs[4 * g] = dudx; gs[4 * g + 1] = dvdx; gs[4 * g + 2] = dudy; gs[4 * g + 3] = dvdy;
+      }
+    for (int c = 0; c < 8; ++c) {
+      if (nd[c] < 1 || nd[c] > N) continue;
+      const long n = nd[c] - 1;
+      int best = 0;
+      double bd = 1e300;
+      for (int g = 0; g < ng * ng; ++g) {
+        const double dx = gxv[g] - coords[n], dy = gyv[g] - coords[N + n];
+        const double d2 = dx * dx + dy * dy;
+        if (d2 < bd) { bd = d2; best = g; }
+      }
+      for (int k = 0; k < 4; ++k) sum[4 * n + k] += gs[4 * best + k];
+      cnt[n] += 1;
+    }
+  }
+  for (long n = 0; n < N; ++n)
+    for (int k = 0; k < 4; ++k) F[4 * n + k] = cnt[n] ? sum[4 * n + k] / cnt[n] : NAN;
+}
+
+// NaN fill (local replacement of the reference's thin-plate RBF fill,
+// Subpb1Quadtree.m:193-259): sweeps in which every node whose displacement is
+// NaN and which shares an element with finite nodes takes the mean of those
+// neighbours' values of the previous sweep (neighbours in increasing node
+// order), until no NaN node has a finite neighbour.
+extern "C" void orc_fill_nans(const double* coords, long N, const int32_t* elems, long E, double* U) {
+  (void)coords;
+  std::vector<std::vector<long>> nb(N);
+  for (long e = 0; e < E; ++e)
+    for (int a = 0; a < 8; ++a) {
+      const long p = elems[a * E + e];
+      if (p < 1 || p > N) continue;
+      for (int b = 0; b < 8; ++b) {
+        const long q = elems[b * E + e];
+        if (q < 1 || q > N || q == p) continue;
+        nb[p - 1].push_back(q - 1);
+      }
+    }
+  for (auto& v : nb) {
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+  }
+  std::vector<double> old(U, U + 2 * N);
+  for (;;) {
+    bool changed = false;
+    for (long n = 0; n < N; ++n) {
+      if (!std::isnan(old[2 * n])) continue;
+      double su = 0, sv = 0;
+      int k = 0;
+      for (long m : nb[n])
+        if (!std::isnan(old[2 * m])) { su += old[2 * m]; sv += old[2 * m + 1]; ++k; }
+      if (k) { U[2 * n] = su / k; U[2 * n + 1] = sv / k; changed = true; }
+    }
+    if (!changed) break;
+    std::copy(U, U + 2 * N, old.begin());
   }
 }
 

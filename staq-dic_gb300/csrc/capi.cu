@@ -34,6 +34,7 @@ struct stdic_ctx {
   // autotuner cache: (N bucket, npx_max, two_dof, frames) -> index of the launch shape
   std::map<std::tuple<int, int, int, int>, int> tune;
   int tuning = 1;
+  bool capturing = false;  // the stream is being captured into a CUDA graph
 };
 
 namespace {
@@ -530,7 +531,10 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
   if (it == c->tune.end()) {
     int best = 0;
     const int pick = tune_pick();
-    if (pick >= 0) {
+    if (c->capturing) {
+      // no timing inside a capture: the first shape, or the fixed one
+      best = pick >= 0 ? std::min(pick, (int)cands.size() - 1) : 0;
+    } else if (pick >= 0) {
       best = std::min(pick, (int)cands.size() - 1);
     } else if (c->tuning && Ntot > 0 && cands.size() > 1) {
       float bt = 1e30f;
@@ -551,6 +555,7 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
     it = c->tune.emplace(key, best).first;
   }
   const BatchedCand* chosen = &cands[std::min<size_t>((size_t)it->second, cands.size() - 1)];
+  if (c->capturing) return launch(*chosen);
   cudaEventRecord(c->es0, c->stream);
   const int rc = launch(*chosen);
   cudaEventRecord(c->es1, c->stream);
@@ -854,6 +859,259 @@ int stdic_icgn_adjoint(stdic_ctx* c, const stdic_frame* fr, const double* coords
   if (e != cudaSuccess) return cuda_fail(c, e, "adjoint");
   c->solver_timed = true;
   return pl.finish(c);
+}
+
+int stdic_nodal_strain(stdic_ctx* c, const double* coords, int N, const int32_t* elems, int E,
+                       const double* U, int gauss_order, double* F) {
+  if (!c) return STDIC_E_ARG;
+  if (N < 0 || E < 0 || (N > 0 && (!coords || !U || !F)) || (E > 0 && !elems) || gauss_order < 2 ||
+      gauss_order > 5)
+    return fail(c, STDIC_E_ARG, "nodal strain: bad arguments (GaussPtOrder 2..5)");
+  cudaSetDevice(c->device);
+  Plan pl;
+  const double *dc = nullptr, *du = nullptr;
+  const int32_t* de = nullptr;
+  double* dF = nullptr;
+  unsigned char* tws = nullptr;
+  pl.in(coords, 2 * (size_t)N, (double**)&dc);
+  pl.in(elems, 8 * (size_t)E, (int32_t**)&de);
+  pl.in(U, 2 * (size_t)N, (double**)&du);
+  pl.out(F, 4 * (size_t)N, &dF);
+  pl.scratch(stdic::topo_workspace_bytes(N, E), &tws);
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  if (N > 0) {
+    int *ptr = nullptr, *list = nullptr;
+    rc = check_launch(c, stdic::build_topology(de, E, N, tws, &ptr, &list, c->stream), "mesh topology");
+    if (!rc) rc = check_launch(c, stdic::launch_nodal_strain(dc, N, de, E, du, gauss_order, ptr, list, dF, c->stream),
+                               "nodal strain");
+    if (rc) return rc;
+  }
+  return pl.finish(c);
+}
+
+int stdic_fill_nans(stdic_ctx* c, const double* coords, int N, const int32_t* elems, int E, double* U) {
+  if (!c) return STDIC_E_ARG;
+  if (N < 0 || E < 0 || (N > 0 && !U) || (E > 0 && !elems))
+    return fail(c, STDIC_E_ARG, "NaN fill: bad arguments");
+  (void)coords;
+  cudaSetDevice(c->device);
+  Plan pl;
+  const double* uin = nullptr;
+  double* uout = nullptr;
+  const int32_t* de = nullptr;
+  double* tmp = nullptr;
+  unsigned char* tws = nullptr;
+  pl.in(elems, 8 * (size_t)E, (int32_t**)&de);
+  pl.in((const double*)U, 2 * (size_t)N, (double**)&uin);
+  pl.out(U, 2 * (size_t)N, &uout);
+  pl.scratch(2 * (size_t)std::max(N, 1), &tmp);
+  pl.scratch(stdic::topo_workspace_bytes(N, E), &tws);
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  if (N > 0) {
+    if (uin != uout) {
+      cudaError_t e = cudaMemcpyAsync(uout, uin, 16 * (size_t)N, cudaMemcpyDeviceToDevice, c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "NaN fill");
+    }
+    int *ptr = nullptr, *list = nullptr;
+    rc = check_launch(c, stdic::build_topology(de, E, N, tws, &ptr, &list, c->stream), "mesh topology");
+    if (!rc) rc = check_launch(c, stdic::launch_fill_nans(N, de, E, ptr, list, uout, tmp, c->stream), "NaN fill");
+    if (rc) return rc;
+  }
+  return pl.finish(c);
+}
+
+int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N, const int32_t* elems, int E,
+               const int32_t* dirichlet, int nd, const int32_t* winsize_list, const uint8_t* mark_hole,
+               double mu, double beta, double tol, int steps, int precision, int use_graph, double* U2,
+               double* F2, double* udual, double* vdual, double* U1, int* badnum, int* pcg_iters,
+               int* graph_used) {
+  if (!c) return STDIC_E_ARG;
+  if (N <= 0 || E <= 0 || !frame_ok(fr) || !coords || !elems || !winsize_list || !U2 || !F2 || !udual ||
+      !vdual || steps < 1 || (nd > 0 && !dirichlet) || nd < 0 || !(tol > 0))
+    return fail(c, STDIC_E_ARG, "ADMM: bad arguments");
+  if (precision == STDIC_PLAIN_F64 && fr->dtype != STDIC_F64)
+    return fail(c, STDIC_E_ARG, "plain FP64 IC-GN needs double images");
+  if (precision != STDIC_PLAIN_F64 && precision != STDIC_BATCHED_F32)
+    return fail(c, STDIC_E_ARG, "unknown precision");
+  cudaSetDevice(c->device);
+  const bool batched = precision == STDIC_BATCHED_F32;
+  int wmax = 2;
+  {
+    std::vector<int32_t> wl(2 * (size_t)N);
+    if (is_device_ptr(winsize_list)) {
+      cudaMemcpyAsync(wl.data(), winsize_list, wl.size() * 4, cudaMemcpyDeviceToHost, c->stream);
+      cudaStreamSynchronize(c->stream);
+    } else {
+      std::memcpy(wl.data(), winsize_list, wl.size() * 4);
+    }
+    for (int32_t w : wl) wmax = std::max(wmax, (int)w);
+  }
+  if (wmax > 96) return fail(c, STDIC_E_ARG, "ADMM: winsize_List entries must be <= 96");
+  const size_t n2 = 2 * (size_t)N, n4 = 4 * (size_t)N;
+  Plan pl;
+  FrameDev d;
+  stage_frame(c, pl, fr, &d, batched, 1);
+  const double* dcoords = nullptr;
+  const int32_t *delems = nullptr, *ddir = nullptr, *dwl = nullptr;
+  const uint8_t* dmark = nullptr;
+  pl.in(coords, n2, (double**)&dcoords);
+  pl.in(elems, 8 * (size_t)E, (int32_t**)&delems);
+  pl.in(dirichlet, (size_t)nd, (int32_t**)&ddir);
+  pl.in(winsize_list, n2, (int32_t**)&dwl);
+  pl.in(mark_hole, mark_hole ? (size_t)N : 0, (uint8_t**)&dmark);
+  // in/out state: read at the start, written at the end
+  const double *iU2 = nullptr, *iF2 = nullptr, *iud = nullptr, *ivd = nullptr;
+  double *oU2 = nullptr, *oF2 = nullptr, *oud = nullptr, *ovd = nullptr, *oU1 = nullptr;
+  pl.in((const double*)U2, n2, (double**)&iU2);
+  pl.in((const double*)F2, n4, (double**)&iF2);
+  pl.in((const double*)udual, n4, (double**)&iud);
+  pl.in((const double*)vdual, n2, (double**)&ivd);
+  pl.out(U2, n2, &oU2);
+  pl.out(F2, n4, &oF2);
+  pl.out(udual, n4, &oud);
+  pl.out(vdual, n2, &ovd);
+  pl.out_opt(U1, n2, &oU1);
+  int *hbad = nullptr, *hit = nullptr, *hst = nullptr, *dsc = nullptr;
+  pl.out_opt(badnum, (size_t)steps, &hbad);
+  pl.out_opt(pcg_iters, (size_t)steps, &hit);
+  pl.scratch((size_t)steps, &hst);
+  pl.scratch(8, &dsc);  // [0] badnum, [1] iters, [2] status
+  double *F1 = nullptr, *tmp = nullptr, *dres = nullptr;
+  int32_t* conv = nullptr;
+  pl.scratch(n4, &F1);
+  pl.scratch(n2, &tmp);
+  pl.scratch(8, &dres);
+  pl.scratch((size_t)N, &conv);
+  unsigned char *tws = nullptr, *sws = nullptr, *bscr = nullptr;
+  pl.scratch(stdic::topo_workspace_bytes(N, E), &tws);
+  pl.scratch(stdic::subpb2_workspace_bytes(N, E), &sws);
+  int32_t* order = nullptr;
+  const int npx_max = stdic::grown_tile_pixels(wmax);
+  std::vector<BatchedCand> cands;
+  if (batched) {
+    cands = batched_candidates(c, true, npx_max, N);
+    pl.scratch((size_t)N, &order);
+    pl.scratch(batched_scratch_need(cands), &bscr);
+  }
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  auto copy_in = [&](double* dst, const double* src, size_t n) -> int {
+    if (dst == src) return STDIC_OK;
+    const cudaError_t e = cudaMemcpyAsync(dst, src, 8 * n, cudaMemcpyDeviceToDevice, c->stream);
+    return e == cudaSuccess ? STDIC_OK : cuda_fail(c, e, "ADMM state");
+  };
+  rc = copy_in(oU2, iU2, n2);
+  if (!rc) rc = copy_in(oF2, iF2, n4);
+  if (!rc) rc = copy_in(oud, iud, n4);
+  if (!rc) rc = copy_in(ovd, ivd, n2);
+  if (!rc && batched) rc = convert_frame(c, fr, &d, 1);
+  int *ptr = nullptr, *list = nullptr;
+  if (!rc) rc = check_launch(c, stdic::build_topology(delems, E, N, tws, &ptr, &list, c->stream), "mesh topology");
+  if (rc) return rc;
+
+  // Subpb1 (2-DOF IC-GN): UOld = U2, FOld = F2 -> U1
+  stdic::IcgnArgs a{};
+  a.f = d.f; a.g = d.g; a.mask = d.mask; a.dfdx = d.dfdx; a.dfdy = d.dfdy;
+  a.W = fr->W; a.H = fr->H; a.N = N; a.mu = mu; a.tol = tol; a.ws_max = wmax; a.npx_max = npx_max;
+  a.coords = dcoords; a.UOld = oU2; a.FOld = oF2; a.vdual = ovd; a.wsl2 = dwl; a.U = oU1; a.conv = conv;
+  stdic::BatchedArgs b{};
+  b.a = a;
+  b.f32 = d.f32; b.g32 = d.g32; b.dfdx32 = d.dfdx32; b.dfdy32 = d.dfdy32;
+  b.order = order; b.two_dof = 1; b.frames = 1; b.g_stride = 0; b.scratch = bscr;
+  // Subpb2: (U1, F1) -> U2
+  stdic::Subpb2Args s2{};
+  s2.coords = dcoords; s2.N = N; s2.elems = delems; s2.E = E; s2.dirichlet = ddir; s2.nd = nd;
+  s2.neumann = nullptr; s2.nn = 0; s2.gauss_order = 2; s2.beta = beta; s2.mu = mu; s2.alpha = 0.0;
+  s2.winstepsize = 1.0; s2.U = oU1; s2.F = F1; s2.tol = 1e-10; s2.maxit = 10000; s2.Uhat = oU2;
+
+  auto body = [&]() -> int {
+    int r = STDIC_OK;
+    if (batched) r = run_batched(c, b, N, cands, QueueKeys{nullptr, dwl, 0});
+    else r = check_launch(c, stdic::launch_icgn2_plain(a, c->stream), "Subpb1 plain");
+    if (!r) r = check_launch(c, stdic::launch_badpoints(conv, N, oU1, nullptr, 1, dsc, c->stream), "bad points");
+    if (!r) r = check_launch(c, stdic::launch_fill_nans(N, delems, E, ptr, list, oU1, tmp, c->stream), "NaN fill");
+    if (!r) {
+      const cudaError_t e = cudaMemcpyAsync(F1, oF2, 8 * n4, cudaMemcpyDeviceToDevice, c->stream);
+      if (e != cudaSuccess) r = cuda_fail(c, e, "FSubpb1");
+    }
+    if (!r) r = check_launch(c, stdic::launch_copy_marked(dmark, N, 2, oU2, oU1, c->stream), "hole copy");
+    if (!r) {
+      long long nl = 0;
+      const cudaError_t e = stdic::run_subpb2(s2, sws, dsc + 1, dres, dsc + 2, c->stream, &nl);
+      c->launches += nl;
+      if (e != cudaSuccess) r = cuda_fail(c, e, "Subpb2");
+    }
+    if (!r) r = check_launch(c, stdic::launch_nodal_strain(dcoords, N, delems, E, oU2, 2, ptr, list, oF2, c->stream),
+                             "nodal strain");
+    if (!r) r = check_launch(c, stdic::launch_copy_marked(dmark, N, 4, F1, oF2, c->stream), "hole copy");
+    if (!r) r = check_launch(c, stdic::launch_copy_marked(dmark, N, 2, oU1, oU2, c->stream), "hole copy");
+    if (!r) r = check_launch(c, stdic::launch_sub(oF2, F1, oud, (long long)n4, c->stream), "dual update");
+    if (!r) r = check_launch(c, stdic::launch_sub(oU2, oU1, ovd, (long long)n2, c->stream), "dual update");
+    return r;
+  };
+  auto record = [&](int step) -> int {
+    cudaError_t e = cudaMemcpyAsync(hbad + step, dsc, sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hit + step, dsc + 1, sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hst + step, dsc + 2, sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
+    return e == cudaSuccess ? STDIC_OK : cuda_fail(c, e, "ADMM history");
+  };
+
+  // the first iteration runs directly (it tunes the batched launch shape);
+  // the others replay one captured graph of the iteration
+  rc = body();
+  if (!rc) rc = record(0);
+  if (rc) return rc;
+  bool graphed = false;
+  cudaGraphExec_t exec = nullptr;
+  if (use_graph && steps > 1) {
+    cudaGraph_t graph = nullptr;
+    const long long l0 = c->launches;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      c->capturing = true;
+      const int r = body();
+      c->capturing = false;
+      e = cudaStreamEndCapture(c->stream, &graph);
+      if (r == STDIC_OK && e == cudaSuccess && graph)
+        e = cudaGraphInstantiate(&exec, graph, 0);
+      if (graph) cudaGraphDestroy(graph);
+      graphed = r == STDIC_OK && e == cudaSuccess && exec;
+    }
+    const long long per = c->launches - l0;
+    c->launches = l0;
+    if (!graphed) {
+      cudaGetLastError();
+      if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+    } else {
+      for (int step = 1; step < steps && !rc; ++step) {
+        e = cudaGraphLaunch(exec, c->stream);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "ADMM graph launch");
+        else { c->launches += per; rc = record(step); }
+      }
+      cudaGraphExecDestroy(exec);
+    }
+  }
+  if (!graphed)
+    for (int step = 1; step < steps && !rc; ++step) {
+      rc = body();
+      if (!rc) rc = record(step);
+    }
+  if (graph_used) *graph_used = graphed ? 1 : 0;
+  if (rc) return rc;
+  rc = pl.finish(c);
+  if (rc) return rc;
+  std::vector<int> st((size_t)steps);
+  cudaError_t e = cudaMemcpyAsync(st.data(), hst, sizeof(int) * steps, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "ADMM status");
+  for (int v : st) {
+    if (v == 2) return fail(c, STDIC_E_TIMEOUT, "ADMM: Subpb2 grid barrier wait gave up");
+    if (v == 3) return fail(c, STDIC_E_ARG, "ADMM: invalid node index or node in >16 elements");
+    if (v == 1) return fail(c, STDIC_E_NOTCONV, "ADMM: Subpb2 PCG did not reach the tolerance");
+  }
+  return STDIC_OK;
 }
 
 int stdic_subpb2(stdic_ctx* c, const double* coords, int N, const int32_t* elems, int E,

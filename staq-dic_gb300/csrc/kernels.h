@@ -149,6 +149,21 @@ struct AdjointArgs {
 };
 cudaError_t launch_adjoint(const AdjointArgs& a, cudaStream_t s, long long* launches);
 
+// Node -> element lists of a mesh (sorted per node), in ws of
+// topo_workspace_bytes(N, E); *ptr (N + 1) and *list point into ws.
+size_t topo_workspace_bytes(int N, int E);
+cudaError_t build_topology(const int32_t* elems, int E, int N, void* ws, int** ptr, int** list,
+                           cudaStream_t s);
+// F (4N) = nodal strain of U (2N); NaN at nodes in no element.
+cudaError_t launch_nodal_strain(const double* coords, int N, const int32_t* elems, int E, const double* U,
+                                int gauss_order, const int* ptr, const int* list, double* F, cudaStream_t s);
+// Fills the NaN nodes of U (2N) from their mesh neighbours; tmp holds 2N doubles.
+cudaError_t launch_fill_nans(int N, const int32_t* elems, int E, const int* ptr, const int* list, double* U,
+                             double* tmp, cudaStream_t s);
+cudaError_t launch_copy_marked(const uint8_t* mark, int N, int width, const double* src, double* dst,
+                               cudaStream_t s);
+cudaError_t launch_sub(const double* a, const double* b, double* out, long long n, cudaStream_t s);
+
 // Subpb2 (FEM).  All pointers are device pointers.
 struct Subpb2Args {
   const double* coords;

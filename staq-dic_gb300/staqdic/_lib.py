@@ -33,7 +33,8 @@ EXPORTS = [
     "stdic_kernel_launches", "stdic_last_solver_ms", "stdic_interp_bicubic", "stdic_img_gradient",
     "stdic_integer_search_grid", "stdic_integer_search", "stdic_icgn_subsets", "stdic_icgn_local",
     "stdic_subpb1_subsets", "stdic_subpb1", "stdic_subpb2", "stdic_subpb2_noalloc",
-    "stdic_icgn_adjoint", "stdic_icgn_subsets_frames",
+    "stdic_icgn_adjoint", "stdic_icgn_subsets_frames", "stdic_nodal_strain", "stdic_fill_nans",
+    "stdic_admm",
 ]
 
 
@@ -93,6 +94,11 @@ def load(build_if_missing=True):
     L.stdic_subpb2.argtypes = [_vp, _vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int,
                                _c.c_int, _c.c_double, _c.c_double, _vp, _vp, _c.c_double,
                                _c.c_double, _c.c_double, _c.c_int, _vp, _vp]
+    L.stdic_nodal_strain.argtypes = [_vp, _vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int, _vp]
+    L.stdic_fill_nans.argtypes = [_vp, _vp, _c.c_int, _vp, _c.c_int, _vp]
+    L.stdic_admm.argtypes = [_vp, _c.POINTER(Frame), _vp, _c.c_int, _vp, _c.c_int, _vp, _c.c_int, _vp, _vp,
+                             _c.c_double, _c.c_double, _c.c_double, _c.c_int, _c.c_int, _c.c_int, _vp, _vp,
+                             _vp, _vp, _vp, _vp, _vp, _vp]
     L.stdic_icgn_subsets_frames.argtypes = [_vp, _c.POINTER(Frame), _c.c_int, _vp, _vp, _c.c_int, _c.c_int,
                                             _vp, _c.c_double, _vp, _vp, _vp, _vp, _c.c_int]
     L.stdic_icgn_adjoint.argtypes = [_vp, _c.POINTER(Frame), _vp, _c.c_int, _c.c_int, _vp, _vp, _vp,

@@ -414,3 +414,61 @@ def icgn_subsets_frames(U0_list, coordinatesFEM, Df, ImgRef, ImgDef_list, winsiz
                                           _lib.STDIC_BATCHED_F32), "funICGNQuadtree (frames)")
     return ([U[2 * N * k:2 * N * (k + 1)] for k in range(P)], [F[4 * N * k:4 * N * (k + 1)] for k in range(P)],
             [conv[N * k:N * (k + 1)] for k in range(P)])
+
+
+def nodal_strain(coordinatesFEM, elementsFEM, U, GaussPtOrder=2, ctx=None):
+    """F (4N) = [du/dx dv/dx du/dy dv/dy] per node from the element Gauss-point
+    strains (stdic_nodal_strain)."""
+    c = _ctx(ctx)
+    b = _Bufs()
+    N = _nodes(coordinatesFEM)
+    E = int(np.asarray(elementsFEM).shape[0])
+    like = U if _is_torch(U) else None
+    F, pF = b.out(like, (4 * N,), np.float64)
+    c.check(c.L.stdic_nodal_strain(c.h, b.ptr(coordinatesFEM, np.float64), N, b.ptr(elementsFEM, np.int32), E,
+                                   b.ptr(U, np.float64), int(GaussPtOrder), pF), "nodal strain")
+    return F
+
+
+def fill_nans(coordinatesFEM, elementsFEM, U, ctx=None):
+    """U (2N) with its NaN nodes filled from their mesh neighbours (stdic_fill_nans)."""
+    c = _ctx(ctx)
+    b = _Bufs()
+    N = _nodes(coordinatesFEM)
+    E = int(np.asarray(elementsFEM).shape[0])
+    out = np.array(U, dtype=np.float64).ravel().copy()
+    c.check(c.L.stdic_fill_nans(c.h, b.ptr(coordinatesFEM, np.float64), N, b.ptr(elementsFEM, np.int32), E,
+                                out.ctypes.data), "NaN fill")
+    return out
+
+
+def admm(DICmesh, Df, ImgRef, ImgDef, winsize_List, U2, F2, udual, vdual, mu, beta, tol=1e-2, steps=2,
+         mark_hole=None, precision="batched", use_graph=True, ctx=None):
+    """ADMM iterations of the AL-DIC loop (stdic_admm).  Returns a dict with
+    U1, U2, F2, udual, vdual, badnum, pcg_iters and graph_used."""
+    c = _ctx(ctx)
+    prec = PRECISIONS[precision]
+    dtype = _data_dtype(prec, ImgRef)
+    b = _Bufs()
+    fr = _frame(b, Df, ImgRef, ImgDef, dtype)
+    coords = DICmesh["coordinatesFEM"]
+    elems = DICmesh["elementsFEM"]
+    dirichlet = DICmesh.get("dirichlet")
+    N = _nodes(coords)
+    E = int(np.asarray(elems).shape[0])
+    nd = 0 if dirichlet is None else int(np.asarray(dirichlet).size)
+    st = {k: np.array(v, dtype=np.float64).ravel().copy()
+          for k, v in (("U2", U2), ("F2", F2), ("udual", udual), ("vdual", vdual))}
+    U1 = np.empty(2 * N)
+    bad = np.zeros(steps, dtype=np.int32)
+    its = np.zeros(steps, dtype=np.int32)
+    used = _lib._c.c_int(0)
+    c.check(c.L.stdic_admm(c.h, _lib._c.byref(fr), b.ptr(coords, np.float64), N, b.ptr(elems, np.int32), E,
+                           b.ptr(dirichlet, np.int32) if nd else None, nd, b.ptr(winsize_List, np.int32),
+                           b.ptr(mark_hole, np.uint8) if mark_hole is not None else None, float(mu),
+                           float(beta), float(tol), int(steps), prec, 1 if use_graph else 0,
+                           st["U2"].ctypes.data, st["F2"].ctypes.data, st["udual"].ctypes.data,
+                           st["vdual"].ctypes.data, U1.ctypes.data, bad.ctypes.data, its.ctypes.data,
+                           _lib._c.byref(used)), "ADMM")
+    st.update(U1=U1, badnum=bad, pcg_iters=its, graph_used=bool(used.value))
+    return st

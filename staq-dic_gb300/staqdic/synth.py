@@ -348,22 +348,30 @@ def quadtree_mesh(W, H, winsize, winstepsize, size_fn, min_size, hole_fn=None):
     coords = np.asarray(coords, dtype=np.float64)
     elems = np.asarray(elems, dtype=np.int32)
     sizes = np.asarray(sizes)
-    # Dirichlet nodes: refined elements and elements on the ROI border, grown twice
+    return coords, elems, dirichlet_nodes(coords, elems, winstepsize), sizes
+
+
+def dirichlet_nodes(coords, elems, winstepsize, refined=True):
+    """markCoordHoleEdge (GenerateQuadtreeMesh.m:90-133): the nodes of the
+    elements on the ROI border and, with refined=True, of every element finer
+    than winstepsize, grown twice by element adjacency.  refined=False keeps
+    only the border band (the mesh then has free nodes in its refined part)."""
     xmin, xmax = coords[:, 0].min(), coords[:, 0].max()
     ymin, ymax = coords[:, 1].min(), coords[:, 1].max()
     c1 = coords[elems[:, 0] - 1]
     c3 = coords[elems[:, 2] - 1]
-    diag = np.hypot(c1[:, 0] - c3[:, 0], c1[:, 1] - c3[:, 1])
-    mark_e = (diag < 0.99 * math.sqrt(2) * winstepsize) | (c1[:, 0] < xmin + 1.01 * winstepsize) | \
-             (c3[:, 0] > xmax - 1.01 * winstepsize) | (c1[:, 1] < ymin + 1.01 * winstepsize) | \
-             (c3[:, 1] > ymax - 1.01 * winstepsize)
+    mark_e = (c1[:, 0] < xmin + 1.01 * winstepsize) | (c3[:, 0] > xmax - 1.01 * winstepsize) | \
+             (c1[:, 1] < ymin + 1.01 * winstepsize) | (c3[:, 1] > ymax - 1.01 * winstepsize)
+    if refined:
+        diag = np.hypot(c1[:, 0] - c3[:, 0], c1[:, 1] - c3[:, 1])
+        mark_e |= diag < 0.99 * math.sqrt(2) * winstepsize
     marked = np.unique(elems[mark_e])
     marked = marked[marked > 0]
     for _ in range(2):
         hit = np.isin(elems, marked).any(axis=1)
         marked = np.unique(elems[hit])
         marked = marked[marked > 0]
-    return coords, elems, marked.astype(np.int32), sizes
+    return marked.astype(np.int32)
 
 
 def node_sizes(coords, elems, sizes):

@@ -530,6 +530,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 2048^2 (C3) pass and the 4096^2 adjoint (C4) timing")
+    ap.add_argument("--only", choices=["c3", "admm", "adjoint", "c5"],
+                    help="run one secondary measurement alone and print it (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -556,6 +558,19 @@ def main():
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     L = ctx.L
+    if args.only:
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        if args.only == "admm":
+            res = measure_admm(ctx, torch, LocalRun(ctx, make_workload("hole2048")))
+        elif args.only == "c3":
+            res = measure_c3(ctx, torch, flush)
+        elif args.only == "adjoint":
+            res = measure_adjoint(ctx, torch)
+        else:
+            res = measure_c5(ctx, torch, flush)
+        print(json.dumps({"only": args.only, "result": res}), flush=True)
+        ctx.close()
+        return 0
     w = make_workload(args.workload)
     run = LocalRun(ctx, w)
     W, H, N, ws_list = run.W, run.H, run.N, run.ws_list

@@ -17,7 +17,7 @@
 // scatteredInterpolant (Subpb1Quadtree.m:193-259).  Here NaN nodes take, in
 // sweeps, the mean of their finite mesh neighbours of the previous sweep
 // (neighbours in increasing node order) until no NaN node has a finite
-// neighbour; one CTA runs all sweeps.
+// neighbour; the NaN nodes are listed first and one CTA sweeps the list.
 #include <algorithm>
 
 #include "device_common.cuh"
@@ -39,21 +39,7 @@ __global__ void k_topo_count(const int32_t* __restrict__ elems, int E, int N, in
 
 // exclusive scan of n ints (one CTA); out has n + 1 entries
 __global__ void __launch_bounds__(1024) k_topo_scan(const int* in, int* out, int n) {
-  __shared__ int part[1024];
-  const int per = (n + blockDim.x - 1) / blockDim.x;
-  const int b0 = threadIdx.x * per, b1 = min(n, b0 + per);
-  int s = 0;
-  for (int k = b0; k < b1; ++k) s += in[k];
-  part[threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int k = 0; k < (int)blockDim.x; ++k) { const int t = part[k]; part[k] = acc; acc += t; }
-  }
-  __syncthreads();
-  int acc = part[threadIdx.x];
-  for (int k = b0; k < b1; ++k) { const int t = in[k]; out[k] = acc; acc += t; }
-  if (threadIdx.x == blockDim.x - 1) out[n] = acc;
+  cta_exclusive_scan(in, out, n);
 }
 
 __global__ void k_topo_fill(const int32_t* __restrict__ elems, int E, int N, const int* ptr, int* cur,
@@ -135,58 +121,78 @@ __global__ void k_nodal_strain(const double* __restrict__ coords, int N, const i
   }
 }
 
-// NaN fill: all sweeps in one CTA (old/new buffers of 2N doubles)
+// NaN fill, step 1: the NaN nodes that lie in some element (the others have
+// no neighbour and stay NaN), in any order
+__global__ void k_nan_nodes(int N, const int* __restrict__ ptr, const double* __restrict__ U, int* cnt,
+                            int* nodes) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x)
+    if (isnan(U[2 * n]) && ptr[n + 1] > ptr[n]) nodes[atomicAdd(cnt, 1)] = n;
+}
+
+// the mean of the finite mesh neighbours of node n (sorted unique neighbour
+// order); false when none is finite
+STDIC_DEV bool neighbour_mean(int n, int N, const int32_t* __restrict__ elems, int E, const int* ptr,
+                              const int* list, const double* U, double* mu, double* mv) {
+  int cand[8 * kMaxElemPerNode];
+  int nc = 0;
+  const int a = ptr[n], b = min(ptr[n + 1], ptr[n] + kMaxElemPerNode);
+  for (int k = a; k < b; ++k) {
+    const int e = list[k];
+    for (int c = 0; c < 8; ++c) {
+      const int q = elems[(size_t)c * E + e];
+      if (q < 1 || q > N || q - 1 == n) continue;
+      const int val = q - 1;
+      bool dup = false;
+      for (int t = 0; t < nc && !dup; ++t) dup = cand[t] == val;
+      if (dup || nc >= 8 * kMaxElemPerNode) continue;
+      int j = nc - 1;
+      while (j >= 0 && cand[j] > val) { cand[j + 1] = cand[j]; --j; }
+      cand[j + 1] = val;
+      ++nc;
+    }
+  }
+  double su = 0, sv = 0;
+  int cnt = 0;
+  for (int t = 0; t < nc; ++t) {
+    const int m = cand[t];
+    if (!isnan(U[2 * m])) { su += U[2 * m]; sv += U[2 * m + 1]; ++cnt; }
+  }
+  if (!cnt) return false;
+  *mu = su / cnt;
+  *mv = sv / cnt;
+  return true;
+}
+
+// NaN fill, step 2: Jacobi sweeps over the listed nodes in one CTA.  A sweep
+// computes every still-NaN node's neighbour mean from the values before the
+// sweep, then writes them; sweeps stop when one fills nothing.
 __global__ void __launch_bounds__(1024) k_fill_nans(int N, const int32_t* __restrict__ elems, int E,
                                                     const int* ptr, const int* list, double* U,
-                                                    double* tmp) {
+                                                    const int* cnt, const int* __restrict__ nodes,
+                                                    double* vals) {
   __shared__ int changed;
-  double* old = U;
-  double* nw = tmp;
-  for (int sweep = 0; sweep <= N; ++sweep) {
+  const int m = *cnt;
+  for (int sweep = 0; sweep <= m; ++sweep) {
     if (threadIdx.x == 0) changed = 0;
     __syncthreads();
-    for (int n = threadIdx.x; n < N; n += blockDim.x) {
-      double u = old[2 * n], v = old[2 * n + 1];
-      if (isnan(u)) {
-        // sorted unique neighbours
-        int cand[8 * kMaxElemPerNode];
-        int nc = 0;
-        const int a = ptr[n], b = min(ptr[n + 1], ptr[n] + kMaxElemPerNode);
-        for (int k = a; k < b; ++k) {
-          const int e = list[k];
-          for (int c = 0; c < 8; ++c) {
-            const int q = elems[(size_t)c * E + e];
-            if (q < 1 || q > N || q - 1 == n) continue;
-            const int val = q - 1;
-            bool dup = false;
-            for (int t = 0; t < nc && !dup; ++t) dup = cand[t] == val;
-            if (dup || nc >= 8 * kMaxElemPerNode) continue;
-            int j = nc - 1;
-            while (j >= 0 && cand[j] > val) { cand[j + 1] = cand[j]; --j; }
-            cand[j + 1] = val;
-            ++nc;
-          }
-        }
-        double su = 0, sv = 0;
-        int cnt = 0;
-        for (int t = 0; t < nc; ++t) {
-          const int m = cand[t];
-          if (!isnan(old[2 * m])) { su += old[2 * m]; sv += old[2 * m + 1]; ++cnt; }
-        }
-        if (cnt) { u = su / cnt; v = sv / cnt; changed = 1; }
-      }
-      nw[2 * n] = u;
-      nw[2 * n + 1] = v;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      const int n = nodes[i];
+      double u = nan(""), v = nan("");
+      if (isnan(U[2 * n]) && neighbour_mean(n, N, elems, E, ptr, list, U, &u, &v)) changed = 1;
+      vals[2 * i] = u;
+      vals[2 * i + 1] = v;
     }
     __syncthreads();
     const int ch = changed;
-    double* t = old; old = nw; nw = t;
+    for (int i = threadIdx.x; i < m; i += blockDim.x)
+      if (!isnan(vals[2 * i])) {
+        const int n = nodes[i];
+        U[2 * n] = vals[2 * i];
+        U[2 * n + 1] = vals[2 * i + 1];
+      }
     __syncthreads();
     if (!ch) break;
   }
-  // the result is in `old`; bring it back to U when it sits in tmp
-  if (old != U)
-    for (int k = threadIdx.x; k < 2 * N; k += blockDim.x) U[k] = old[k];
 }
 
 // dst[k] = src[k] at the flagged nodes (width values per node)
@@ -240,10 +246,18 @@ cudaError_t launch_nodal_strain(const double* coords, int N, const int32_t* elem
   return cudaGetLastError();
 }
 
+size_t fill_tmp_doubles(int N) { return 2 * (size_t)N + ((size_t)N + 1) / 2 + 2; }
+
 cudaError_t launch_fill_nans(int N, const int32_t* elems, int E, const int* ptr, const int* list, double* U,
                              double* tmp, cudaStream_t s) {
   if (N <= 0) return cudaSuccess;
-  k_fill_nans<<<1, 1024, 0, s>>>(N, elems, E, ptr, list, U, tmp);
+  double* vals = tmp;
+  int* nodes = (int*)(tmp + 2 * (size_t)N);
+  int* cnt = nodes + N + 1;
+  cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  k_nan_nodes<<<grid_for(N, 256), 256, 0, s>>>(N, ptr, U, cnt, nodes);
+  k_fill_nans<<<1, 1024, 0, s>>>(N, elems, E, ptr, list, U, cnt, nodes, vals);
   return cudaGetLastError();
 }
 

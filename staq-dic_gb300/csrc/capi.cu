@@ -905,7 +905,7 @@ int stdic_fill_nans(stdic_ctx* c, const double* coords, int N, const int32_t* el
   pl.in(elems, 8 * (size_t)E, (int32_t**)&de);
   pl.in((const double*)U, 2 * (size_t)N, (double**)&uin);
   pl.out(U, 2 * (size_t)N, &uout);
-  pl.scratch(2 * (size_t)std::max(N, 1), &tmp);
+  pl.scratch(stdic::fill_tmp_doubles(std::max(N, 1)), &tmp);
   pl.scratch(stdic::topo_workspace_bytes(N, E), &tws);
   int rc = pl.commit(c);
   if (rc) return rc;
@@ -981,7 +981,7 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
   double *F1 = nullptr, *tmp = nullptr, *dres = nullptr;
   int32_t* conv = nullptr;
   pl.scratch(n4, &F1);
-  pl.scratch(n2, &tmp);
+  pl.scratch(stdic::fill_tmp_doubles(N), &tmp);
   pl.scratch(8, &dres);
   pl.scratch((size_t)N, &conv);
   unsigned char *tws = nullptr, *sws = nullptr, *bscr = nullptr;
@@ -1039,7 +1039,8 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
     if (!r) r = check_launch(c, stdic::launch_copy_marked(dmark, N, 2, oU2, oU1, c->stream), "hole copy");
     if (!r) {
       long long nl = 0;
-      const cudaError_t e = stdic::run_subpb2(s2, sws, dsc + 1, dres, dsc + 2, c->stream, &nl);
+      const cudaError_t e =
+          stdic::run_subpb2(s2, sws, dsc + 1, dres, dsc + 2, c->stream, &nl, stdic::kSubpb2Solve);
       c->launches += nl;
       if (e != cudaSuccess) r = cuda_fail(c, e, "Subpb2");
     }
@@ -1058,6 +1059,15 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
     return e == cudaSuccess ? STDIC_OK : cuda_fail(c, e, "ADMM history");
   };
 
+  // the Subpb2 structure (mesh graph, CSR pattern, Dirichlet flags) is the
+  // same in every iteration: built once here
+  {
+    long long nl = 0;
+    const cudaError_t e =
+        stdic::run_subpb2(s2, sws, dsc + 1, dres, dsc + 2, c->stream, &nl, stdic::kSubpb2Structure);
+    c->launches += nl;
+    if (e != cudaSuccess) return cuda_fail(c, e, "Subpb2 structure");
+  }
   // the first iteration runs directly (it tunes the batched launch shape);
   // the others replay one captured graph of the iteration
   rc = body();

@@ -9,6 +9,39 @@ namespace stdic {
 
 constexpr int kMaxIter = 100;  // maxIterNum of funICGNQuadtree.m:59
 
+// Exclusive prefix sum of n ints by one CTA of blockDim.x threads (a multiple
+// of 32, at most 1024): each thread sums a contiguous segment, the segment
+// sums are scanned with warp shuffles, then each thread writes its segment.
+// out has n + 1 entries (out[n] = total).
+STDIC_DEV void cta_exclusive_scan(const int* in, int* out, int n) {
+  __shared__ int warp_tot[32];
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int b0 = min(n, (int)threadIdx.x * per), b1 = min(n, b0 + per);
+  int s = 0;
+  for (int k = b0; k < b1; ++k) s += in[k];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int inc = s;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) warp_tot[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    int v = lane < nw ? warp_tot[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
+    }
+    if (lane < nw) warp_tot[lane] = v;  // inclusive warp totals
+  }
+  __syncthreads();
+  int acc = inc - s + (wid ? warp_tot[wid - 1] : 0);
+  for (int k = b0; k < b1; ++k) { const int t = in[k]; out[k] = acc; acc += t; }
+  if (threadIdx.x == blockDim.x - 1) out[n] = acc;
+}
+
 // ---------------------------------------------------------------------------
 // Keys cubic (a = -1/2) interpolation with clamp-to-edge borders, evaluated in
 // the exact operation order of ba_interp2.cpp:188-233 with every product and

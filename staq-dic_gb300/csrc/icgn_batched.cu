@@ -514,7 +514,6 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
   const int err_code = TWO ? 0 : -1;  // value the reference leaves on a run-time error
   int cntf = 0;
   float meanf = 0.f, bottomf = 0.f, sabs = 0.f;
-  double A11 = 0, A12 = 0, A22 = 0;
   int mx = 0, my = 0, npx = 0, sc = 0, sr = 0;
   int4 pstart = make_int4(0, 0, 0, 0);  // PixIter start of this thread for the tile
   float* tg = nullptr;
@@ -682,17 +681,27 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     sabs = st4[3];
     if constexpr (TWO) {
       tm.template sumf<3>(*reinterpret_cast<float(*)[3]>(hs), fscr);
-      const double b2 = (double)bottomf * (double)bottomf;
-      A11 = (double)hs[0] * 2 / b2 + a.mu;
-      A12 = (double)hs[1] * 2 / b2;
-      A22 = (double)hs[2] * 2 / b2 + a.mu;
-      // H2 + 1e-3 max(diag H2) I of funICGN_Subpb1.m:391-394, inverted once per change
-      const double dmax = isnan(A11) ? A22 : (isnan(A22) ? A11 : fmax(A11, A22));
-      double i00, i01, i10, i11;
-      solve2(A11 + 1e-3 * dmax, A12, A22 + 1e-3 * dmax, 1.0, 0.0, &i00, &i10);
-      solve2(A11 + 1e-3 * dmax, A12, A22 + 1e-3 * dmax, 0.0, 1.0, &i01, &i11);
-      split_f64(lane == 1 ? i10 : i00, ih[0], il[0]);
-      split_f64(lane == 1 ? i11 : i01, ih[1], il[1]);
+      // H2 + 1e-3 max(diag H2) I of funICGN_Subpb1.m:391-394, inverted in FP64
+      // by the two lanes that apply it (lane k holds row k)
+      if (lane < 2) {
+        const double s2 = 2.0 / ((double)bottomf * (double)bottomf);
+        const double A11 = (double)hs[0] * s2 + a.mu, A12 = (double)hs[1] * s2, A22 = (double)hs[2] * s2 + a.mu;
+        const double dmax = isnan(A11) ? A22 : (isnan(A22) ? A11 : fmax(A11, A22));
+        const double h11 = A11 + 1e-3 * dmax, h22 = A22 + 1e-3 * dmax;
+        const double det = h11 * h22 - A12 * A12;
+        double r0, r1;
+        if (h11 > 0 && h22 > 0 && det > 1e-8 * (h11 * h22)) {
+          // well-conditioned symmetric positive definite: the adjugate
+          const double rd = 1.0 / det;
+          r0 = (lane == 0 ? h22 : -A12) * rd;
+          r1 = (lane == 0 ? -A12 : h11) * rd;
+        } else {
+          // Cholesky or pivoted elimination of mldivide on e_lane
+          solve2(h11, A12, h22, lane == 0 ? 1.0 : 0.0, lane == 0 ? 0.0 : 1.0, &r0, &r1);
+        }
+        split_f64(r0, ih[0], il[0]);
+        split_f64(r1, ih[1], il[1]);
+      }
     } else {
       tm.template sumf<21>(hs, fscr);
       // packed lower (row-major) Hessian for the factor kernel and the output
@@ -909,9 +918,18 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         tm.sync();
       }
       if constexpr (TWO) {
-        bw = bwg;
-        f_side();
-        ibf = 1.f / bottomf;
+        // the f side depends on the tile and the selection only: it is kept
+        // while the selection equals the one it was last evaluated for, which
+        // bwf holds (bw nullptr: every pixel)
+        int diff = 0;
+        for (int p = tm.tl; p < npx; p += tm.TT) diff |= bwg[p] != (bw ? bw[p] : 1);
+        if (tm.any(diff, iscr)) {
+          for (int p = tm.tl; p < npx; p += tm.TT) bwf[p] = bwg[p];
+          tm.sync();
+          bw = bwf;
+          f_side();
+          ibf = 1.f / bottomf;
+        }
       }
       if constexpr (!TWO) {
         // The g tile restricted to its selection.  J depends only on the fixed

@@ -157,7 +157,9 @@ cudaError_t build_topology(const int32_t* elems, int E, int N, void* ws, int** p
 // F (4N) = nodal strain of U (2N); NaN at nodes in no element.
 cudaError_t launch_nodal_strain(const double* coords, int N, const int32_t* elems, int E, const double* U,
                                 int gauss_order, const int* ptr, const int* list, double* F, cudaStream_t s);
-// Fills the NaN nodes of U (2N) from their mesh neighbours; tmp holds 2N doubles.
+// Fills the NaN nodes of U (2N) from their mesh neighbours; tmp holds
+// fill_tmp_doubles(N) doubles.
+size_t fill_tmp_doubles(int N);
 cudaError_t launch_fill_nans(int N, const int32_t* elems, int E, const int* ptr, const int* list, double* U,
                              double* tmp, cudaStream_t s);
 cudaError_t launch_copy_marked(const uint8_t* mark, int N, int width, const double* src, double* dst,
@@ -184,7 +186,13 @@ struct Subpb2Args {
 };
 // workspace: caller-provided device memory of subpb2_workspace_bytes(N, E)
 size_t subpb2_workspace_bytes(int N, int E);
+// phase: kSubpb2Structure builds the node graph, CSR pattern, Dirichlet flags
+// and reference-element tables in the workspace; kSubpb2Solve assembles the
+// values for a.U and a.F on that structure and runs the PCG.  A solve-only call
+// needs an earlier structure call on the same workspace, mesh, Dirichlet set
+// and Gauss order.
+constexpr int kSubpb2Structure = 1, kSubpb2Solve = 2, kSubpb2All = 3;
 cudaError_t run_subpb2(const Subpb2Args& a, void* workspace, int* iters_dev, double* resid_dev,
-                       int* status_dev, cudaStream_t s, long long* launches);
+                       int* status_dev, cudaStream_t s, long long* launches, int phase = kSubpb2All);
 
 }  // namespace stdic

@@ -23,6 +23,8 @@ namespace {
 
 constexpr int kMaxElemPerNode = 16;
 constexpr long long kSpinLimit = 1ll << 24;  // bounded grid-barrier wait
+// per hanging-node pattern: Sxx, Syy, M (8x8 each), Gx, Gy (8 each)
+constexpr int kTabStride = 3 * 64 + 16;
 
 struct Ws {  // carved from the caller's workspace
   int* deg;        // N+1
@@ -44,6 +46,7 @@ struct Ws {  // carved from the caller's workspace
   uint8_t* dirn;   // N
   int* misc;       // 16 ints: [0] any zero entry, [1] min node, [2] barrier count, [3] barrier gen
   double* part;    // partial sums: 10 slots x 1024 blocks (one region per CG phase)
+  double* tab;     // reference-element tables: 16 hanging patterns x kTabStride
 };
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -75,6 +78,7 @@ Ws carve(void* base, int N, int E, size_t* total) {
   w.dirn = (uint8_t*)take(N);
   w.misc = (int*)take(sizeof(int) * 16);
   w.part = (double*)take(sizeof(double) * 10 * 1024);
+  w.tab = (double*)take(sizeof(double) * 16 * kTabStride);
   if (total) *total = o;
   return w;
 }
@@ -103,21 +107,7 @@ __global__ void k_degree(Subpb2Args a, Ws w) {
 
 // exclusive scan of n+1 ints in one CTA (n up to a few million)
 __global__ void __launch_bounds__(1024) k_scan(const int* in, int* out, int n) {
-  __shared__ int part[1024];
-  const int per = (n + blockDim.x - 1) / blockDim.x;
-  const int b0 = threadIdx.x * per, b1 = min(n, b0 + per);
-  int s = 0;
-  for (int k = b0; k < b1; ++k) s += in[k];
-  part[threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int k = 0; k < (int)blockDim.x; ++k) { const int t = part[k]; part[k] = acc; acc += t; }
-  }
-  __syncthreads();
-  int acc = part[threadIdx.x];
-  for (int k = b0; k < b1; ++k) { const int t = in[k]; out[k] = acc; acc += t; }
-  if (threadIdx.x == blockDim.x - 1) out[n] = acc;
+  cta_exclusive_scan(in, out, n);
 }
 
 __global__ void k_fill_elist(Subpb2Args a, Ws w) {
@@ -170,10 +160,6 @@ __global__ void k_rowlen(Subpb2Args a, Ws w) {
 __global__ void k_fill_cols(Subpb2Args a, Ws w) {
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < a.N; n += gridDim.x * blockDim.x) {
     neighbours(a, w, n, w.col + w.rowptr[n]);
-    for (int k = w.rowptr[n]; k < w.rowptr[n + 1]; ++k) w.val[k] = 0.0;
-    w.diag[n] = 0.0;
-    w.b[n] = 0.0;
-    w.b[a.N + n] = 0.0;
   }
 }
 
@@ -189,79 +175,160 @@ STDIC_DEV int find_col(const Ws& w, int row, int c) {
   return -1;
 }
 
-__global__ void k_element(Subpb2Args a, Ws w) {
+// Reference-square integrals of each hanging-node pattern (bit c of the
+// pattern: hanging node 5 + c present), over the Gauss rule of the call:
+//   Sxx_pq = sum w dN_p/dksi dN_q/dksi,  Syy_pq = sum w dN_p/deta dN_q/deta,
+//   M_pq = sum w N_p N_q,  Gx_p = sum w dN_p/dksi,  Gy_p = sum w dN_p/deta.
+// An axis-aligned rectangle with edges hx = x2 - x1, hy = y4 - y1 (and any
+// hanging node at its edge midpoint) has the constant Jacobian diag(hx, hy)/2,
+// so its element integrals are these tables scaled by hx and hy.
+__global__ void k_ref_tables(int gauss_order, Ws w) {
+  const int pat = blockIdx.x, p = threadIdx.x >> 3, q = threadIdx.x & 7;
   double gpt[5], gwt[5];
-  const int ng = gauss_rule(a.gauss_order, gpt, gwt);
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.E; e += gridDim.x * blockDim.x) {
+  const int ng = gauss_rule(gauss_order, gpt, gwt);
+  double dp[4];
+  for (int c = 0; c < 4; ++c) dp[c] = (pat >> c) & 1 ? 1.0 : 0.0;
+  double sxx = 0, syy = 0, m = 0, gx = 0, gy = 0;
+  for (int gi = 0; gi < ng * ng; ++gi) {
+    const double ksi = gpt[gi % ng], eta = gpt[gi / ng];
+    const double wgt = gwt[gi % ng] * gwt[gi / ng];
+    double Nv[8], dk[8], de[8];
+    shape(ksi, eta, dp, Nv, dk, de);
+    double np = 0, nq = 0, kp = 0, kq = 0, ep = 0, eq = 0;
+    for (int c = 0; c < 8; ++c) {
+      if (c == p) { np = Nv[c]; kp = dk[c]; ep = de[c]; }
+      if (c == q) { nq = Nv[c]; kq = dk[c]; eq = de[c]; }
+    }
+    sxx += wgt * kp * kq;
+    syy += wgt * ep * eq;
+    m += wgt * np * nq;
+    gx += wgt * kp;
+    gy += wgt * ep;
+  }
+  double* t = w.tab + pat * kTabStride;
+  t[p * 8 + q] = sxx;
+  t[64 + p * 8 + q] = syy;
+  t[128 + p * 8 + q] = m;
+  if (q == 0) { t[192 + p] = gx; t[200 + p] = gy; }
+}
+
+// Element integration, eight lanes per element: lane p assembles row p of the
+// element matrix and right-hand side.  Rectangles take the reference tables;
+// any other element integrates its Gauss points directly.
+__global__ void __launch_bounds__(256) k_element(Subpb2Args a, Ws w) {
+  const int p = threadIdx.x & 7;
+  const long long g0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const long long gs = ((long long)gridDim.x * blockDim.x) >> 3;
+  for (long long e = g0; e < a.E; e += gs) {
     int nd[8];
     double px[8], py[8], dp[4];
+    bool corners = true;
     for (int c = 0; c < 8; ++c) {
       nd[c] = a.elems[(size_t)c * a.E + e];
       const bool ok = nd[c] >= 1 && nd[c] <= a.N;
+      if (c < 4) corners &= ok;
       px[c] = ok ? a.coords[nd[c] - 1] : 0.0;
       py[c] = ok ? a.coords[a.N + nd[c] - 1] : 0.0;
     }
-    for (int c = 0; c < 4; ++c) dp[c] = nd[4 + c] != 0 ? 1.0 : 0.0;
-    double K[8][8], bu[8], bv[8];
-    for (int p = 0; p < 8; ++p) {
-      bu[p] = bv[p] = 0;
-      for (int q = 0; q < 8; ++q) K[p][q] = 0;
+    int pat = 0;
+    for (int c = 0; c < 4; ++c) {
+      dp[c] = nd[4 + c] != 0 ? 1.0 : 0.0;
+      pat |= nd[4 + c] != 0 ? 1 << c : 0;
     }
-    double Uu[8], Uv[8], F11[8], F21[8], F12[8], F22[8];
+    const double hx = px[1] - px[0], hy = py[3] - py[0];
+    bool rect = corners && py[1] == py[0] && px[2] == px[1] && py[2] == py[3] && px[3] == px[0] && hx != 0 &&
+                hy != 0;
+    // hanging nodes at their edge midpoints: 5 on 2-3, 6 on 3-4, 7 on 4-1, 8 on 1-2
+    const int ea[4] = {1, 2, 3, 0}, eb[4] = {2, 3, 0, 1};
+    for (int c = 0; c < 4; ++c)
+      if (nd[4 + c] != 0)
+        rect &= nd[4 + c] >= 1 && nd[4 + c] <= a.N && px[4 + c] == 0.5 * (px[ea[c]] + px[eb[c]]) &&
+                py[4 + c] == 0.5 * (py[ea[c]] + py[eb[c]]);
+    const bool okp = nd[p] >= 1 && nd[p] <= a.N;
+    double Uu[8], Uv[8];
     for (int c = 0; c < 8; ++c) {
       const bool ok = nd[c] >= 1 && nd[c] <= a.N;
-      const int n0 = nd[c] - 1;
-      Uu[c] = ok ? a.U[2 * n0] : 0.0;
-      Uv[c] = ok ? a.U[2 * n0 + 1] : 0.0;
-      F11[c] = ok ? a.F[4 * n0] : 0.0;
-      F21[c] = ok ? a.F[4 * n0 + 1] : 0.0;
-      F12[c] = ok ? a.F[4 * n0 + 2] : 0.0;
-      F22[c] = ok ? a.F[4 * n0 + 3] : 0.0;
+      Uu[c] = ok ? a.U[2 * (nd[c] - 1)] : 0.0;
+      Uv[c] = ok ? a.U[2 * (nd[c] - 1) + 1] : 0.0;
     }
-    for (int gi = 0; gi < ng * ng; ++gi) {
-      const double ksi = gpt[gi % ng], eta = gpt[gi / ng];
-      const double wgt = gwt[gi % ng] * gwt[gi / ng];
-      double Nv[8], dk[8], de[8];
-      shape(ksi, eta, dp, Nv, dk, de);
-      double J11 = 0, J12 = 0, J21 = 0, J22 = 0;
-      for (int c = 0; c < 8; ++c) {
-        J11 += dk[c] * px[c]; J12 += dk[c] * py[c];
-        J21 += de[c] * px[c]; J22 += de[c] * py[c];
+    double F11 = 0, F21 = 0, F12 = 0, F22 = 0;
+    if (okp) {
+      const double* Fp = a.F + 4 * (size_t)(nd[p] - 1);
+      F11 = Fp[0]; F21 = Fp[1]; F12 = Fp[2]; F22 = Fp[3];
+    }
+    double Kr[8], bu = 0, bv = 0;
+    if (rect) {
+      const double* t = w.tab + pat * kTabStride;
+      const double ryx = hy / hx, rxy = hx / hy, cm = a.mu * (0.25 * hx * hy), cs = a.beta + a.alpha;
+      for (int q = 0; q < 8; ++q) {
+        const double sd = ryx * t[p * 8 + q] + rxy * t[64 + p * 8 + q];
+        const double mm = cm * t[128 + p * 8 + q];
+        Kr[q] = cs * sd + mm;
+        const double r = mm + a.alpha * sd;
+        bu += r * Uu[q];
+        bv += r * Uv[q];
       }
-      const double Jac = J11 * J22 - J12 * J21;
-      const double i11 = 1 / Jac * J22, i12 = 1 / Jac * (-J12), i21 = 1 / Jac * (-J21),
-                   i22 = 1 / Jac * J11;
-      double gx[8], gy[8];
-      for (int c = 0; c < 8; ++c) {
-        gx[c] = i11 * dk[c] + i12 * de[c];
-        gy[c] = i21 * dk[c] + i22 * de[c];
-      }
-      const double wj = Jac * wgt;
-      for (int p = 0; p < 8; ++p) {
+      const double gxp = 0.5 * hy * t[192 + p], gyp = 0.5 * hx * t[200 + p];
+      bu += a.beta * (gxp * F11 + gyp * F12);
+      bv += a.beta * (gxp * F21 + gyp * F22);
+    } else {
+      double gpt[5], gwt[5];
+      const int ng = gauss_rule(a.gauss_order, gpt, gwt);
+      for (int q = 0; q < 8; ++q) Kr[q] = 0;
+      for (int gi = 0; gi < ng * ng; ++gi) {
+        const double ksi = gpt[gi % ng], eta = gpt[gi / ng];
+        const double wgt = gwt[gi % ng] * gwt[gi / ng];
+        double Nv[8], dk[8], de[8];
+        shape(ksi, eta, dp, Nv, dk, de);
+        double J11 = 0, J12 = 0, J21 = 0, J22 = 0;
+        for (int c = 0; c < 8; ++c) {
+          J11 += dk[c] * px[c]; J12 += dk[c] * py[c];
+          J21 += de[c] * px[c]; J22 += de[c] * py[c];
+        }
+        const double Jac = J11 * J22 - J12 * J21;
+        const double i11 = 1 / Jac * J22, i12 = 1 / Jac * (-J12), i21 = 1 / Jac * (-J21),
+                     i22 = 1 / Jac * J11;
+        double gx[8], gy[8], gxp = 0, gyp = 0, np = 0;
+        for (int c = 0; c < 8; ++c) {
+          gx[c] = i11 * dk[c] + i12 * de[c];
+          gy[c] = i21 * dk[c] + i22 * de[c];
+          if (c == p) { gxp = gx[c]; gyp = gy[c]; np = Nv[c]; }
+        }
+        const double wj = Jac * wgt;
         double nnu = 0, nnv = 0, ddu = 0, ddv = 0;
         for (int q = 0; q < 8; ++q) {
-          const double dd = gx[p] * gx[q] + gy[p] * gy[q];
-          const double nn = Nv[p] * Nv[q];
-          K[p][q] += wj * ((a.beta + a.alpha) * dd + a.mu * nn);
+          const double dd = gxp * gx[q] + gyp * gy[q];
+          const double nn = np * Nv[q];
+          Kr[q] += wj * ((a.beta + a.alpha) * dd + a.mu * nn);
           nnu += nn * Uu[q]; nnv += nn * Uv[q];
           ddu += dd * Uu[q]; ddv += dd * Uv[q];
         }
-        bu[p] += wj * (a.beta * (gx[p] * F11[p] + gy[p] * F12[p]) + a.mu * nnu + a.alpha * ddu);
-        bv[p] += wj * (a.beta * (gx[p] * F21[p] + gy[p] * F22[p]) + a.mu * nnv + a.alpha * ddv);
+        bu += wj * (a.beta * (gxp * F11 + gyp * F12) + a.mu * nnu + a.alpha * ddu);
+        bv += wj * (a.beta * (gxp * F21 + gyp * F22) + a.mu * nnv + a.alpha * ddv);
       }
     }
-    for (int p = 0; p < 8; ++p) {
-      if (nd[p] < 1 || nd[p] > a.N) continue;
-      const int row = nd[p] - 1;
-      atomicAdd(&w.b[row], bu[p]);
-      atomicAdd(&w.b[a.N + row], bv[p]);
-      for (int q = 0; q < 8; ++q) {
-        if (nd[q] < 1 || nd[q] > a.N) continue;
-        const int k = find_col(w, row, nd[q] - 1);
-        if (k >= 0) atomicAdd(&w.val[k], K[p][q]);
-        if (nd[q] == nd[p]) atomicAdd(&w.diag[row], K[p][q]);
-      }
+    if (!okp) continue;
+    const int row = nd[p] - 1;
+    atomicAdd(&w.b[row], bu);
+    atomicAdd(&w.b[a.N + row], bv);
+    for (int q = 0; q < 8; ++q) {
+      if (nd[q] < 1 || nd[q] > a.N) continue;
+      const int k = find_col(w, row, nd[q] - 1);
+      if (k >= 0) atomicAdd(&w.val[k], Kr[q]);
+      if (nd[q] == nd[p]) atomicAdd(&w.diag[row], Kr[q]);
     }
+  }
+}
+
+// zero the matrix values, diagonal and right-hand sides of an assembled structure
+__global__ void k_zero_values(Subpb2Args a, Ws w) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) w.misc[2] = 0;  // grid-barrier count
+  const int nnz = w.rowptr[a.N];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += gridDim.x * blockDim.x) w.val[k] = 0.0;
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < a.N; n += gridDim.x * blockDim.x) {
+    w.diag[n] = 0.0;
+    w.b[n] = 0.0;
+    w.b[a.N + n] = 0.0;
   }
 }
 
@@ -503,23 +570,33 @@ size_t subpb2_workspace_bytes(int N, int E) {
 }
 
 cudaError_t run_subpb2(const Subpb2Args& a, void* workspace, int* iters_dev, double* resid_dev,
-                       int* status_dev, cudaStream_t s, long long* launches) {
+                       int* status_dev, cudaStream_t s, long long* launches, int phase) {
   if (a.N <= 0) return cudaSuccess;
   Ws w = carve(workspace, a.N, a.E, nullptr);
   const int T = 256;
   auto blocks = [&](long long n) { return (int)std::min<long long>((n + T - 1) / T, 152 * 8); };
   long long nl = 0;
+  if (phase & kSubpb2Structure) {
+    // node graph, CSR pattern, Dirichlet flags and reference tables: they
+    // depend on the mesh, the Dirichlet set and the Gauss order only
+    k_init<<<blocks(a.N + 1), T, 0, s>>>(w, a.N); ++nl;
+    if (a.E > 0) { k_degree<<<blocks(a.E), T, 0, s>>>(a, w); ++nl; }
+    k_scan<<<1, 1024, 0, s>>>(w.deg, w.eptr, a.N); ++nl;
+    if (a.E > 0) { k_fill_elist<<<blocks(a.E), T, 0, s>>>(a, w); ++nl; }
+    k_rowlen<<<blocks(a.N), T, 0, s>>>(a, w); ++nl;
+    k_scan<<<1, 1024, 0, s>>>(w.rowlen, w.rowptr, a.N); ++nl;
+    k_fill_cols<<<blocks(a.N), T, 0, s>>>(a, w); ++nl;
+    if (a.nd > 0) { k_dirichlet<<<blocks(a.nd), T, 0, s>>>(a, w); ++nl; }
+    k_ref_tables<<<16, 64, 0, s>>>(a.gauss_order, w); ++nl;
+  }
+  if (!(phase & kSubpb2Solve)) {
+    if (launches) *launches += nl;
+    return cudaGetLastError();
+  }
   cudaMemsetAsync(status_dev, 0, sizeof(int), s);
-  k_init<<<blocks(a.N + 1), T, 0, s>>>(w, a.N); ++nl;
-  if (a.E > 0) { k_degree<<<blocks(a.E), T, 0, s>>>(a, w); ++nl; }
-  k_scan<<<1, 1024, 0, s>>>(w.deg, w.eptr, a.N); ++nl;
-  if (a.E > 0) { k_fill_elist<<<blocks(a.E), T, 0, s>>>(a, w); ++nl; }
-  k_rowlen<<<blocks(a.N), T, 0, s>>>(a, w); ++nl;
-  k_scan<<<1, 1024, 0, s>>>(w.rowlen, w.rowptr, a.N); ++nl;
-  k_fill_cols<<<blocks(a.N), T, 0, s>>>(a, w); ++nl;
-  if (a.E > 0) { k_element<<<blocks(a.E), T, 0, s>>>(a, w); ++nl; }
+  k_zero_values<<<blocks(64ll * a.E > a.N ? 64ll * a.E : a.N), T, 0, s>>>(a, w); ++nl;
+  if (a.E > 0) { k_element<<<blocks(8ll * a.E), T, 0, s>>>(a, w); ++nl; }
   if (a.nn > 0) { k_neumann<<<blocks(a.nn), T, 0, s>>>(a, w); ++nl; }
-  if (a.nd > 0) { k_dirichlet<<<blocks(a.nd), T, 0, s>>>(a, w); ++nl; }
   k_free_and_lift<<<blocks(a.N), T, 0, s>>>(a, w); ++nl;
   k_lift_rhs<<<blocks(a.N), T, 0, s>>>(a, w); ++nl;
   cudaError_t e = cudaGetLastError();

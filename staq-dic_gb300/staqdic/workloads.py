@@ -78,13 +78,16 @@ def _hole_case(name, seed, W, a, eps, scale_sizes=1.0):
     s = scale_sizes
     hmin = 4.0
 
+    # element size by distance from the hole edge: 4 px in a band of 75 px per
+    # 1024 px of image, 8 px to 0.35 W, 16 px to 0.46 W, 32 px beyond (about
+    # 20k nodes at 1024^2 and 80k at 2048^2, subsets of 8-64 px)
     def size_fn(x, y):
         d = abs(math.hypot(x - centre[0], y - centre[1]) - a)
-        if d < 40 * s:
+        if d < 75 * s:
             return 4.0
-        if d < 0.3 * W:
+        if d < 0.35 * W:
             return 8.0
-        if d < 0.4 * W:
+        if d < 0.46 * W:
             return 16.0
         return 32.0
 
@@ -109,7 +112,7 @@ def hole1024(seed=1, size=1024):
 
 
 def hole2048(seed=2, size=2048):
-    return _hole_case("hole2048", seed, size, 300.0 * size / 2048, 0.02, size / 2048)
+    return _hole_case("hole2048", seed, size, 300.0 * size / 2048, 0.02, size / 1024)
 
 
 def bumps4096(seed=3, size=4096):
@@ -144,9 +147,11 @@ def series1024(seed=4, size=1024, pairs=16):
     fN = np.asfortranarray((synth.normalize(f) * maskf).astype(np.float32))
     gs, Us, ufuns = [], [], []
 
+    # element size by distance from the crack: 4 px within 170 px, 8 px to
+    # 500 px, 16 px to 640 px, 32 px beyond (per 1024 px; about 25k nodes)
     def size_fn(x, y):
-        d = abs(y - cy) if x < cxm + 40 else math.hypot(x - cxm, y - cy)
-        return 4.0 if d < 24 else (8.0 if d < 0.4 * W else 16.0)
+        d = (abs(y - cy) if x < cxm + 40 else math.hypot(x - cxm, y - cy)) * 1024.0 / W
+        return 4.0 if d < 170 else (8.0 if d < 500 else (16.0 if d < 640 else 32.0))
 
     st = 32
     coords, elems, dirichlet, sizes = synth.quadtree_mesh(W, H, 64, st, size_fn, 4.0, None)

@@ -814,11 +814,15 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     const float dx0 = (float)(int)(x1 - x0), dy0 = (float)(int)(y1 - y0);
     const float shift = meanf;  // one-pass variance around meanf
     // one pass: interpolation, zero/NaN counts, g statistics and sum J g
-    constexpr int NR = 7 + 2 * NQ;
+    // zero count, NaN flag, compensated sum g and sum g^2, count, sum J g
+    constexpr int NR = 7 + NQ;
     float red[NR];
     {
       int zg = 0, nang = 0;
-      Kahan sg, qg, kg[NQ];
+      Kahan sg, qg;
+      float kg[NQ];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) kg[k] = 0.f;
       float ng = 0.f;
       PixIter it(pstart, mx);
       auto one = [&](int p, int i, int j, float t) {
@@ -834,7 +838,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         float J[NQ];
         jac(i, j, bw ? (float)bw[p] : 1.f, J);
 #pragma unroll
-        for (int k = 0; k < NQ; ++k) kg[k].add(J[k] * t);
+        for (int k = 0; k < NQ; ++k) kg[k] = fmaf(J[k], t, kg[k]);
       };
       // Stage the warped footprint of g in shared memory when it fits: the
       // tap range follows from the four corners (the warp is affine), with a
@@ -897,7 +901,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
       red[0] = (float)zg; red[1] = (float)nang;
       red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
 #pragma unroll
-      for (int k = 0; k < NQ; ++k) { red[7 + 2 * k] = kg[k].s; red[8 + 2 * k] = -kg[k].c; }
+      for (int k = 0; k < NQ; ++k) red[7 + k] = kg[k];
     }
     tm.template sumf<NR>(red, fscr);
     if (red[1] > 0.f) { err = true; break; }
@@ -936,7 +940,10 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         // f selection here, so the sums of the first pass stay valid for the
         // kept pixels: only the removed pixels' parts are summed and taken off.
         int cnt = 0, rem = 0;
-        Kahan rsg, rqg, rkg[NQ];
+        Kahan rsg, rqg;
+        float rkg[NQ];
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) rkg[k] = 0.f;
         float rng = 0.f;
         PixIter it(pstart, mx);
         for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
@@ -956,7 +963,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
               float J[NQ];
               jac(it.i, it.j, bw ? (float)bw[p] : 1.f, J);
 #pragma unroll
-              for (int k = 0; k < NQ; ++k) rkg[k].add(J[k] * t);
+              for (int k = 0; k < NQ; ++k) rkg[k] = fmaf(J[k], t, rkg[k]);
             }
           }
         }
@@ -966,7 +973,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
           rr[0] = 0.f; rr[1] = 0.f;
           rr[2] = rsg.s; rr[3] = -rsg.c; rr[4] = rqg.s; rr[5] = -rqg.c; rr[6] = rng;
 #pragma unroll
-          for (int k = 0; k < NQ; ++k) { rr[7 + 2 * k] = rkg[k].s; rr[8 + 2 * k] = -rkg[k].c; }
+          for (int k = 0; k < NQ; ++k) rr[7 + k] = rkg[k];
           tm.template sumf<NR>(rr, fscr);
 #pragma unroll
           for (int k = 2; k < NR; ++k) red[k] -= rr[k];
@@ -976,7 +983,10 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         // the g tile restricted to its selection, and its sums again (the f
         // selection, and with it J, follows the g selection in this form)
         int cnt = 0;
-        Kahan sg, qg, kg[NQ];
+        Kahan sg, qg;
+        float kg[NQ];
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) kg[k] = 0.f;
         float ng = 0.f;
         PixIter it(pstart, mx);
         for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
@@ -992,12 +1002,12 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
           float J[NQ];
           jac(it.i, it.j, bw ? (float)bw[p] : 1.f, J);
 #pragma unroll
-          for (int k = 0; k < NQ; ++k) kg[k].add(J[k] * t);
+          for (int k = 0; k < NQ; ++k) kg[k] = fmaf(J[k], t, kg[k]);
         }
         red[0] = (float)cnt; red[1] = 0.f;
         red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
 #pragma unroll
-        for (int k = 0; k < NQ; ++k) { red[7 + 2 * k] = kg[k].s; red[8 + 2 * k] = -kg[k].c; }
+        for (int k = 0; k < NQ; ++k) red[7 + k] = kg[k];
         tm.template sumf<NR>(red, fscr);
         cg = (int)red[0];
       }
@@ -1022,7 +1032,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     float b2[NQ];
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
-      const float jg = red[7 + 2 * k] + red[8 + 2 * k];
+      const float jg = red[7 + k];
       b2[k] = jf[k] * ibf - (jg - meang * j1[k]) * ibg;
     }
     // convergence test (FP32) and the update, identical on every lane

@@ -13,10 +13,11 @@
 // occupancy is set by registers, not by the largest subset of the batch.
 //
 // Precision: warped positions are an integer base plus an FP32 offset;
-// bicubic weights, interpolation and residuals are FP32.  Per-lane sums are
-// Kahan-compensated FP32 (b-vector and g statistics; the g variance is a
-// one-pass shifted sum around meanf), reduced across lanes in FP32 together
-// with their compensations; the Hessian is accumulated in plain FP32 (it only
+// bicubic weights, interpolation and residuals are FP32.  The per-iteration
+// sums (sum J g for the b-vector; the g statistics as one-pass sums shifted by
+// meanf, so that the variance does not cancel) are per-lane FP32 FMA chains
+// reduced across lanes in FP32; the set-up's f statistics and b-vector parts
+// are Kahan-compensated; the Hessian is accumulated in plain FP32 (it only
 // scales the step, never the converged point).  The 6x6 Hessian is reduced,
 // factorised (Cholesky, else LU with partial pivoting) and inverted in FP64
 // once per subset; every iteration applies that FP64 inverse to the FP32
@@ -814,12 +815,12 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     const float dx0 = (float)(int)(x1 - x0), dy0 = (float)(int)(y1 - y0);
     const float shift = meanf;  // one-pass variance around meanf
     // one pass: interpolation, zero/NaN counts, g statistics and sum J g
-    // zero count, NaN flag, compensated sum g and sum g^2, count, sum J g
-    constexpr int NR = 7 + NQ;
+    // zero count, NaN flag, sum g and sum g^2 (shifted), count, sum J g
+    constexpr int NR = 5 + NQ;
     float red[NR];
     {
       int zg = 0, nang = 0;
-      Kahan sg, qg;
+      float sg = 0.f, qg = 0.f;
       float kg[NQ];
 #pragma unroll
       for (int k = 0; k < NQ; ++k) kg[k] = 0.f;
@@ -831,8 +832,8 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         if (t == 0.f) ++zg;
         if (fabsf(t) > 1e-10f) {
           const float d = t - shift;
-          sg.add(d);
-          qg.add(d * d);
+          sg += d;
+          qg = fmaf(d, d, qg);
           ng += 1.f;
         }
         float J[NQ];
@@ -899,9 +900,9 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         one(p, it.i, it.j, t);
       }
       red[0] = (float)zg; red[1] = (float)nang;
-      red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
+      red[2] = sg; red[3] = qg; red[4] = ng;
 #pragma unroll
-      for (int k = 0; k < NQ; ++k) red[7 + k] = kg[k];
+      for (int k = 0; k < NQ; ++k) red[5 + k] = kg[k];
     }
     tm.template sumf<NR>(red, fscr);
     if (red[1] > 0.f) { err = true; break; }
@@ -940,7 +941,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         // f selection here, so the sums of the first pass stay valid for the
         // kept pixels: only the removed pixels' parts are summed and taken off.
         int cnt = 0, rem = 0;
-        Kahan rsg, rqg;
+        float rsg = 0.f, rqg = 0.f;
         float rkg[NQ];
 #pragma unroll
         for (int k = 0; k < NQ; ++k) rkg[k] = 0.f;
@@ -956,8 +957,8 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
               tg[p] = 0.f;
               if (fabsf(t) > 1e-10f) {
                 const float d = t - shift;
-                rsg.add(d);
-                rqg.add(d * d);
+                rsg += d;
+                rqg = fmaf(d, d, rqg);
                 rng += 1.f;
               }
               float J[NQ];
@@ -971,9 +972,9 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         if (tm.any(rem, iscr)) {
           float rr[NR];
           rr[0] = 0.f; rr[1] = 0.f;
-          rr[2] = rsg.s; rr[3] = -rsg.c; rr[4] = rqg.s; rr[5] = -rqg.c; rr[6] = rng;
+          rr[2] = rsg; rr[3] = rqg; rr[4] = rng;
 #pragma unroll
-          for (int k = 0; k < NQ; ++k) rr[7 + k] = rkg[k];
+          for (int k = 0; k < NQ; ++k) rr[5 + k] = rkg[k];
           tm.template sumf<NR>(rr, fscr);
 #pragma unroll
           for (int k = 2; k < NR; ++k) red[k] -= rr[k];
@@ -983,7 +984,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         // the g tile restricted to its selection, and its sums again (the f
         // selection, and with it J, follows the g selection in this form)
         int cnt = 0;
-        Kahan sg, qg;
+        float sg = 0.f, qg = 0.f;
         float kg[NQ];
 #pragma unroll
         for (int k = 0; k < NQ; ++k) kg[k] = 0.f;
@@ -995,8 +996,8 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
           cnt += bwg[p];
           if (fabsf(t) > 1e-10f) {
             const float d = t - shift;
-            sg.add(d);
-            qg.add(d * d);
+            sg += d;
+            qg = fmaf(d, d, qg);
             ng += 1.f;
           }
           float J[NQ];
@@ -1005,17 +1006,17 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
           for (int k = 0; k < NQ; ++k) kg[k] = fmaf(J[k], t, kg[k]);
         }
         red[0] = (float)cnt; red[1] = 0.f;
-        red[2] = sg.s; red[3] = -sg.c; red[4] = qg.s; red[5] = -qg.c; red[6] = ng;
+        red[2] = sg; red[3] = qg; red[4] = ng;
 #pragma unroll
-        for (int k = 0; k < NQ; ++k) red[7 + k] = kg[k];
+        for (int k = 0; k < NQ; ++k) red[5 + k] = kg[k];
         tm.template sumf<NR>(red, fscr);
         cg = (int)red[0];
       }
     }
     // g statistics from the shifted one-pass sums: mean and
     // sqrt((n-1) var) = sqrt(max(s2 - s1^2/n, 0)) (NaN for n = 0, 0 for n = 1)
-    const float cntg = red[6];
-    const float s1 = red[2] + red[3], s2 = red[4] + red[5];
+    const float cntg = red[4];
+    const float s1 = red[2], s2 = red[3];
     const float icnt = 1.f / cntg;
     const float meang = shift + s1 * icnt;
     float bg2 = fmaxf(s2 - s1 * s1 * icnt, 0.f);
@@ -1032,7 +1033,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     float b2[NQ];
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
-      const float jg = red[7 + k];
+      const float jg = red[5 + k];
       b2[k] = jf[k] * ibf - (jg - meang * j1[k]) * ibg;
     }
     // convergence test (FP32) and the update, identical on every lane

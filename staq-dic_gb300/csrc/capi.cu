@@ -418,15 +418,15 @@ std::vector<BatchedCand> batched_candidates(stdic_ctx* c, bool two, int npx_max,
   // per-pixel slot leaves more of the SM's unified L1 to cache the gradients;
   // tiles that do not fit use the warp's global slice, footprints that do not
   // fit are gathered from global memory.
-  const int shapes[][5] = {{1, 256, 0, 12800, 0},   {4, 256, 64, 2800, 0},
-                           {1, 256, 0, 2800, 1600}, {1, 256, 0, 4800, 1600},
-                           {4, 256, 32, 2800, 1300}, {4, 256, 64, 2800, 1300},
-                           {8, 256, 64, 2800, 650},  {4, 256, 32, 2800, 1600},
-                           {2, 256, 32, 2800, 1300}};
+  const int shapes[][5] = {{1, 256, 0, 12800, 0},   {4, 256, 64, 5600, 0},
+                           {1, 256, 0, 5600, 1600}, {1, 256, 0, 9600, 1600},
+                           {4, 256, 32, 5600, 1300}, {4, 256, 64, 5600, 1300},
+                           {8, 256, 64, 5600, 650},  {4, 256, 32, 5600, 1600},
+                           {2, 256, 32, 5600, 1300}};
   for (auto& sh : shapes) {
     const int tw = sh[0], threads = sh[1], split = sh[2], per_warp = sh[3], gt_warp = sh[4];
     const int teams_per_block = threads / (32 * tw);
-    const int bpp = two ? 12 : 8;
+    const int bpp = stdic::batched_tile_px_bytes(two);
     int smem_px = (int)((per_warp * tw - 512 - 32 * 4 * tw) / bpp);
     smem_px = std::max(64, std::min(smem_px, npx_max));
     const int gtile = gt_warp * tw;

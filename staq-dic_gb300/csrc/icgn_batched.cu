@@ -402,14 +402,17 @@ STDIC_DEV float dot_df(const float* hh, const float* hl, const float* x) {
 
 // Team slot layout: per-pixel arrays, the staged g footprint, the control
 // block and the reduction scratch.
+// Bytes per tile pixel: 6-DOF: the masked gradients (float2) cached for the
+// iterations, tempg and five bitmaps; 2-DOF: tempg, tempf and five bitmaps.
+__host__ __device__ __forceinline__ int tile_px_bytes(bool two) { return two ? 13 : 17; }
 __host__ __device__ __forceinline__ size_t tiles_bytes(int px, bool two) {
-  return ((size_t)px * (two ? 8 : 4) + 5 * (size_t)px + 15) / 16 * 16;
+  return ((size_t)px * tile_px_bytes(two) + 15) / 16 * 16;
 }
 // Bytes of one warp's global scratch slice (the per-pixel arrays for npx_max
 // pixels), a multiple of 16 so that every slice keeps the alignment of the
 // buffer for its float arrays.
 __host__ __device__ __forceinline__ size_t slice_bytes(int npx_max, bool two) {
-  return ((size_t)npx_max * (two ? 8 : 4) + 5 * (size_t)npx_max + 15) / 16 * 16;
+  return ((size_t)npx_max * tile_px_bytes(two) + 15) / 16 * 16;
 }
 __host__ __device__ __forceinline__ size_t gtile_bytes(int gt) {
   return ((size_t)(gt > 0 ? gt : 0) * 4 + 15) / 16 * 16;
@@ -455,6 +458,8 @@ STDIC_DEV float cubic_tile(const float* __restrict__ gt, int gtw, int gth, int g
 
 }  // namespace
 
+int batched_tile_px_bytes(bool two) { return tile_px_bytes(two); }
+
 size_t batched_team_bytes(int sm_px, bool two, int tw, int gtile) {
   return team_bytes(sm_px, two, tw, gtile);
 }
@@ -467,7 +472,7 @@ int batched_small_px(int sm_px, bool two, int tw, int gtile) {
   const size_t sub = (team_bytes(sm_px, two, tw, gtile) / tw) & ~(size_t)15;
   const int gs = gtile / tw;
   const long long fixed = (long long)(gtile_bytes(gs) + sizeof(TeamCtl) + sizeof(float) * 32 + 16 + 64 + 15);
-  long long px = ((long long)sub - fixed) / (two ? 12 : 8);
+  long long px = ((long long)sub - fixed) / tile_px_bytes(two);
   while (px > 0 && team_bytes((int)px, two, 1, gs) > sub) --px;
   return (int)(px > 0 ? px : 0);
 }
@@ -519,6 +524,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
   int4 pstart = make_int4(0, 0, 0, 0);  // PixIter start of this thread for the tile
   float* tg = nullptr;
   float* tf = nullptr;
+  float2* gq = nullptr;  // 6-DOF iterations: (gx, gy) of each tile pixel times the f selection
   uint8_t *mtile = nullptr, *bwf = nullptr, *bwg = nullptr, *tmp = nullptr, *bwm8 = nullptr;
   bool have_m8 = false;  // bwm8 holds the 8-connected selection of the mask tile
   bool has_masked = false;
@@ -586,6 +592,10 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     const bool in_smem = npx <= smpx;
     const int cap = in_smem ? smpx : a.npx_max;
     unsigned char* stp = in_smem ? base : gbase;
+    if constexpr (!TWO) {
+      gq = (float2*)stp;
+      stp += 8 * (size_t)cap;
+    }
     tg = (float*)stp;
     tf = tg + cap;
     mtile = (uint8_t*)(tg + (TWO ? 2 : 1) * cap);
@@ -606,6 +616,17 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
   }
 
   const uint8_t* bw = has_masked ? bwf : nullptr;  // nullptr: every pixel selected
+  if constexpr (!TWO) {
+    // the iterations' steepest-descent images depend on the fixed f selection
+    // only: each thread caches the masked gradients of its own pixels
+    if (stage == 2 && !decided && code == 0 && !nan_out) {
+      PixIter it(pstart, mx);
+      for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+        const float s = bw ? (float)bw[p] : 1.f;
+        gq[p] = make_float2(fr.GX(x1 + it.i, y1 + it.j) * s, fr.GY(x1 + it.i, y1 + it.j) * s);
+      }
+    }
+  }
   constexpr int NQ = TWO ? 2 : 6;  // parameters of the b-vector
   // inverse of the 2x2 system (2-DOF) as double-float pairs: row k of lane k < 2
   float ih[2] = {0.f, 0.f}, il[2] = {0.f, 0.f};
@@ -615,6 +636,14 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
   for (int q = 0; q < NQ; ++q) { jf[q] = 0.f; j1[q] = 0.f; }
   // steepest-descent images J of pixel (i, j): [dx gx, dx gy, dy gx, dy gy, gx, gy]
   // (6-DOF) or [gx, gy] (2-DOF), gx/gy masked by the current selection
+  // the same from the cached gradients of pixel p (6-DOF iterations)
+  auto jacq = [&](int p, int i, int j, float (&J)[NQ]) {
+    if constexpr (!TWO) {
+      const float2 g2 = gq[p];
+      const float dx = (float)(int)(x1 + i - x0), dy = (float)(int)(y1 + j - y0);
+      J[0] = dx * g2.x; J[1] = dx * g2.y; J[2] = dy * g2.x; J[3] = dy * g2.y; J[4] = g2.x; J[5] = g2.y;
+    }
+  };
   auto jac = [&](int i, int j, float s, float (&J)[NQ]) {
     const float gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
     if constexpr (TWO) {
@@ -837,7 +866,8 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
           ng += 1.f;
         }
         float J[NQ];
-        jac(i, j, bw ? (float)bw[p] : 1.f, J);
+        if constexpr (TWO) jac(i, j, bw ? (float)bw[p] : 1.f, J);
+        else jacq(p, i, j, J);
 #pragma unroll
         for (int k = 0; k < NQ; ++k) kg[k] = fmaf(J[k], t, kg[k]);
       };
@@ -962,7 +992,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
                 rng += 1.f;
               }
               float J[NQ];
-              jac(it.i, it.j, bw ? (float)bw[p] : 1.f, J);
+              jacq(p, it.i, it.j, J);
 #pragma unroll
               for (int k = 0; k < NQ; ++k) rkg[k] = fmaf(J[k], t, rkg[k]);
             }

@@ -95,6 +95,8 @@ cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hin
 
 
 // Size of one team's shared slot / global slice of the batched kernel.
+// bytes per tile pixel of the per-subset arrays
+int batched_tile_px_bytes(bool two);
 size_t batched_team_bytes(int sm_px, bool two, int tw, int gtile);
 size_t batched_scratch_bytes(int npx_max, bool two, long long warps);
 int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px, int gtile);

@@ -769,7 +769,9 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         // large ones they go to the wide teams of the split form
         const bool wide = B.split && (cntf > 0 || has_masked || wx >= B.split_ws);
         const int slot = atomicAdd(&B.n2[wide ? 0 : 1], 1);
-        B.order2[(wide ? 0 : Ntot) + slot] = item;
+        // the single-warp list is filled from its end, so that the iteration
+        // stage takes it in the reverse of the set-up order (smallest first)
+        B.order2[wide ? (size_t)slot : 2 * (size_t)Ntot - 1 - slot] = item;
       }
       if (code != 0 || nan_out) {
         a.conv[item] = code;
@@ -1208,7 +1210,7 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
       team_loop<TW, TWO, STAGE>(B, tm, B.queue_head, 0, nwide, tbase, B.smem_px, B.gtile, gteam, B.order2);
     else
       team_loop<TW, TWO, STAGE>(B, tm, B.queue_head, 0, nrest, tbase, B.smem_px, B.gtile, gteam,
-                                B.order2 + Ntot);
+                                B.order2 + 2 * (size_t)Ntot - nrest);
     if constexpr (TW > 1) {
       if (split) {
         Team<1> t1;
@@ -1217,7 +1219,7 @@ __global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
         const size_t sub = (tb / TW) & ~(size_t)15;
         team_loop<1, TWO, STAGE>(B, t1, B.queue_head + 1, 0, nrest, tbase + sub * (warp % TW),
                                  B.smem_px_small, B.gtile_small, B.scratch + gstride * (gwarp0 + warp),
-                                 B.order2 + Ntot);
+                                 B.order2 + 2 * (size_t)Ntot - nrest);
       }
     }
     return;

@@ -24,7 +24,7 @@ struct stdic_ctx {
   size_t ws_size = 0;
   int* scal = nullptr;  // device scalars: [1] badnum, [2] iters, [3] status, [4..5] queue heads, [6] queue split,
                         // [7] adjoint queue head, [8..9] iteration-list counts,
-                        // [10] gradient tile-copy time-out flag
+                        // [10] gradient tile-copy time-out flag, [20] bad-point threshold
   double* scald = nullptr;  // device double scalars: [0] residual
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t es0 = nullptr, es1 = nullptr;  // around the last IC-GN solver kernel
@@ -146,9 +146,10 @@ struct Plan {
   }
 };
 
-int check_launch(stdic_ctx* c, cudaError_t e, const char* what) {
+// kernels: how many kernels the launcher issued
+int check_launch(stdic_ctx* c, cudaError_t e, const char* what, int kernels = 1) {
   if (e != cudaSuccess) return cuda_fail(c, e, what);
-  ++c->launches;
+  c->launches += kernels;
   return STDIC_OK;
 }
 
@@ -638,7 +639,7 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
     }
     if (rc) return rc;
     if (filter) {
-      rc = check_launch(c, stdic::launch_badpoints(a.conv, N, a.U, a.F, 0, c->scal + 1, c->stream), "bad points");
+      rc = check_launch(c, stdic::launch_badpoints(a.conv, N, a.U, a.F, 0, c->scal + 1, c->scal + 20, c->stream), "bad points", 2);
       if (rc) return rc;
     }
   } else if (filter) {
@@ -765,7 +766,7 @@ static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, 
     }
     if (rc) return rc;
     if (filter) {
-      rc = check_launch(c, stdic::launch_badpoints(a.conv, N, a.U, nullptr, 1, c->scal + 1, c->stream), "bad points");
+      rc = check_launch(c, stdic::launch_badpoints(a.conv, N, a.U, nullptr, 1, c->scal + 1, c->scal + 20, c->stream), "bad points", 2);
       if (rc) return rc;
     }
   } else if (filter) {
@@ -882,7 +883,7 @@ int stdic_nodal_strain(stdic_ctx* c, const double* coords, int N, const int32_t*
   if (rc) return rc;
   if (N > 0) {
     int *ptr = nullptr, *list = nullptr;
-    rc = check_launch(c, stdic::build_topology(de, E, N, tws, &ptr, &list, c->stream), "mesh topology");
+    rc = check_launch(c, stdic::build_topology(de, E, N, tws, &ptr, &list, c->stream), "mesh topology", E > 0 ? 4 : 2);
     if (!rc) rc = check_launch(c, stdic::launch_nodal_strain(dc, N, de, E, du, gauss_order, ptr, list, dF, c->stream),
                                "nodal strain");
     if (rc) return rc;
@@ -915,8 +916,8 @@ int stdic_fill_nans(stdic_ctx* c, const double* coords, int N, const int32_t* el
       if (e != cudaSuccess) return cuda_fail(c, e, "NaN fill");
     }
     int *ptr = nullptr, *list = nullptr;
-    rc = check_launch(c, stdic::build_topology(de, E, N, tws, &ptr, &list, c->stream), "mesh topology");
-    if (!rc) rc = check_launch(c, stdic::launch_fill_nans(N, de, E, ptr, list, uout, tmp, c->stream), "NaN fill");
+    rc = check_launch(c, stdic::build_topology(de, E, N, tws, &ptr, &list, c->stream), "mesh topology", E > 0 ? 4 : 2);
+    if (!rc) rc = check_launch(c, stdic::launch_fill_nans(N, de, E, ptr, list, uout, tmp, c->stream), "NaN fill", 2);
     if (rc) return rc;
   }
   return pl.finish(c);
@@ -977,7 +978,7 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
   pl.out_opt(badnum, (size_t)steps, &hbad);
   pl.out_opt(pcg_iters, (size_t)steps, &hit);
   pl.scratch((size_t)steps, &hst);
-  pl.scratch(8, &dsc);  // [0] badnum, [1] iters, [2] status
+  pl.scratch(8, &dsc);  // [0] badnum, [1] iters, [2] status, [3] bad-point threshold
   double *F1 = nullptr, *tmp = nullptr, *dres = nullptr;
   int32_t* conv = nullptr;
   pl.scratch(n4, &F1);
@@ -1008,7 +1009,7 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
   if (!rc) rc = copy_in(ovd, ivd, n2);
   if (!rc && batched) rc = convert_frame(c, fr, &d, 1);
   int *ptr = nullptr, *list = nullptr;
-  if (!rc) rc = check_launch(c, stdic::build_topology(delems, E, N, tws, &ptr, &list, c->stream), "mesh topology");
+  if (!rc) rc = check_launch(c, stdic::build_topology(delems, E, N, tws, &ptr, &list, c->stream), "mesh topology", E > 0 ? 4 : 2);
   if (rc) return rc;
 
   // Subpb1 (2-DOF IC-GN): UOld = U2, FOld = F2 -> U1
@@ -1030,8 +1031,8 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
     int r = STDIC_OK;
     if (batched) r = run_batched(c, b, N, cands, QueueKeys{nullptr, dwl, 0});
     else r = check_launch(c, stdic::launch_icgn2_plain(a, c->stream), "Subpb1 plain");
-    if (!r) r = check_launch(c, stdic::launch_badpoints(conv, N, oU1, nullptr, 1, dsc, c->stream), "bad points");
-    if (!r) r = check_launch(c, stdic::launch_fill_nans(N, delems, E, ptr, list, oU1, tmp, c->stream), "NaN fill");
+    if (!r) r = check_launch(c, stdic::launch_badpoints(conv, N, oU1, nullptr, 1, dsc, dsc + 3, c->stream), "bad points", 2);
+    if (!r) r = check_launch(c, stdic::launch_fill_nans(N, delems, E, ptr, list, oU1, tmp, c->stream), "NaN fill", 2);
     if (!r) {
       const cudaError_t e = cudaMemcpyAsync(F1, oF2, 8 * n4, cudaMemcpyDeviceToDevice, c->stream);
       if (e != cudaSuccess) r = cuda_fail(c, e, "FSubpb1");

@@ -5,6 +5,7 @@
 //   intsearch_kernel   func/funIntegerSearch.m:110-170 + func/findpeak.m:27-68 with
 //                      normxcorr2 restated from its published definition
 //   badpoints_kernel   LocalICGNQuadtree.m:153-177 / Subpb1Quadtree.m:173-191
+#include <algorithm>
 #include <cfloat>
 #include <cstdint>
 #include <mutex>
@@ -439,25 +440,32 @@ cudaError_t launch_icgn2_plain(const IcgnArgs& a, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
-// Bad-subset filter after the per-node loop (one CTA; N is at most a few
-// hundred thousand).  LocalICGNQuadtree: bad = conv<0 | conv>99, then also
-// conv > max(mean+std, 6) of the good codes; Subpb1Quadtree: max(mean+0.25 std,
-// 10).  U (and F for the first pass) become NaN at bad nodes; badnum is
-// #bad - #(conv==102).
+// Bad-subset filter after the per-node loop.  LocalICGNQuadtree: bad =
+// conv<0 | conv>99, then also conv > max(mean+std, 6) of the good codes;
+// Subpb1Quadtree: max(mean+0.25 std, 10).  U (and F for the first pass) become
+// NaN at bad nodes; badnum is #bad - #(conv==102).  One CTA takes the
+// statistics and writes the threshold as the largest good code (the codes are
+// integers, so c > thr <=> c > floor(thr)); a grid then writes the NaNs.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) badpoints_kernel(const int32_t* __restrict__ conv, int N,
-                                                         double* U, double* F, int two_dof,
-                                                         int* badnum) {
+__global__ void __launch_bounds__(1024) badpoints_stats_kernel(const int32_t* __restrict__ conv, int N,
+                                                               int two_dof, int* badnum, int* cmax) {
   // the statistics of the good codes are integer sums, taken exactly in int64
   __shared__ long long red[5][32];
-  __shared__ double thr_s;
   long long sc = 0, sc2 = 0, ng = 0, nbad = 0, n102 = 0;
-  for (int k = threadIdx.x; k < N; k += blockDim.x) {
-    const long long c = conv[k];
-    const bool bad = c < 0 || c > kMaxIter - 1;
-    if (!bad) { sc += c; sc2 += c * c; ++ng; }
-    nbad += bad;
-    n102 += (c == kMaxIter + 2);
+  const int step = 4 * blockDim.x;
+  for (int k0 = 4 * threadIdx.x; k0 < N; k0 += step) {
+    int cc[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) cc[u] = k0 + u < N ? conv[k0 + u] : 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (k0 + u >= N) continue;
+      const long long c = cc[u];
+      const bool bad = c < 0 || c > kMaxIter - 1;
+      if (!bad) { sc += c; sc2 += c * c; ++ng; }
+      nbad += bad;
+      n102 += (c == kMaxIter + 2);
+    }
   }
   long long v[5] = {sc, sc2, ng, nbad, n102};
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
@@ -468,25 +476,33 @@ __global__ void __launch_bounds__(1024) badpoints_kernel(const int32_t* __restri
     if (lane == 0) red[q][warp] = v[q];
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    long long t[5] = {0, 0, 0, 0, 0};
-    for (int q = 0; q < 5; ++q)
-      for (int w = 0; w < nw; ++w) t[q] += red[q][w];
-    const double n = (double)t[2];
-    const double mean = (double)t[0] / n;
-    // sum (c - mean)^2 = (n sum c^2 - (sum c)^2) / n, the numerator exact in integers
-    const long long num = t[2] * t[1] - t[0] * t[0];
-    const double sd = t[2] > 1 ? sqrt((double)num / n / (n - 1.0)) : (t[2] == 1 ? 0.0 : nan(""));
-    const double cand = two_dof ? mean + 0.25 * sd : mean + 1.0 * sd;
-    const double floorv = two_dof ? 10.0 : 6.0;
-    thr_s = isnan(cand) ? floorv : fmax(cand, floorv);
-    if (badnum) *badnum = (int)(t[3] - t[4]);
+  if (warp != 0) return;
+  long long t[5];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    t[q] = lane < nw ? red[q][lane] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t[q] += __shfl_xor_sync(0xffffffffu, t[q], o);
   }
-  __syncthreads();
-  const double thr = thr_s;
-  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+  if (lane != 0) return;
+  const double n = (double)t[2];
+  const double mean = (double)t[0] / n;
+  // sum (c - mean)^2 = (n sum c^2 - (sum c)^2) / n, the numerator exact in integers
+  const long long num = t[2] * t[1] - t[0] * t[0];
+  const double sd = t[2] > 1 ? sqrt((double)num / n / (n - 1.0)) : (t[2] == 1 ? 0.0 : nan(""));
+  const double cand = two_dof ? mean + 0.25 * sd : mean + 1.0 * sd;
+  const double floorv = two_dof ? 10.0 : 6.0;
+  const double thr = isnan(cand) ? floorv : fmax(cand, floorv);
+  *cmax = thr >= (double)kMaxIter ? kMaxIter : (int)floor(thr);
+  if (badnum) *badnum = (int)(t[3] - t[4]);
+}
+
+__global__ void badpoints_apply_kernel(const int32_t* __restrict__ conv, int N, double* U, double* F,
+                                       int two_dof, const int* __restrict__ cmax) {
+  const int thr = *cmax;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
     const int c = conv[k];
-    if (c < 0 || c > kMaxIter - 1 || (double)c > thr) {
+    if (c < 0 || c > kMaxIter - 1 || c > thr) {
       U[2 * k] = nan("");
       U[2 * k + 1] = nan("");
       if (F && !two_dof)
@@ -496,9 +512,11 @@ __global__ void __launch_bounds__(1024) badpoints_kernel(const int32_t* __restri
 }
 
 cudaError_t launch_badpoints(int32_t* conv, int N, double* U, double* F, int two_dof,
-                             int* badnum_dev, cudaStream_t s) {
+                             int* badnum_dev, int* tmp_dev, cudaStream_t s) {
   if (N <= 0) return cudaSuccess;
-  badpoints_kernel<<<1, 1024, 0, s>>>(conv, N, U, F, two_dof, badnum_dev);
+  badpoints_stats_kernel<<<1, 1024, 0, s>>>(conv, N, two_dof, badnum_dev, tmp_dev);
+  const int blocks = (int)std::min<long long>(((long long)N + 255) / 256, 152 * 4);
+  badpoints_apply_kernel<<<blocks, 256, 0, s>>>(conv, N, U, F, two_dof, tmp_dev);
   return cudaGetLastError();
 }
 
@@ -559,17 +577,42 @@ __global__ void __launch_bounds__(1024) build_queue_kernel(const int32_t* __rest
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int b = 0; b < 256; ++b) { start[b] = acc; acc += hist[b]; }
-    if (n_big) {
+  {
+    // exclusive scan of the 256 bins by the first eight warps (shuffles, then
+    // the eight warp totals), and the count of the team phase's bins
+    __shared__ int wsum[8];
+    __shared__ int nbig_w[8];
+    const int b = threadIdx.x, warp = threadIdx.x >> 5;
+    if (b < 256) {
+      const int h = hist[b];
+      int inc = h;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+      }
+      if (lane == 31) wsum[warp] = inc;
+      // bin b holds subsets of edge w, with b = 255 - w (0), w (1) or, for
+      // order 2, 255 - w when w >= big_ws
+      const int w = ascending == 2 ? 255 - b : (ascending ? b : 255 - b);
+      int big = (w >= max(big_ws, 0)) ? h : 0;
+      for (int o = 16; o > 0; o >>= 1) big += __shfl_xor_sync(0xffffffffu, big, o);
+      if (lane == 0) nbig_w[warp] = big;
+      __syncwarp();
+      start[b] = inc - h;
+    }
+    __syncthreads();
+    if (b < 256) {
+      int off = 0;
+      for (int q = 0; q < warp; ++q) off += wsum[q];
+      start[b] += off;
+    }
+    if (threadIdx.x == 0 && n_big) {
       int nb = 0;
-      for (int w = max(big_ws, 0); w < 256; ++w)
-        nb += hist[ascending == 2 ? 255 - w : (ascending ? w : 255 - w)];
+      for (int q = 0; q < 8; ++q) nb += nbig_w[q];
       *n_big = nb;
     }
+    __syncthreads();
   }
-  __syncthreads();
   for (int it0 = 0; it0 < nit; it0 += R) {
     int kk[R];
 #pragma unroll

@@ -16,9 +16,9 @@
 // bicubic weights, interpolation and residuals are FP32.  The per-iteration
 // sums (sum J g for the b-vector; the g statistics as one-pass sums shifted by
 // meanf, so that the variance does not cancel) are per-lane FP32 FMA chains
-// reduced across lanes in FP32; the set-up's f statistics and b-vector parts
-// are Kahan-compensated; the Hessian is accumulated in plain FP32 (it only
-// scales the step, never the converged point).  The 6x6 Hessian is reduced,
+// reduced across lanes in FP32, and so are the set-up's f statistics (two
+// passes: the mean, then the sums around it) and the Hessian (it only scales
+// the step, never the converged point).  The 6x6 Hessian is reduced,
 // factorised (Cholesky, else LU with partial pivoting) and inverted in FP64
 // once per subset; every iteration applies that FP64 inverse to the FP32
 // right-hand side in double-float arithmetic (FP32 pairs with exact products
@@ -136,16 +136,6 @@ STDIC_DEV bool corners_oob_warp(const float P[6], int x0, int y0, int x1, int y1
   }
   return __any_sync(0xffffffffu, bad);
 }
-
-struct Kahan {
-  float s = 0.f, c = 0.f;
-  STDIC_DEV void add(float x) {
-    const float y = x - c;
-    const float t = s + y;
-    c = (t - s) - y;
-    s = t;
-  }
-};
 
 // Runs of the set bits of A that contain a bit of S (S subset of A): adding S
 // to A carries through each seeded run and clears it, so ((A + S) ^ A) & A
@@ -660,8 +650,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     float hs[21];
 #pragma unroll
     for (int k = 0; k < 21; ++k) hs[k] = 0.f;
-    Kahan sf;
-    float nf = 0.f, sa = 0.f;
+    float sf = 0.f, nf = 0.f, sa = 0.f;
     PixIter it(pstart, mx);
     for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
       const int i = it.i, j = it.j;
@@ -669,7 +658,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
       const float fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
       if constexpr (TWO) tf[p] = fv;
       sa += fabsf(fv);
-      if (fabsf(fv) > 1e-10f) { sf.add(fv); nf += 1.f; }
+      if (fabsf(fv) > 1e-10f) { sf += fv; nf += 1.f; }
       float J[NQ];
       jac(i, j, s, J);
       int q = 0;
@@ -678,37 +667,37 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
 #pragma unroll
         for (int bb = aa; bb < NQ; ++bb) hs[q++] += J[aa] * J[bb];
     }
-    float st4[4] = {sf.s, -sf.c, nf, sa};
-    tm.template sumf<4>(st4, fscr);
-    const float cnt = st4[2];
-    const float mean = (st4[0] + st4[1]) / cnt;
-    Kahan q, kjf[NQ], kj1[NQ];
+    float st3[3] = {sf, nf, sa};
+    tm.template sumf<3>(st3, fscr);
+    const float cnt = st3[1];
+    const float mean = st3[0] / cnt;
+    float q = 0.f, kjf[NQ], kj1[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) { kjf[k] = 0.f; kj1[k] = 0.f; }
     PixIter it2(pstart, mx);
     for (int p = tm.tl; p < npx; p += tm.TT, it2.next()) {
       const float s = bw ? (float)bw[p] : 1.f;
       float fv;
       if constexpr (TWO) fv = tf[p];
       else fv = fr.F(x1 + it2.i, y1 + it2.j) * fr.M(x1 + it2.i, y1 + it2.j) * s;
-      if (fabsf(fv) > 1e-10f) { const float d = fv - mean; q.add(d * d); }
+      const float d = fv - mean;
+      if (fabsf(fv) > 1e-10f) q = fmaf(d, d, q);
       float J[NQ];
       jac(it2.i, it2.j, s, J);
 #pragma unroll
-      for (int k = 0; k < NQ; ++k) { kjf[k].add(J[k] * (fv - mean)); kj1[k].add(J[k]); }
+      for (int k = 0; k < NQ; ++k) { kjf[k] = fmaf(J[k], d, kjf[k]); kj1[k] += J[k]; }
     }
-    float qq[2 + 4 * NQ];
-    qq[0] = q.s; qq[1] = -q.c;
+    float qq[1 + 2 * NQ];
+    qq[0] = q;
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      qq[2 + 4 * k] = kjf[k].s; qq[3 + 4 * k] = -kjf[k].c;
-      qq[4 + 4 * k] = kj1[k].s; qq[5 + 4 * k] = -kj1[k].c;
-    }
-    tm.template sumf<2 + 4 * NQ>(qq, fscr);
+    for (int k = 0; k < NQ; ++k) { qq[1 + k] = kjf[k]; qq[1 + NQ + k] = kj1[k]; }
+    tm.template sumf<1 + 2 * NQ>(qq, fscr);
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) { jf[k] = qq[2 + 4 * k] + qq[3 + 4 * k]; j1[k] = qq[4 + 4 * k] + qq[5 + 4 * k]; }
-    const float var = cnt == 0.f ? __int_as_float(0x7fc00000) : (cnt == 1.f ? 0.f : (qq[0] + qq[1]) / (cnt - 1.f));
+    for (int k = 0; k < NQ; ++k) { jf[k] = qq[1 + k]; j1[k] = qq[1 + NQ + k]; }
+    const float var = cnt == 0.f ? __int_as_float(0x7fc00000) : (cnt == 1.f ? 0.f : qq[0] / (cnt - 1.f));
     meanf = mean;
     bottomf = sqrtf((cnt - 1.f) * var);
-    sabs = st4[3];
+    sabs = st3[2];
     if constexpr (TWO) {
       tm.template sumf<3>(*reinterpret_cast<float(*)[3]>(hs), fscr);
       // H2 + 1e-3 max(diag H2) I of funICGN_Subpb1.m:391-394, inverted in FP64

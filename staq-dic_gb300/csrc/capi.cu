@@ -24,7 +24,8 @@ struct stdic_ctx {
   size_t ws_size = 0;
   int* scal = nullptr;  // device scalars: [1] badnum, [2] iters, [3] status, [4..5] queue heads, [6] queue split,
                         // [7] adjoint queue head, [8..9] iteration-list counts,
-                        // [10] gradient tile-copy time-out flag, [20] bad-point threshold
+                        // [10] gradient tile-copy time-out flag, [20] bad-point threshold,
+                        // [64..575] work-queue histogram and bin cursors
   double* scald = nullptr;  // device double scalars: [0] residual
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t es0 = nullptr, es1 = nullptr;  // around the last IC-GN solver kernel
@@ -186,7 +187,7 @@ int stdic_ctx_create(stdic_ctx** out, int device) {
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&c->scal, 64 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&c->scal, (64 + 512) * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c->scald, 8 * sizeof(double));
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
@@ -499,9 +500,9 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
     // list, filled in set-up order, then runs largest first too.
     const int mode = cd.split ? (two ? 2 : 0) : (cd.tw == 1 ? 1 : 0);
     int rc = check_launch(c, stdic::launch_build_queue(qk.ws_list, qk.wsl2, qk.ws_all, b.a.N,
-                                                       (int32_t*)b.order, c->scal + 6, c->stream, mode,
-                                                       cd.split),
-                          "queue");
+                                                       (int32_t*)b.order, c->scal + 6, c->scal + 64, c->stream,
+                                                       mode, cd.split),
+                          "queue", 3);
     if (rc) return rc;
     // 2-DOF: one fused pass; 6-DOF: set-up, FP64 factorisation, iterations
     const int stages[2] = {two ? 0 : 1, 2};

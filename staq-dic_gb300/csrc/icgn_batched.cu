@@ -656,11 +656,13 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
       const int i = it.i, j = it.j;
       const float s = bw ? (float)bw[p] : 1.f;
       const float fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
-      if constexpr (TWO) tf[p] = fv;
       sa += fabsf(fv);
       if (fabsf(fv) > 1e-10f) { sf += fv; nf += 1.f; }
       float J[NQ];
       jac(i, j, s, J);
+      // the second pass reads f and the masked gradients back from the tile
+      if constexpr (TWO) tf[p] = fv;
+      else { tg[p] = fv; gq[p] = make_float2(J[4], J[5]); }
       int q = 0;
 #pragma unroll
       for (int aa = 0; aa < NQ; ++aa)
@@ -677,13 +679,12 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     PixIter it2(pstart, mx);
     for (int p = tm.tl; p < npx; p += tm.TT, it2.next()) {
       const float s = bw ? (float)bw[p] : 1.f;
-      float fv;
-      if constexpr (TWO) fv = tf[p];
-      else fv = fr.F(x1 + it2.i, y1 + it2.j) * fr.M(x1 + it2.i, y1 + it2.j) * s;
+      const float fv = TWO ? tf[p] : tg[p];
       const float d = fv - mean;
       if (fabsf(fv) > 1e-10f) q = fmaf(d, d, q);
       float J[NQ];
-      jac(it2.i, it2.j, s, J);
+      if constexpr (TWO) jac(it2.i, it2.j, s, J);
+      else jacq(p, it2.i, it2.j, J);
 #pragma unroll
       for (int k = 0; k < NQ; ++k) { kjf[k] = fmaf(J[k], d, kjf[k]); kj1[k] += J[k]; }
     }

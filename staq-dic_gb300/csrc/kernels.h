@@ -120,8 +120,9 @@ cudaError_t launch_to_f32(const double* in, float* out, long long n, cudaStream_
 // decreasing size, 1 by increasing size, 2 puts the subsets of at least big_ws
 // pixels a side first (decreasing) and the rest after them (increasing).
 // n_big (optional) receives the number of nodes whose size is at least big_ws.
+// scratch: 512 device ints
 cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int ws_all, int N,
-                               int32_t* order, int* n_big, cudaStream_t s, int ascending = 0,
+                               int32_t* order, int* n_big, int* scratch, cudaStream_t s, int ascending = 0,
                                int big_ws = 0);
 // Largest tile of a single warp's share of a split team slot.
 int batched_small_px(int sm_px, bool two, int tw, int gtile);

@@ -536,108 +536,116 @@ cudaError_t launch_to_f32(const double* in, float* out, long long n, cudaStream_
 }
 
 // ---------------------------------------------------------------------------
-// Work queue of the batched solver: nodes ordered by decreasing subset size
-// (counting sort over the subset edge length, one CTA).
+// Work queue of the batched solver: nodes ordered by subset size, a counting
+// sort over the subset edge length in three grid-wide steps (per-block
+// histograms merged into 256 global bins, a scan of the bins, then a scatter
+// in which each block reserves its range of every bin with one atomic).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) build_queue_kernel(const int32_t* __restrict__ ws_list,
-                                                           const int32_t* __restrict__ wsl2,
-                                                           int ws_all, int N, int32_t* order,
-                                                           int ascending, int big_ws, int* n_big) {
-  __shared__ int hist[256];
-  __shared__ int start[256];
-  for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
-  __syncthreads();
+struct QueueKey {
+  const int32_t* ws_list;
+  const int32_t* wsl2;
+  int ws_all, N, ascending, bw;
   // order 0: larger subsets first; 1: smaller first; 2: subsets of at least
-  // big_ws pixels a side first (larger first), then the rest smaller first
-  const int bw = min(max(big_ws, 1), 255);
-  auto key = [&](int k) {
+  // bw pixels a side first (larger first), then the rest smaller first
+  STDIC_DEV int operator()(int k) const {
     int w = ws_all;
     if (wsl2) w = max(wsl2[k], wsl2[N + k]);
     else if (ws_list) w = ws_list[k];
     const int b = min(max(w, 0), 255);
     if (ascending == 2) return b >= bw ? 255 - b : 256 - bw + b;
     return ascending ? b : 255 - b;
-  };
-  // warp-aggregated counting sort: one shared atomic per distinct key of a
-  // warp; the keys of eight rounds are loaded together so their loads overlap
+  }
+};
+
+constexpr int kQueueBlockItems = 2048;  // items per block of the histogram and scatter steps
+
+__global__ void __launch_bounds__(256) queue_hist_kernel(QueueKey key, int* __restrict__ ghist) {
+  __shared__ int hist[256];
+  hist[threadIdx.x] = 0;
+  __syncthreads();
   const int lane = threadIdx.x & 31;
-  const int nit = (N + blockDim.x - 1) / blockDim.x;
-  constexpr int R = 8;
-  for (int it0 = 0; it0 < nit; it0 += R) {
-    int kk[R];
-#pragma unroll
-    for (int u = 0; u < R; ++u) {
-      const int k = (it0 + u) * blockDim.x + threadIdx.x;
-      kk[u] = (it0 + u < nit && k < N) ? key(k) : -1;
-    }
-#pragma unroll
-    for (int u = 0; u < R; ++u) {
-      const unsigned grp = __match_any_sync(0xffffffffu, kk[u]);
-      if (kk[u] >= 0 && lane == __ffs(grp) - 1) atomicAdd(&hist[kk[u]], __popc(grp));
-    }
+  const int k0 = blockIdx.x * kQueueBlockItems;
+  const int k1 = min(key.N, k0 + kQueueBlockItems);
+  // the trip count is the same for every thread, so all lanes of a warp take
+  // part in each match, whether or not they hold an item
+  for (int k = k0 + threadIdx.x; k - threadIdx.x < k1; k += blockDim.x) {
+    const int kk = k < k1 ? key(k) : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, kk);
+    if (kk >= 0 && lane == __ffs(grp) - 1) atomicAdd(&hist[kk], __popc(grp));
   }
   __syncthreads();
-  {
-    // exclusive scan of the 256 bins by the first eight warps (shuffles, then
-    // the eight warp totals), and the count of the team phase's bins
-    __shared__ int wsum[8];
-    __shared__ int nbig_w[8];
-    const int b = threadIdx.x, warp = threadIdx.x >> 5;
-    if (b < 256) {
-      const int h = hist[b];
-      int inc = h;
-      for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += t;
-      }
-      if (lane == 31) wsum[warp] = inc;
-      // bin b holds subsets of edge w, with b = 255 - w (0), w (1) or, for
-      // order 2, 255 - w when w >= big_ws
-      const int w = ascending == 2 ? 255 - b : (ascending ? b : 255 - b);
-      int big = (w >= max(big_ws, 0)) ? h : 0;
-      for (int o = 16; o > 0; o >>= 1) big += __shfl_xor_sync(0xffffffffu, big, o);
-      if (lane == 0) nbig_w[warp] = big;
-      __syncwarp();
-      start[b] = inc - h;
-    }
-    __syncthreads();
-    if (b < 256) {
-      int off = 0;
-      for (int q = 0; q < warp; ++q) off += wsum[q];
-      start[b] += off;
-    }
-    if (threadIdx.x == 0 && n_big) {
-      int nb = 0;
-      for (int q = 0; q < 8; ++q) nb += nbig_w[q];
-      *n_big = nb;
-    }
-    __syncthreads();
+  if (hist[threadIdx.x]) atomicAdd(&ghist[threadIdx.x], hist[threadIdx.x]);
+}
+
+// exclusive scan of the 256 bins into cursor, and the number of items of at
+// least big_ws pixels a side
+__global__ void __launch_bounds__(256) queue_scan_kernel(const int* __restrict__ ghist, int* cursor,
+                                                         int ascending, int big_ws, int* n_big) {
+  __shared__ int wsum[8], wbig[8];
+  const int b = threadIdx.x, lane = b & 31, warp = b >> 5;
+  const int h = ghist[b];
+  int inc = h;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
   }
-  for (int it0 = 0; it0 < nit; it0 += R) {
-    int kk[R];
-#pragma unroll
-    for (int u = 0; u < R; ++u) {
-      const int k = (it0 + u) * blockDim.x + threadIdx.x;
-      kk[u] = (it0 + u < nit && k < N) ? key(k) : -1;
-    }
-#pragma unroll
-    for (int u = 0; u < R; ++u) {
-      const int k = (it0 + u) * blockDim.x + threadIdx.x;
-      const unsigned grp = __match_any_sync(0xffffffffu, kk[u]);
-      const int leader = __ffs(grp) - 1;
-      int base = 0;
-      if (kk[u] >= 0 && lane == leader) base = atomicAdd(&start[kk[u]], __popc(grp));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (kk[u] >= 0) order[base + __popc(grp & ((1u << lane) - 1u))] = k;
-    }
+  // bin b holds subsets of edge w, with b = 255 - w (orders 0 and 2 for
+  // w >= big_ws) or b = w (order 1)
+  const int w = ascending == 2 ? 255 - b : (ascending ? b : 255 - b);
+  int big = w >= max(big_ws, 0) ? h : 0;
+  for (int o = 16; o > 0; o >>= 1) big += __shfl_xor_sync(0xffffffffu, big, o);
+  if (lane == 31) wsum[warp] = inc;
+  if (lane == 0) wbig[warp] = big;
+  __syncthreads();
+  int off = 0;
+  for (int q = 0; q < warp; ++q) off += wsum[q];
+  cursor[b] = off + inc - h;
+  if (b == 0 && n_big) {
+    int nb = 0;
+    for (int q = 0; q < 8; ++q) nb += wbig[q];
+    *n_big = nb;
+  }
+}
+
+__global__ void __launch_bounds__(256) queue_scatter_kernel(QueueKey key, int* cursor, int32_t* __restrict__ order) {
+  __shared__ int cnt[256], base[256];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int k0 = blockIdx.x * kQueueBlockItems;
+  const int k1 = min(key.N, k0 + kQueueBlockItems);
+  for (int k = k0 + threadIdx.x; k - threadIdx.x < k1; k += blockDim.x) {
+    const int kk = k < k1 ? key(k) : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, kk);
+    if (kk >= 0 && lane == __ffs(grp) - 1) atomicAdd(&cnt[kk], __popc(grp));
+  }
+  __syncthreads();
+  base[threadIdx.x] = cnt[threadIdx.x] ? atomicAdd(&cursor[threadIdx.x], cnt[threadIdx.x]) : 0;
+  __syncthreads();
+  for (int k = k0 + threadIdx.x; k - threadIdx.x < k1; k += blockDim.x) {
+    const int kk = k < k1 ? key(k) : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, kk);
+    const int leader = __ffs(grp) - 1;
+    int pos = 0;
+    if (kk >= 0 && lane == leader) pos = atomicAdd(&base[kk], __popc(grp));
+    pos = __shfl_sync(0xffffffffu, pos, leader);
+    if (kk >= 0) order[pos + __popc(grp & ((1u << lane) - 1u))] = k;
   }
 }
 
 cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int ws_all, int N,
-                               int32_t* order, int* n_big, cudaStream_t s, int ascending,
+                               int32_t* order, int* n_big, int* scratch, cudaStream_t s, int ascending,
                                int big_ws) {
   if (N <= 0) return cudaSuccess;
-  build_queue_kernel<<<1, 1024, 0, s>>>(ws_list, wsl2, ws_all, N, order, ascending, big_ws, n_big);
+  QueueKey key{ws_list, wsl2, ws_all, N, ascending, min(max(big_ws, 1), 255)};
+  int* ghist = scratch;
+  int* cursor = scratch + 256;
+  cudaError_t e = cudaMemsetAsync(ghist, 0, 256 * sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  const int blocks = (N + kQueueBlockItems - 1) / kQueueBlockItems;
+  queue_hist_kernel<<<blocks, 256, 0, s>>>(key, ghist);
+  queue_scan_kernel<<<1, 256, 0, s>>>(ghist, cursor, ascending, big_ws, n_big);
+  queue_scatter_kernel<<<blocks, 256, 0, s>>>(key, cursor, order);
   return cudaGetLastError();
 }
 

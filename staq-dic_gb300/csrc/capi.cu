@@ -24,7 +24,7 @@ struct stdic_ctx {
   size_t ws_size = 0;
   int* scal = nullptr;  // device scalars: [1] badnum, [2] iters, [3] status, [4..5] queue heads, [6] queue split,
                         // [7] adjoint queue head, [8..9] iteration-list counts,
-                        // [10] gradient tile-copy time-out flag, [20] bad-point threshold,
+                        // [10] gradient tile-copy time-out flag, [24..33] bad-point code statistics (5 x int64),
                         // [64..575] work-queue histogram and bin cursors
   double* scald = nullptr;  // device double scalars: [0] residual
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -640,7 +640,7 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
     }
     if (rc) return rc;
     if (filter) {
-      rc = check_launch(c, stdic::launch_badpoints(a.conv, N, a.U, a.F, 0, c->scal + 1, c->scal + 20, c->stream), "bad points", 2);
+      rc = check_launch(c, stdic::launch_badpoints(a.conv, N, a.U, a.F, 0, c->scal + 1, (unsigned long long*)(c->scal + 24), c->stream), "bad points", 2);
       if (rc) return rc;
     }
   } else if (filter) {
@@ -767,7 +767,7 @@ static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, 
     }
     if (rc) return rc;
     if (filter) {
-      rc = check_launch(c, stdic::launch_badpoints(a.conv, N, a.U, nullptr, 1, c->scal + 1, c->scal + 20, c->stream), "bad points", 2);
+      rc = check_launch(c, stdic::launch_badpoints(a.conv, N, a.U, nullptr, 1, c->scal + 1, (unsigned long long*)(c->scal + 24), c->stream), "bad points", 2);
       if (rc) return rc;
     }
   } else if (filter) {
@@ -979,7 +979,7 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
   pl.out_opt(badnum, (size_t)steps, &hbad);
   pl.out_opt(pcg_iters, (size_t)steps, &hit);
   pl.scratch((size_t)steps, &hst);
-  pl.scratch(8, &dsc);  // [0] badnum, [1] iters, [2] status, [3] bad-point threshold
+  pl.scratch(16, &dsc);  // [0] badnum, [1] iters, [2] status, [4..13] bad-point code statistics (5 x int64)
   double *F1 = nullptr, *tmp = nullptr, *dres = nullptr;
   int32_t* conv = nullptr;
   pl.scratch(n4, &F1);
@@ -1032,7 +1032,7 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
     int r = STDIC_OK;
     if (batched) r = run_batched(c, b, N, cands, QueueKeys{nullptr, dwl, 0});
     else r = check_launch(c, stdic::launch_icgn2_plain(a, c->stream), "Subpb1 plain");
-    if (!r) r = check_launch(c, stdic::launch_badpoints(conv, N, oU1, nullptr, 1, dsc, dsc + 3, c->stream), "bad points", 2);
+    if (!r) r = check_launch(c, stdic::launch_badpoints(conv, N, oU1, nullptr, 1, dsc, (unsigned long long*)(dsc + 4), c->stream), "bad points", 2);
     if (!r) r = check_launch(c, stdic::launch_fill_nans(N, delems, E, ptr, list, oU1, tmp, c->stream), "NaN fill", 2);
     if (!r) {
       const cudaError_t e = cudaMemcpyAsync(F1, oF2, 8 * n4, cudaMemcpyDeviceToDevice, c->stream);

@@ -1273,16 +1273,21 @@ __global__ void __launch_bounds__(128) factor6_kernel(const SubsetState6* __rest
   double l[21];
 #pragma unroll
   for (int k = 0; k < 21; ++k) l[k] = H6[(size_t)t * 21 + k];
+  // GB300 issues FP64 at a small fraction of the FP32 rate, so each pivot
+  // takes one reciprocal square root (l_jj = d rsqrt(d), 1/l_jj = rsqrt(d))
+  // instead of a square root and a division
   bool ok = true;
+  double rl[6];
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
     double d = l[j * (j + 1) / 2 + j];
 #pragma unroll
     for (int k = 0; k < j; ++k) d -= l[j * (j + 1) / 2 + k] * l[j * (j + 1) / 2 + k];
     ok = ok && (d > 0);
-    const double ljj = sqrt(d > 0 ? d : 1.0);
-    const double inv = 1.0 / ljj;
-    l[j * (j + 1) / 2 + j] = ljj;
+    const double dd = d > 0 ? d : 1.0;
+    const double inv = rsqrt(dd);
+    rl[j] = inv;
+    l[j * (j + 1) / 2 + j] = dd * inv;
 #pragma unroll
     for (int i = j + 1; i < 6; ++i) {
       double s2 = l[i * (i + 1) / 2 + j];
@@ -1300,7 +1305,7 @@ __global__ void __launch_bounds__(128) factor6_kernel(const SubsetState6* __rest
   double m[21];
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
-    const double inv = 1.0 / l[i * (i + 1) / 2 + i];
+    const double inv = rl[i];
     m[i * (i + 1) / 2 + i] = inv;
 #pragma unroll
     for (int j = 0; j < i; ++j) {

@@ -112,9 +112,9 @@ cudaError_t launch_intsearch(const double* f, const double* g, int W, int H, int
                              int32_t* peak, cudaStream_t s);
 cudaError_t launch_icgn6_plain(const IcgnArgs& a, cudaStream_t s);
 cudaError_t launch_icgn2_plain(const IcgnArgs& a, cudaStream_t s);
-// tmp_dev: one device int of scratch (the threshold between the two launches)
+// tmp_dev: five device 64-bit integers of scratch (the code statistics)
 cudaError_t launch_badpoints(int32_t* conv, int N, double* U, double* F, int two_dof,
-                             int* badnum_dev, int* tmp_dev, cudaStream_t s);
+                             int* badnum_dev, unsigned long long* tmp_dev, cudaStream_t s);
 cudaError_t launch_to_f32(const double* in, float* out, long long n, cudaStream_t s);
 // Counting sort of the nodes by subset size into order: ascending 0 sorts by
 // decreasing size, 1 by increasing size, 2 puts the subsets of at least big_ws

@@ -443,32 +443,23 @@ cudaError_t launch_icgn2_plain(const IcgnArgs& a, cudaStream_t s) {
 // Bad-subset filter after the per-node loop.  LocalICGNQuadtree: bad =
 // conv<0 | conv>99, then also conv > max(mean+std, 6) of the good codes;
 // Subpb1Quadtree: max(mean+0.25 std, 10).  U (and F for the first pass) become
-// NaN at bad nodes; badnum is #bad - #(conv==102).  One CTA takes the
-// statistics and writes the threshold as the largest good code (the codes are
-// integers, so c > thr <=> c > floor(thr)); a grid then writes the NaNs.
+// NaN at bad nodes; badnum is #bad - #(conv==102).  A grid adds the
+// statistics of the good codes exactly in 64-bit integers; a second grid
+// derives the threshold in every block (the codes are integers, so
+// c > thr <=> c > floor(thr)) and writes the NaNs.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) badpoints_stats_kernel(const int32_t* __restrict__ conv, int N,
-                                                               int two_dof, int* badnum, int* cmax) {
-  // the statistics of the good codes are integer sums, taken exactly in int64
-  __shared__ long long red[5][32];
-  long long sc = 0, sc2 = 0, ng = 0, nbad = 0, n102 = 0;
-  const int step = 4 * blockDim.x;
-  for (int k0 = 4 * threadIdx.x; k0 < N; k0 += step) {
-    int cc[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) cc[u] = k0 + u < N ? conv[k0 + u] : 0;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      if (k0 + u >= N) continue;
-      const long long c = cc[u];
-      const bool bad = c < 0 || c > kMaxIter - 1;
-      if (!bad) { sc += c; sc2 += c * c; ++ng; }
-      nbad += bad;
-      n102 += (c == kMaxIter + 2);
-    }
+__global__ void __launch_bounds__(256) badpoints_stats_kernel(const int32_t* __restrict__ conv, int N,
+                                                              unsigned long long* sums) {
+  __shared__ long long red[5][8];
+  long long v[5] = {0, 0, 0, 0, 0};  // sum c, sum c^2, #good, #bad, #(c == 102)
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
+    const long long c = conv[k];
+    const bool bad = c < 0 || c > kMaxIter - 1;
+    if (!bad) { v[0] += c; v[1] += c * c; ++v[2]; }
+    v[3] += bad;
+    v[4] += (c == kMaxIter + 2);
   }
-  long long v[5] = {sc, sc2, ng, nbad, n102};
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q < 5; ++q) {
 #pragma unroll
@@ -476,30 +467,33 @@ __global__ void __launch_bounds__(1024) badpoints_stats_kernel(const int32_t* __
     if (lane == 0) red[q][warp] = v[q];
   }
   __syncthreads();
-  if (warp != 0) return;
-  long long t[5];
-#pragma unroll
-  for (int q = 0; q < 5; ++q) {
-    t[q] = lane < nw ? red[q][lane] : 0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t[q] += __shfl_xor_sync(0xffffffffu, t[q], o);
+  if (threadIdx.x < 5) {
+    long long t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+    if (t) atomicAdd(&sums[threadIdx.x], (unsigned long long)t);
   }
-  if (lane != 0) return;
-  const double n = (double)t[2];
-  const double mean = (double)t[0] / n;
-  // sum (c - mean)^2 = (n sum c^2 - (sum c)^2) / n, the numerator exact in integers
-  const long long num = t[2] * t[1] - t[0] * t[0];
-  const double sd = t[2] > 1 ? sqrt((double)num / n / (n - 1.0)) : (t[2] == 1 ? 0.0 : nan(""));
-  const double cand = two_dof ? mean + 0.25 * sd : mean + 1.0 * sd;
-  const double floorv = two_dof ? 10.0 : 6.0;
-  const double thr = isnan(cand) ? floorv : fmax(cand, floorv);
-  *cmax = thr >= (double)kMaxIter ? kMaxIter : (int)floor(thr);
-  if (badnum) *badnum = (int)(t[3] - t[4]);
 }
 
-__global__ void badpoints_apply_kernel(const int32_t* __restrict__ conv, int N, double* U, double* F,
-                                       int two_dof, const int* __restrict__ cmax) {
-  const int thr = *cmax;
+__global__ void __launch_bounds__(256) badpoints_apply_kernel(const int32_t* __restrict__ conv, int N, double* U,
+                                                              double* F, int two_dof,
+                                                              const unsigned long long* __restrict__ sums,
+                                                              int* badnum) {
+  __shared__ int cmax_s;
+  if (threadIdx.x == 0) {
+    const long long t0 = (long long)sums[0], t1 = (long long)sums[1], t2 = (long long)sums[2];
+    const double n = (double)t2;
+    const double mean = (double)t0 / n;
+    // sum (c - mean)^2 = (n sum c^2 - (sum c)^2) / n, the numerator exact in integers
+    const long long num = t2 * t1 - t0 * t0;
+    const double sd = t2 > 1 ? sqrt((double)num / n / (n - 1.0)) : (t2 == 1 ? 0.0 : nan(""));
+    const double cand = two_dof ? mean + 0.25 * sd : mean + 1.0 * sd;
+    const double floorv = two_dof ? 10.0 : 6.0;
+    const double thr = isnan(cand) ? floorv : fmax(cand, floorv);
+    cmax_s = thr >= (double)kMaxIter ? kMaxIter : (int)floor(thr);
+    if (blockIdx.x == 0 && badnum) *badnum = (int)((long long)sums[3] - (long long)sums[4]);
+  }
+  __syncthreads();
+  const int thr = cmax_s;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
     const int c = conv[k];
     if (c < 0 || c > kMaxIter - 1 || c > thr) {
@@ -512,11 +506,13 @@ __global__ void badpoints_apply_kernel(const int32_t* __restrict__ conv, int N, 
 }
 
 cudaError_t launch_badpoints(int32_t* conv, int N, double* U, double* F, int two_dof,
-                             int* badnum_dev, int* tmp_dev, cudaStream_t s) {
+                             int* badnum_dev, unsigned long long* tmp_dev, cudaStream_t s) {
   if (N <= 0) return cudaSuccess;
-  badpoints_stats_kernel<<<1, 1024, 0, s>>>(conv, N, two_dof, badnum_dev, tmp_dev);
+  cudaError_t e = cudaMemsetAsync(tmp_dev, 0, 5 * sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
   const int blocks = (int)std::min<long long>(((long long)N + 255) / 256, 152 * 4);
-  badpoints_apply_kernel<<<blocks, 256, 0, s>>>(conv, N, U, F, two_dof, tmp_dev);
+  badpoints_stats_kernel<<<blocks, 256, 0, s>>>(conv, N, tmp_dev);
+  badpoints_apply_kernel<<<blocks, 256, 0, s>>>(conv, N, U, F, two_dof, tmp_dev, badnum_dev);
   return cudaGetLastError();
 }
 

@@ -64,6 +64,40 @@ struct Team {
     sync();
     return s;
   }
+  // Team reduce-scatter of K <= 32 FP32 values: team thread k < K returns
+  // the team total of v[k] (the others return partial sums).  Within a warp
+  // each level exchanges half of the remaining values with the partner lane,
+  // 31 shuffles in all instead of 5 K.
+  template <int K>
+  STDIC_DEV float scatter_sum32(const float (&v)[K], float* scr) const {
+    static_assert(K <= 32, "at most 32 values");
+    const int lane = tl & 31;
+    float a[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) a[k] = k < K ? v[k] : 0.f;
+#pragma unroll
+    for (int lev = 0; lev < 5; ++lev) {
+      const int o = 16 >> lev, h = 16 >> lev;
+      const bool up = (lane & o) != 0;
+#pragma unroll
+      for (int k = 0; k < h; ++k) {
+        const float send = up ? a[k] : a[k + h];
+        const float keep = up ? a[k + h] : a[k];
+        a[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
+    }
+    float t = a[0];  // warp total of v[lane]
+    if constexpr (TW > 1) {
+      sync();
+      scr[(tl >> 5) * 32 + lane] = t;
+      sync();
+      t = 0.f;
+#pragma unroll
+      for (int w = 0; w < TW; ++w) t += scr[w * 32 + lane];
+      sync();
+    }
+    return t;
+  }
   // in-place team sum of K FP32 values (every thread receives the totals)
   template <int K>
   STDIC_DEV void sumf(float (&v)[K], float* scr) const {
@@ -723,13 +757,11 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         split_f64(r1, ih[1], il[1]);
       }
     } else {
-      tm.template sumf<21>(hs, fscr);
+      // each of the 21 sums is needed by one thread only (the one that
+      // writes it): a reduce-scatter leaves sum k with team thread k
+      const float v = tm.scatter_sum32(hs, fscr);
       // packed lower (row-major) Hessian for the factor kernel and the output
       if (tm.tl < 21) {
-        float v = 0.f;
-#pragma unroll
-        for (int k = 0; k < 21; ++k)
-          if (k == tm.tl) v = hs[k];
         // hs index of (row aa, col bb >= aa) -> packed lower (bb, aa)
         int aa = 0, rem = tm.tl;
         while (rem >= 6 - aa) { rem -= 6 - aa; ++aa; }

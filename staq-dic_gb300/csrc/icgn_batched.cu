@@ -98,6 +98,46 @@ struct Team {
     }
     return t;
   }
+  // In-place team sum of K <= 16 FP32 values, every thread receiving the
+  // totals: a warp reduce-scatter (value k ends in lanes 2k, 2k+1 after 16
+  // shuffles), then K shuffles (or shared-memory reads across the team) to
+  // give every lane all K totals; 16 + K shuffles instead of 5 K.
+  template <int K>
+  STDIC_DEV void sumf16(float (&v)[K], float* scr) const {
+    static_assert(K <= 16, "at most 16 values");
+    const int lane = tl & 31;
+    float a[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) a[k] = k < K ? v[k] : 0.f;
+#pragma unroll
+    for (int lev = 0; lev < 4; ++lev) {
+      const int o = 16 >> lev, h = 8 >> lev;
+      const bool up = (lane & o) != 0;
+#pragma unroll
+      for (int k = 0; k < h; ++k) {
+        const float send = up ? a[k] : a[k + h];
+        const float keep = up ? a[k + h] : a[k];
+        a[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
+    }
+    const float t = a[0] + __shfl_xor_sync(0xffffffffu, a[0], 1);  // total of value lane >> 1
+    if constexpr (TW == 1) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) v[k] = __shfl_sync(0xffffffffu, t, 2 * k);
+    } else {
+      sync();
+      if ((lane & 1) == 0) scr[(tl >> 5) * 16 + (lane >> 1)] = t;
+      sync();
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        float s2 = 0.f;
+#pragma unroll
+        for (int w = 0; w < TW; ++w) s2 += scr[w * 16 + k];
+        v[k] = s2;
+      }
+      sync();
+    }
+  }
   // in-place team sum of K FP32 values (every thread receives the totals)
   template <int K>
   STDIC_DEV void sumf(float (&v)[K], float* scr) const {
@@ -958,7 +998,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
 #pragma unroll
       for (int k = 0; k < NQ; ++k) red[5 + k] = kg[k];
     }
-    tm.template sumf<NR>(red, fscr);
+    tm.template sumf16<NR>(red, fscr);
     if (red[1] > 0.f) { err = true; break; }
     if (cntf > 0 || red[0] > 0.f) {
       for (int p = tm.tl; p < npx; p += tm.TT) tmp[p] = tg[p] != 0.f;
@@ -1029,7 +1069,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
           rr[2] = rsg; rr[3] = rqg; rr[4] = rng;
 #pragma unroll
           for (int k = 0; k < NQ; ++k) rr[5 + k] = rkg[k];
-          tm.template sumf<NR>(rr, fscr);
+          tm.template sumf16<NR>(rr, fscr);
 #pragma unroll
           for (int k = 2; k < NR; ++k) red[k] -= rr[k];
         }
@@ -1063,7 +1103,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         red[2] = sg; red[3] = qg; red[4] = ng;
 #pragma unroll
         for (int k = 0; k < NQ; ++k) red[5 + k] = kg[k];
-        tm.template sumf<NR>(red, fscr);
+        tm.template sumf16<NR>(red, fscr);
         cg = (int)red[0];
       }
     }

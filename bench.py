@@ -175,6 +175,16 @@ def traffic_from_profiles():
 
 
 # ----------------------------------------------------------------------------
+def workload_config(name, w):
+    """The config object both arms print for a LocalICGNQuadtree workload."""
+    W, H = w["f"].shape
+    ws = np.asarray(w["winsize_list"])
+    return {"workload": "%s: %dx%d plate with hole, Kirsch 1%% strain, quadtree, %d nodes, subsets 8..64 px, "
+                        "one LocalICGNQuadtree pass per step" % (name, W, H, w["coordinatesFEM"].shape[0]),
+            "nodes": int(w["coordinatesFEM"].shape[0]),
+            "subset_sizes": {str(k): int(v) for k, v in zip(*np.unique(ws, return_counts=True))}}
+
+
 def run_reference(args, world, rank):
     """CPU implementation of the path on the host cores (oracle port)."""
     if rank != 0:
@@ -210,8 +220,8 @@ def run_reference(args, world, rank):
     out = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "impl": "reference",
-           "config": {"workload": args.workload, "nodes": int(N), "sample_nodes": int(idx.size)},
+           "impl": "reference", "parallelism": "host threads", "precision": "FP64 (the oracle port)",
+           "config": workload_config(args.workload, w),
            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
@@ -725,12 +735,10 @@ def main():
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "%s: %dx%d plate with hole, Kirsch 1%% strain, quadtree, %d nodes, "
-                                  "subsets 8..64 px, one LocalICGNQuadtree pass per step" % (args.workload, W, H, N),
-                      "nodes": N, "subset_sizes": {str(k): int(v) for k, v in zip(*np.unique(ws_list, return_counts=True))},
-                      "precision": "batched FP32 (compensated sums, FP64 solves)",
-                      "l2": "flushed between timed steps (256 MiB write)",
-                      "parallelism": "replicas" if world > 1 else "single GPU"},
+           "config": workload_config(args.workload, w),
+           "precision": "batched FP32 (FMA sums, FP64 Hessian inverses)",
+           "l2": "flushed between timed steps (256 MiB write)",
+           "parallelism": "replicas" if world > 1 else "single GPU",
            "clocks": clocks,
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_mean},

@@ -177,3 +177,57 @@ def test_oracle_adjoint_matches_finite_differences(oracle):
         fd = (np.nansum(oracle.icgn_adjoint(f, gp, None, c, 32, U, F, False)[0]) -
               np.nansum(oracle.icgn_adjoint(f, gm, None, c, 32, U, F, False)[0])) / (2 * h)
         assert abs(fd - dg[x, y]) <= 1e-4 * max(abs(fd), 1e-8)
+
+
+def test_oracle_nodal_strain_of_linear_field_on_quadtree(oracle):
+    """The strain step (a replacement of the reference's, so pinned
+    analytically): on a quadtree mesh with hanging nodes, an affine
+    displacement field gives its constant gradient [du/dx dv/dx du/dy dv/dy]
+    at every node that lies in an element, and NaN elsewhere; the Gauss order
+    does not change it."""
+    from staqdic import workloads
+    w = workloads.hole1024(seed=1, size=256)
+    c, el = w["coordinatesFEM"], w["elementsFEM"]
+    A = np.array([[0.012, -0.004], [0.003, -0.007]])
+    U = (c @ A.T + np.array([2.0, -1.0])).ravel()
+    inel = np.zeros(c.shape[0], bool)
+    e = el[:, :8]
+    inel[e[e > 0] - 1] = True
+    for order in (2, 3):
+        F = oracle.nodal_strain(c, el, U, order).reshape(-1, 4)
+        assert np.all(np.isnan(F[~inel])) and not np.any(np.isnan(F[inel]))
+        assert np.max(np.abs(F[inel] - [A[0, 0], A[1, 0], A[0, 1], A[1, 1]])) < 1e-12
+
+
+def test_oracle_fill_nans_rules(oracle):
+    """The NaN fill (a replacement of the reference's RBF fill): a NaN node
+    takes the mean of its finite mesh neighbours; a NaN region fills from its
+    edge inwards sweep by sweep; a node in no element stays NaN."""
+    from staqdic import synth
+    xn, yn = synth.uniform_nodes(160, 160, 32, 16)
+    c, el = synth.uniform_mesh(xn, yn)
+    N = c.shape[0]
+    nx = len(xn)
+    rng = np.random.default_rng(5)
+    U = rng.normal(0, 1, 2 * N)
+    k = 2 * nx + 2  # an interior node
+    U[2 * k] = U[2 * k + 1] = np.nan
+    out = oracle.fill_nans(c, el, U)
+    # the neighbours of an interior Q4 node: the 8 surrounding grid nodes
+    nb = [k + d for d in (-nx - 1, -nx, -nx + 1, -1, 1, nx - 1, nx, nx + 1)]
+    assert np.isclose(out[2 * k], np.mean(U[2 * np.array(nb)]), rtol=0, atol=1e-15)
+    assert np.isclose(out[2 * k + 1], np.mean(U[2 * np.array(nb) + 1]), rtol=0, atol=1e-15)
+    keep = np.ones(2 * N, bool)
+    keep[[2 * k, 2 * k + 1]] = False
+    assert np.array_equal(out[keep], U[keep])
+    # a block of NaN nodes fills completely
+    V = U.copy()
+    blk = [r * nx + q for r in range(1, 5) for q in range(1, 5)]
+    for b in blk:
+        V[2 * b] = V[2 * b + 1] = np.nan
+    assert not np.any(np.isnan(oracle.fill_nans(c, el, V)))
+    # a node that no element contains keeps its NaN
+    c2 = np.vstack([c, [[500.0, 500.0]]])
+    V2 = np.concatenate([U, [np.nan, np.nan]])
+    out2 = oracle.fill_nans(c2, el, V2)
+    assert np.all(np.isnan(out2[-2:]))

@@ -1,30 +1,37 @@
 """Benchmark of the STAQ-DIC hot path on GB300.
 
 Metric: converged IC-GN subsets per second, counting a subset only when its
-code is 1..100 (and the LocalICGNQuadtree bad-subset filter kept it) and its
-displacement is within 0.01 px of the plain FP64 drop-in on the same inputs.
+code is 1..100, the LocalICGNQuadtree bad-subset filter (LocalICGNQuadtree.m:
+153-169) kept it (its U is not NaN) and its displacement is within 0.01 px of
+the FP64 solution on the same inputs.  Both arms count by that one rule: the
+GPU arm against the plain FP64 drop-in (equal to the FP64 oracle to 1e-6 px),
+the CPU arm is FP64 itself.
 
-Step (default workload hole1024): one LocalICGNQuadtree pass — the batched
-FP32 persistent kernel behind stdic_icgn_local — over all nodes of a seeded
-1024^2 plate-with-hole pair (Kirsch field, 1 % strain, quadtree 4..32 px,
-uneven subsets 8..64 px).  Inputs are resident in HBM (`value`); the same call
-with pinned host buffers, copies inside the timed region, gives `e2e`.  The L2
-is flushed (256 MiB write) between timed steps.
+Step (default workload hole2048, the 2048^2 quadtree config): one
+LocalICGNQuadtree pass -- the batched FP32 persistent kernel behind
+stdic_icgn_local -- over all 80,695 nodes of a seeded 2048^2 plate-with-hole
+pair (Kirsch field at 2 % strain, quadtree 4..32 px, uneven subsets 8..64 px).
+Inputs are resident in HBM (`value`); the same call with pinned host buffers,
+copies inside the timed region, gives `e2e`.  The L2 is flushed (256 MiB write)
+between timed steps.
 
-Beside the headline the line carries, on one GPU, the 2048^2 quadtree pass
-(config C3, ``c3``: batched vs plain FP64 vs the host CPU), the timing of
-the adjoint on the 4096^2 bumps pair (config C4, ``adjoint_c4``) and 16 frames
-in one multi-frame launch against the frames one by one (config C5, ``c5``);
---no-extras skips them.
+Beside the headline the line carries the plain FP64 drop-in on the same pass
+(`plain_fp64`, with its FP64-pipe roofline), the CPU port on the whole mesh
+(`cpu_baseline`, median of 5 runs), and, on one GPU, the 1024^2 quadtree pass
+(``c2``), three ADMM iterations on the 2048^2 mesh (``admm``), the adjoint on
+the 4096^2 bumps pair (``adjoint_c4``) and 16 frames in one multi-frame launch
+(``c5``); --no-extras skips them.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 N > 1 runs one replica per GPU (the path has no data-path collective);
 `value` is all ranks' converged subsets over the slowest rank's time.
 --impl reference times the CPU implementation of the path on the host cores
-(the reference is MATLAB, so the oracle's C++ restatement stands in).
+(the reference is MATLAB, so the oracle's C++ restatement stands in) on the
+same workload, the whole mesh every step.
 """
 import argparse
+import hashlib
 import json
 import os
 import subprocess
@@ -44,6 +51,11 @@ UNIT = "subsets/s"
 TOLPX = 0.01
 WS_MAX = 64
 TOL = 1e-2
+DEFAULT_WORKLOAD = "hole2048"
+# sources of the batched solver kernels: a traffic figure is quoted only from
+# an ncu capture of exactly these sources
+KERNEL_SOURCES = ("staq-dic_gb300/csrc/icgn_batched.cu", "staq-dic_gb300/csrc/device_common.cuh",
+                  "staq-dic_gb300/csrc/kernels.h")
 
 
 def log(*a):
@@ -68,13 +80,59 @@ def flops_per_subset(conv, ws_list):
     return 70.0 * npx + 106.0 * it * npx
 
 
+def converged_rule(U, conv, U_fp64=None):
+    """The metric's rule: code 1..100, not NaN (kept by the bad-subset filter),
+    and, when an FP64 solution is given, within 0.01 px of it."""
+    ok = (conv >= 1) & (conv <= 100) & ~np.isnan(U[0::2])
+    if U_fp64 is not None:
+        dU = np.abs(U - U_fp64).reshape(-1, 2).max(axis=1)
+        ok &= ~np.isnan(U_fp64[0::2]) & (dU <= TOLPX)
+    return ok
+
+
+def kernel_source_hash():
+    h = hashlib.sha256()
+    for rel in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, rel), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def traffic_from_profile(workload):
+    """DRAM bytes per pass of the batched solver from the committed ncu summary
+    of this workload, quoted only when that capture was taken of the current
+    kernel sources (the summary records their hash)."""
+    p = os.path.join(ROOT, "profiles", "icgn_batched_%s.md" % workload)
+    if not os.path.exists(p):
+        return None, "no ncu summary of this workload"
+    sha, val = None, None
+    for ln in open(p):
+        s = ln.strip()
+        if s.startswith("kernel_sources_sha256_16:"):
+            sha = s.split(":", 1)[1].strip()
+        elif s.startswith("dram_bytes_per_pass:"):
+            try:
+                val = float(s.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                val = None
+    cur = kernel_source_hash()
+    if sha != cur:
+        return None, "the ncu summary was captured on other kernel sources (%s, now %s)" % (sha, cur)
+    return val, "ncu capture of these kernel sources (%s), profiles/icgn_batched_%s.md" % (cur, workload)
+
+
 class ClockSampler:
-    """nvidia-smi clock / throttle samples during the timed region."""
+    """nvidia-smi clock / throttle samples around and during the timed region:
+    the last sample before it starts, every sample inside it, and the first
+    after it ends (so a region shorter than the 100 ms period still has two)."""
+
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, index=0):
         self.index = index
-        self.lines = []
+        self.samples = []  # (host time, line)
         self.proc = None
+        self.t0 = self.t1 = None
 
     def start(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -86,29 +144,43 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
-            # the timed region starts once the sampler reports (at most 3 s)
-            t0 = time.perf_counter()
-            while not self.lines and time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+            t = time.perf_counter()
+            while not self.samples and time.perf_counter() - t < 3.0 and self.proc.poll() is None:
                 time.sleep(0.01)
-            self.lines.clear()
         except Exception:
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.samples.append((time.perf_counter(), line.strip()))
+
+    def region_start(self):
+        self.t0 = time.perf_counter()
+
+    def region_end(self):
+        self.t1 = time.perf_counter()
+        if self.proc is not None:
+            t = time.perf_counter()
+            while (not any(ts > self.t1 for ts, _ in self.samples) and time.perf_counter() - t < 1.0
+                   and self.proc.poll() is None):
+                time.sleep(0.01)
 
     def stop(self):
         if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
+        s = list(self.samples)
+        t0 = self.t0 if self.t0 is not None else -1e30
+        t1 = self.t1 if self.t1 is not None else 1e30
+        before = [x for x in s if x[0] <= t0][-1:]
+        inside = [x for x in s if t0 < x[0] <= t1]
+        after = [x for x in s if x[0] > t1][:1]
         sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for _, ln in before + inside + after:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -117,12 +189,12 @@ class ClockSampler:
                 smax.append(float(parts[2]))
             except ValueError:
                 continue
-            for n, v in zip(names, parts[5:9]):
+            for n, v in zip(self.NAMES, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": float(max(smax)) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "samples_inside": len(inside)}
 
 
 def measured_peaks():
@@ -134,14 +206,14 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def fp32_peak_tflops(torch):
-    """FP32 CUDA-core throughput: cuBLAS SGEMM with TF32 disabled, 8192^3."""
+def gemm_peak_tflops(torch, dtype, n):
+    """CUDA-core throughput of one precision: a cuBLAS GEMM n^3 (TF32 off),
+    best of 5 (the burst figure, for kernels timed alone)."""
     old = torch.backends.cuda.matmul.allow_tf32
     torch.backends.cuda.matmul.allow_tf32 = False
     try:
-        n = 8192
-        a = torch.randn(n, n, device="cuda", dtype=torch.float32)
-        b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        a = torch.randn(n, n, device="cuda", dtype=dtype)
+        b = torch.randn(n, n, device="cuda", dtype=dtype)
         for _ in range(2):
             torch.matmul(a, b)
         torch.cuda.synchronize()
@@ -160,69 +232,87 @@ def fp32_peak_tflops(torch):
         torch.backends.cuda.matmul.allow_tf32 = old
 
 
-def traffic_from_profiles():
-    """DRAM bytes per launch of the batched kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "icgn_batched_hole1024.md")
-    if not os.path.exists(p):
-        return None
-    for ln in open(p):
-        if ln.strip().startswith("dram_bytes_per_launch:"):
-            try:
-                return float(ln.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
-
-
 # ----------------------------------------------------------------------------
 def workload_config(name, w):
     """The config object both arms print for a LocalICGNQuadtree workload."""
     W, H = w["f"].shape
     ws = np.asarray(w["winsize_list"])
-    return {"workload": "%s: %dx%d plate with hole, Kirsch 1%% strain, quadtree, %d nodes, subsets 8..64 px, "
-                        "one LocalICGNQuadtree pass per step" % (name, W, H, w["coordinatesFEM"].shape[0]),
+    return {"workload": "%s: %dx%d plate with hole, Kirsch %g%% strain, quadtree, %d nodes, subsets 8..64 px, "
+                        "one LocalICGNQuadtree pass per step" % (name, W, H, 100 * w.get("eps", 0),
+                                                                  w["coordinatesFEM"].shape[0]),
             "nodes": int(w["coordinatesFEM"].shape[0]),
-            "subset_sizes": {str(k): int(v) for k, v in zip(*np.unique(ws, return_counts=True))}}
+            "subset_sizes": {str(k): int(v) for k, v in zip(*np.unique(ws, return_counts=True))},
+            "count_rule": "code 1..100 after the LocalICGNQuadtree.m:153-169 bad-subset filter, "
+                          "within 0.01 px of FP64"}
+
+
+class CpuPass:
+    """The oracle (FP64 C++ restatement, OpenMP over subsets on all host cores)
+    running LocalICGNQuadtree over the whole mesh of a workload."""
+
+    def __init__(self, w):
+        from oracle import build as ob
+        ob.build_oracle()
+        from oracle import oracle as orc
+        self.orc = orc
+        self.w = w
+        self.f = w["f"].astype(np.float64)
+        self.g = w["g"].astype(np.float64)
+        self.Df = orc.funImgGradient(self.f, w["maskf"])
+        self.cores = os.cpu_count() or 1
+        orc.set_threads(self.cores)
+        self.out = None
+
+    def run(self):
+        w = self.w
+        t0 = time.perf_counter()
+        out = self.orc.LocalICGNQuadtree(w["U0"], w["coordinatesFEM"], self.Df, self.f, self.g,
+                                         w["winsize_list"], TOL)
+        dt = time.perf_counter() - t0
+        self.out = out
+        U, F, Hp, conv, badnum, mark = out
+        return dt, int(converged_rule(U, conv).sum())
+
+    def measure(self, runs, warm=1):
+        for _ in range(warm):
+            self.run()
+        ts, n = [], 0
+        for _ in range(runs):
+            dt, n = self.run()
+            ts.append(dt)
+        med = float(np.median(ts))
+        return {"value": n / med, "unit": UNIT, "cores": self.cores, "kind": "port",
+                "ms_median": 1e3 * med, "runs": runs, "converged": n,
+                "sample": "whole mesh (%d nodes) of %s, LocalICGNQuadtree with its bad-subset filter, FP64, "
+                          "OpenMP %d threads, median of %d runs" % (self.w["coordinatesFEM"].shape[0],
+                                                                     self.w["name"], self.cores, runs)}
 
 
 def run_reference(args, world, rank):
-    """CPU implementation of the path on the host cores (oracle port)."""
+    """CPU implementation of the path on the host cores (oracle port), on the
+    same workload, metric and counting rule as the GPU arm."""
     if rank != 0:
         return 0
-    from oracle import build as ob
-    ob.build_oracle()
-    from oracle import oracle as orc
     w = make_workload(args.workload)
-    f = w["f"].astype(np.float64)
-    g = w["g"].astype(np.float64)
-    Df = orc.funImgGradient(f, w["maskf"])
-    coords = w["coordinatesFEM"]
-    N = coords.shape[0]
-    cores = os.cpu_count() or 1
-    orc.set_threads(cores)
-    # bounded sample: every k-th node, about 4000 subsets per step
-    k = max(1, N // 4000)
-    idx = np.arange(0, N, k)
-    U0 = w["U0"].reshape(-1, 2)[idx].ravel()
-    cs = coords[idx]
-    wl = w["winsize_list"][idx]
+    cp = CpuPass(w)
     for _ in range(args.warmup):
-        orc.icgn6(U0, cs, Df, f, g, wl, TOL)
-    t0 = time.perf_counter()
-    conv_total = 0
+        cp.run()
+    ts, n = [], 0
     for _ in range(args.steps):
-        U, F, Hp, conv, mark = orc.icgn6(U0, cs, Df, f, g, wl, TOL)
-        conv_total += int(((conv >= 1) & (conv <= 100)).sum())
-    dt = time.perf_counter() - t0
-    val = conv_total / dt
-    sample = "%d of %d nodes of %s (every %d-th), FP64 IC-GN, %d OpenMP threads" % (
-        idx.size, N, args.workload, k, cores)
+        dt, n = cp.run()
+        ts.append(dt)
+    med = float(np.median(ts))
+    val = n / med
+    sample = "whole mesh (%d nodes) of %s every step, FP64 LocalICGNQuadtree with its bad-subset filter, " \
+             "%d OpenMP threads, median step of %d" % (w["coordinatesFEM"].shape[0], args.workload, cp.cores,
+                                                       args.steps)
     out = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+           "warmup": args.warmup, "ms_per_step": 1e3 * med, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "impl": "reference", "parallelism": "host threads", "precision": "FP64 (the oracle port)",
+           "ms_per_step_mean": 1e3 * float(np.mean(ts)),
            "config": workload_config(args.workload, w),
-           "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "cpu_baseline": {"value": val, "unit": UNIT, "cores": cp.cores, "kind": "port", "sample": sample},
            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
     return 0
@@ -300,58 +390,78 @@ class LocalRun:
 
         self.solve = solve
 
-
-def converged_within(Ub, cb, Up):
-    """Converged subsets of a batched result within TOLPX of the plain FP64 one."""
-    dU = np.abs(Ub - Up).reshape(-1, 2).max(axis=1)
-    return (cb >= 1) & (cb <= 100) & ~np.isnan(Ub[0::2]) & ~np.isnan(Up[0::2]) & (dU <= TOLPX)
+    def host(self):
+        return self.U.cpu().numpy(), self.F.cpu().numpy(), self.conv.cpu().numpy()
 
 
-def measure_c3(ctx, torch, flush, steps=5):
-    """The 2048^2 quadtree with hole (config C3): one LocalICGNQuadtree pass,
-    batched FP32 against the plain FP64 drop-in and the host CPU."""
+def timed_solves(torch, run, fr, prec, k, flush):
+    """k solves, each bracketed by CUDA events on the library's stream, with
+    the L2 flushed before each; returns per-call ms and the solver kernels' ms."""
+    ms, kern = [], []
+    for i in range(k):
+        flush.fill_(float(i))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run.solve(fr, prec)
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        kern.append(run.ctx.last_solver_ms())
+    return ms, kern
+
+
+def accuracy(Ub, Fb, cb, Ur, Fr, cr):
+    """Batched against an FP64 solution: max |du| and |dF| over the subsets
+    converged in both, and the share of equal result codes."""
+    both = (cb >= 1) & (cb <= 100) & (cr >= 1) & (cr <= 100) & ~np.isnan(Ub[0::2]) & ~np.isnan(Ur[0::2])
+    dU = np.abs(Ub - Ur).reshape(-1, 2).max(axis=1)
+    dF = np.abs(Fb - Fr).reshape(-1, 4).max(axis=1)
+    return {"max_abs_du_px_converged": float(np.max(dU[both])) if both.any() else None,
+            "max_abs_dF_converged": float(np.max(dF[both])) if both.any() else None,
+            "codes_equal_frac": float(np.mean(cb == cr)),
+            "within_0.01px_frac_of_both_converged": float(np.mean(dU[both] <= TOLPX)) if both.any() else None}
+
+
+def plain_roofline(flops, ms, fp64_peak):
+    a = flops / (ms * 1e-3) / 1e12
+    return {"bound": "fp64", "achieved": a, "peak": fp64_peak, "unit": "TFLOP/s", "frac": a / fp64_peak,
+            "peak_source": "cuBLAS DGEMM 4096^3, measured in this run (MEASURED_PEAKS.json has no FP64 figure)"}
+
+
+def measure_local_extra(ctx, torch, flush, name, steps=10, with_cpu=True):
+    """One LocalICGNQuadtree workload beside the headline: batched FP32 against
+    the plain FP64 drop-in and the CPU port, by the same rule."""
     from staqdic import _lib
-    w = make_workload("hole2048")
+    w = make_workload(name)
     run = LocalRun(ctx, w)
-
-    def timed(fr, prec, k):
-        ms = []
-        for i in range(k):
-            flush.fill_(float(i))
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            run.solve(fr, prec)
-            e1.record()
-            e1.synchronize()
-            ms.append(e0.elapsed_time(e1))
-        return float(np.mean(ms))
-
     run.solve(run.fr64, _lib.STDIC_PLAIN_F64)
     torch.cuda.synchronize()
-    Up, cp = run.U.cpu().numpy(), run.conv.cpu().numpy()
-    plain_ms = timed(run.fr64, _lib.STDIC_PLAIN_F64, 2)
-    plain_conv = int(((cp >= 1) & (cp <= 100) & ~np.isnan(Up[0::2])).sum())
+    Up, Fp, cp = run.host()
+    plain_ms, _ = timed_solves(torch, run, run.fr64, _lib.STDIC_PLAIN_F64, 2, flush)
+    plain_conv = int(converged_rule(Up, cp).sum())
     for _ in range(3):
         run.solve(run.fr32, _lib.STDIC_BATCHED_F32)
-    bat_ms = timed(run.fr32, _lib.STDIC_BATCHED_F32, steps)
-    Ub, cb = run.U.cpu().numpy(), run.conv.cpu().numpy()
-    n_conv = int(converged_within(Ub, cb, Up).sum())
-    out = {"workload": "hole2048: 2048x2048 plate with hole, Kirsch 2%% strain, quadtree, %d nodes" % run.N,
-           "value": n_conv / (bat_ms * 1e-3), "ms_per_step": bat_ms, "unit": UNIT,
-           "plain_fp64": {"value": plain_conv / (plain_ms * 1e-3), "ms_per_step": plain_ms},
-           "codes_equal_frac": float(np.mean(cb == cp))}
+    bat_ms, kern = timed_solves(torch, run, run.fr32, _lib.STDIC_BATCHED_F32, steps, flush)
+    Ub, Fb, cb = run.host()
+    n_conv = int(converged_rule(Ub, cb, Up).sum())
+    bms = float(np.mean(bat_ms))
+    out = {"workload": workload_config(name, w)["workload"], "nodes": run.N,
+           "value": n_conv / (bms * 1e-3), "ms_per_step": bms, "unit": UNIT, "converged": n_conv,
+           "solver_kernels_ms": float(np.mean(kern)),
+           "plain_fp64": {"value": plain_conv / (np.mean(plain_ms) * 1e-3), "ms_per_step": float(np.mean(plain_ms))},
+           "accuracy_vs_plain_fp64": accuracy(Ub, Fb, cb, Up, Fp, cp)}
     out["batched_over_plain"] = out["value"] / out["plain_fp64"]["value"]
-    cpu = cpu_baseline(w, "hole2048")
-    if cpu and cpu.get("value"):
+    if with_cpu:
+        cpu = guarded(lambda: CpuPass(w).measure(5))
         out["cpu_baseline"] = cpu
-        out["batched_over_cpu"] = out["value"] / cpu["value"]
-    out["admm"] = measure_admm(ctx, torch, run)
+        if cpu.get("value"):
+            out["batched_over_cpu"] = out["value"] / cpu["value"]
     return out
 
 
 def measure_admm(ctx, torch, run):
     """ADMM iterations (Subpb1 batched FP32, fill, Subpb2 FP64 PCG, strain, dual
-    update) on the C3 mesh after its local pass, through stdic_admm with
+    update) on the 2048^2 mesh after its local pass, through stdic_admm with
     device-resident state: the first iteration runs directly, the others
     replay one captured CUDA graph.  mu = 1e-3, beta = 1e-3 * step^2 * mu.
 
@@ -428,8 +538,8 @@ def admm_timing(ctx, torch, run, dirichlet_nodes):
 
 def measure_c5(ctx, torch, flush, steps=3):
     """16 deformed frames (rotation 2k degrees plus a crack opening) of one
-    1024^2 reference frame and quadtree mesh (config C5): one multi-frame
-    batched launch against the 16 frames one by one, device-resident inputs."""
+    1024^2 reference frame and quadtree mesh: one multi-frame batched launch
+    against the 16 frames one by one, device-resident inputs."""
     import ctypes
     from staqdic import _lib
     w = make_workload("series1024")
@@ -505,8 +615,8 @@ def measure_c5(ctx, torch, flush, steps=3):
 
 
 def measure_adjoint(ctx, torch, size=4096):
-    """Adjoint of the subset ZNSSD cost on the bumps field (config C4: 4096^2,
-    ws 32, step 16), FP32, both modes, with dg."""
+    """Adjoint of the subset ZNSSD cost on the bumps field (4096^2, ws 32,
+    step 16), FP32, both modes, with dg."""
     import staqdic
     w = make_workload("bumps4096", size=size)
     c = w["coordinatesFEM"]
@@ -534,19 +644,30 @@ def measure_adjoint(ctx, torch, size=4096):
     return out
 
 
+def guarded(fn, *args):
+    """One secondary measurement: its failure is reported in its own object and
+    leaves the headline line intact."""
+    try:
+        return fn(*args)
+    except Exception as e:  # pragma: no cover
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
 # ----------------------------------------------------------------------------
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="hole1024")
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the 2048^2 (C3) pass and the 4096^2 adjoint (C4) timing")
-    ap.add_argument("--only", choices=["c3", "admm", "adjoint", "c5"],
+                    help="skip the 1024^2 pass, the ADMM iterations, the adjoint and the multi-frame launch")
+    ap.add_argument("--only", choices=["c2", "admm", "adjoint", "c5"],
                     help="run one secondary measurement alone and print it (for profiling)")
+    ap.add_argument("--profile", action="store_true",
+                    help="only the headline workload's batched passes (warm-up + steps), for ncu captures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -563,6 +684,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
+    import ctypes
     import staqdic
     from staqdic import _lib
 
@@ -573,12 +695,12 @@ def main():
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     L = ctx.L
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     if args.only:
-        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
         if args.only == "admm":
-            res = measure_admm(ctx, torch, LocalRun(ctx, make_workload("hole2048")))
-        elif args.only == "c3":
-            res = measure_c3(ctx, torch, flush)
+            res = measure_admm(ctx, torch, LocalRun(ctx, make_workload(DEFAULT_WORKLOAD)))
+        elif args.only == "c2":
+            res = measure_local_extra(ctx, torch, flush, "hole1024", with_cpu=False)
         elif args.only == "adjoint":
             res = measure_adjoint(ctx, torch)
         else:
@@ -589,33 +711,25 @@ def main():
     w = make_workload(args.workload)
     run = LocalRun(ctx, w)
     W, H, N, ws_list = run.W, run.H, run.N, run.ws_list
-    fr32, fr64, solve = run.fr32, run.fr64, run.solve
-    U, F, conv = run.U, run.F, run.conv
-    gx32, gy32 = run.gx32, run.gy32
-    import ctypes
+    if args.profile:
+        for _ in range(args.warmup + args.steps):
+            run.solve(run.fr32, _lib.STDIC_BATCHED_F32)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": args.workload, "passes": args.warmup + args.steps}), flush=True)
+        ctx.close()
+        return 0
 
     # ---- plain FP64 drop-in: accuracy reference and the 'plain' throughput
-    solve(fr64, _lib.STDIC_PLAIN_F64)
+    run.solve(run.fr64, _lib.STDIC_PLAIN_F64)
     torch.cuda.synchronize()
-    U_plain = U.clone()
-    F_plain = F.clone()
-    conv_plain = conv.clone()
-    plain_ms = []
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    for _ in range(2):
-        flush.fill_(1.0)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        solve(fr64, _lib.STDIC_PLAIN_F64)
-        e1.record()
-        e1.synchronize()
-        plain_ms.append(e0.elapsed_time(e1))
-    plain_conv = int((((conv_plain >= 1) & (conv_plain <= 100)) & ~torch.isnan(U_plain[0::2])).sum())
+    U_plain, F_plain, conv_plain = run.host()
+    plain_ms, plain_kern = timed_solves(torch, run, run.fr64, _lib.STDIC_PLAIN_F64, 2, flush)
+    plain_conv = int(converged_rule(U_plain, conv_plain).sum())
     plain_value = plain_conv / (np.mean(plain_ms) * 1e-3)
 
     # ---- batched FP32: warm-up (the first call autotunes), then K timed steps
     for _ in range(args.warmup):
-        solve(fr32, _lib.STDIC_BATCHED_F32)
+        run.solve(run.fr32, _lib.STDIC_BATCHED_F32)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -623,33 +737,18 @@ def main():
     launches0 = ctx.launches
     sampler = ClockSampler(local)
     sampler.start()
-    step_ms, solver_ms = [], []
-    t_wall0 = time.perf_counter()
-    for _ in range(args.steps):
-        flush.fill_(float(len(step_ms)))
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        solve(fr32, _lib.STDIC_BATCHED_F32)
-        e1.record()
-        e1.synchronize()
-        step_ms.append(e0.elapsed_time(e1))
-        solver_ms.append(ctx.last_solver_ms())
+    sampler.region_start()
+    step_ms, solver_ms = timed_solves(torch, run, run.fr32, _lib.STDIC_BATCHED_F32, args.steps, flush)
     torch.cuda.synchronize()
-    t_wall = time.perf_counter() - t_wall0
+    sampler.region_end()
     clocks = sampler.stop()
     launches = ctx.launches - launches0
     if dist:
         dist.barrier()
 
-    # accuracy and the converged count of the last step
-    Uc, cc = U.cpu().numpy(), conv.cpu().numpy()
-    Fc = F.cpu().numpy()
-    Up, cp = U_plain.cpu().numpy(), conv_plain.cpu().numpy()
-    dU = np.abs(Uc - Up).reshape(-1, 2).max(axis=1)
-    ok = (cc >= 1) & (cc <= 100) & ~np.isnan(Uc[0::2]) & ~np.isnan(Up[0::2]) & (dU <= TOLPX)
-    n_conv = int(ok.sum())
-    total_ms = float(np.sum(step_ms))
-    mean_ms = total_ms / len(step_ms)
+    Uc, Fc, cc = run.host()
+    n_conv = int(converged_rule(Uc, cc, U_plain).sum())
+    mean_ms = float(np.mean(step_ms))
     if dist:
         mean_ms, n_conv_all = reduce_over_ranks(dist, mean_ms, n_conv, "cuda")
     else:
@@ -658,11 +757,10 @@ def main():
 
     # ---- end to end through the C ABI with pinned host buffers
     def pinned(a, dt):
-        t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dt).ravel(order="F"))).pin_memory()
-        return t
+        return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dt).ravel(order="F"))).pin_memory()
 
     hf, hg, hm = pinned(w["f"], np.float32), pinned(w["g"], np.float32), pinned(w["maskf"], np.uint8)
-    hgx, hgy = gx32.cpu().pin_memory(), gy32.cpu().pin_memory()
+    hgx, hgy = run.gx32.cpu().pin_memory(), run.gy32.cpu().pin_memory()
     hU0, hc, hw = pinned(w["U0"], np.float64), pinned(w["coordinatesFEM"], np.float64), pinned(ws_list, np.int32)
     oU = torch.empty(2 * N, dtype=torch.float64).pin_memory()
     oF = torch.empty(4 * N, dtype=torch.float64).pin_memory()
@@ -692,9 +790,7 @@ def main():
         t0 = time.perf_counter()
         solve_host()  # H2D copies, kernels, D2H copies, stream sync
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    oUn, ocn = oU.numpy(), oc.numpy()
-    dUe = np.abs(oUn - Up).reshape(-1, 2).max(axis=1)
-    n_conv_e2e = int(((ocn >= 1) & (ocn <= 100) & ~np.isnan(oUn[0::2]) & ~np.isnan(Up[0::2]) & (dUe <= TOLPX)).sum())
+    n_conv_e2e = int(converged_rule(oU.numpy(), oc.numpy(), U_plain).sum())
     e2e_mean = float(np.mean(e2e_ms))
     if dist:
         e2e_mean, n_conv_e2e = reduce_over_ranks(dist, e2e_mean, n_conv_e2e, "cuda")
@@ -707,36 +803,34 @@ def main():
 
     # ---- roofline of the dominant kernel (the batched persistent IC-GN)
     peaks, src = measured_peaks()
-    fp32_peak = fp32_peak_tflops(torch)
+    fp32_peak = gemm_peak_tflops(torch, torch.float32, 8192)
+    fp64_peak = gemm_peak_tflops(torch, torch.float64, 4096)
     flops = float(flops_per_subset(cc, ws_list).sum())
     sv = [s for s in solver_ms if s > 0]
     kern_ms = float(np.mean(sv)) if sv else mean_ms
     achieved = flops / (kern_ms * 1e-3) / 1e12
     alg_bytes = (2 * 4 * W * H + W * H + 2 * 4 * (W - 6) * (H - 6) + N * (16 + 16 + 4 + 16 + 32 + 168 + 4 + 1))
-    traffic = traffic_from_profiles()
+    traffic, traffic_src = traffic_from_profile(args.workload)
     roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp32_peak,
-                "traffic": traffic,
+                "frac": achieved / fp32_peak, "traffic": traffic, "traffic_source": traffic_src,
                 "peak_source": "cuBLAS SGEMM 8192^3 with TF32 off, measured in this run "
                                "(MEASURED_PEAKS.json has no FP32 CUDA-core figure)",
-                "flops_per_launch": flops, "kernel_ms": kern_ms}
+                "flops_per_launch": flops, "kernel_ms": kern_ms,
+                "kernel": "icgn_batched_kernel set-up + factor6_kernel + icgn_batched_kernel iterations"}
     roofline_hbm = {"bound": "hbm", "achieved": alg_bytes / (kern_ms * 1e-3) / 1e9,
                     "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                     "frac": alg_bytes / (kern_ms * 1e-3) / 1e9 / peaks.get("hbm_gbs"),
                     "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
                     "peak_source": src}
-
-    both_conv = (cc >= 1) & (cc <= 100) & (cp >= 1) & (cp <= 100)
-    dF = np.abs(Fc - F_plain.cpu().numpy()).reshape(-1, 4).max(axis=1)
-    cpu = None
-    if world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(w, args.workload)
+    plain_flops = float(flops_per_subset(conv_plain, ws_list).sum())
+    pk = [s for s in plain_kern if s > 0]
+    plain_rf = plain_roofline(plain_flops, float(np.mean(pk)) if pk else float(np.mean(plain_ms)), fp64_peak)
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": workload_config(args.workload, w),
-           "precision": "batched FP32 (FMA sums, FP64 Hessian inverses)",
+           "precision": "batched FP32 (FMA sums, FP64 Hessian inverses applied in double-float)",
            "l2": "flushed between timed steps (256 MiB write)",
            "parallelism": "replicas" if world > 1 else "single GPU",
            "clocks": clocks,
@@ -746,18 +840,30 @@ def main():
            "roofline": roofline,
            "roofline_hbm": roofline_hbm,
            "plain_fp64": {"value": plain_value, "ms_per_step": float(np.mean(plain_ms)),
-                          "converged": plain_conv},
+                          "converged": plain_conv, "roofline": plain_rf},
            "batched_over_plain": value / plain_value if plain_value > 0 else None,
-           "accuracy": {"converged": n_conv, "nodes": N,
-                        "max_abs_du_px_converged": float(np.nanmax(dU[both_conv])) if both_conv.any() else None,
-                        "max_abs_dF_converged": float(np.nanmax(dF[both_conv])) if both_conv.any() else None,
-                        "codes_equal_frac": float(np.mean(cc == cp))},
-           "wall_s_timed": t_wall}
-    if cpu:
-        out["cpu_baseline"] = cpu
-        out["batched_over_cpu"] = value / cpu["value"] if cpu.get("value") else None
+           "accuracy": dict(converged=n_conv, nodes=N,
+                            **accuracy(Uc, Fc, cc, U_plain, F_plain, conv_plain))}
+    if world == 1 and not args.no_cpu_baseline:
+        cp = guarded(CpuPass, w)
+        if isinstance(cp, CpuPass):
+            cpu = guarded(cp.measure, 5)
+            out["cpu_baseline"] = cpu
+            if cpu.get("value"):
+                out["batched_over_cpu"] = value / cpu["value"]
+                Uo, Fo, _, co, badno, _ = cp.out
+                out["accuracy_vs_fp64_oracle"] = dict(
+                    converged_batched_within_0_01px=int(converged_rule(Uc, cc, Uo).sum()),
+                    badnum_oracle=int(badno), **accuracy(Uc, Fc, cc, Uo, Fo, co))
+                dpo = np.abs(U_plain - Uo).reshape(-1, 2).max(axis=1)
+                both = (co >= 1) & (co <= 100) & ~np.isnan(Uo[0::2])
+                out["accuracy_vs_fp64_oracle"]["plain_max_abs_du_px"] = float(np.nanmax(dpo[both]))
+                out["accuracy_vs_fp64_oracle"]["plain_codes_equal_frac"] = float(np.mean(conv_plain == co))
+        else:
+            out["cpu_baseline"] = cp
     if world == 1 and not args.no_extras:
-        out["c3"] = guarded(measure_c3, ctx, torch, flush)
+        out["c2"] = guarded(measure_local_extra, ctx, torch, flush, "hole1024")
+        out["admm"] = guarded(measure_admm, ctx, torch, run)
         out["adjoint_c4"] = guarded(measure_adjoint, ctx, torch)
         out["c5"] = guarded(measure_c5, ctx, torch, flush)
     print(json.dumps(out), flush=True)
@@ -765,50 +871,6 @@ def main():
         dist.destroy_process_group()
     ctx.close()
     return 0
-
-
-def guarded(fn, *args):
-    """One secondary measurement: its failure is reported in its own object and
-    leaves the headline line intact."""
-    try:
-        return fn(*args)
-    except Exception as e:  # pragma: no cover
-        return {"error": "%s: %s" % (type(e).__name__, e)}
-
-
-def cpu_baseline(w, name):
-    """The oracle (FP64 C++ restatement, OpenMP on all host cores) on a bounded
-    sample of the same workload, about 10-20 s of CPU work."""
-    try:
-        from oracle import build as ob
-        ob.build_oracle()
-        from oracle import oracle as orc
-    except Exception as e:  # pragma: no cover
-        return {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                "sample": "oracle unavailable: %s" % e}
-    f = w["f"].astype(np.float64)
-    g = w["g"].astype(np.float64)
-    Df = orc.funImgGradient(f, w["maskf"])
-    coords = w["coordinatesFEM"]
-    N = coords.shape[0]
-    cores = os.cpu_count() or 1
-    orc.set_threads(cores)
-    k = max(1, N // 4000)
-    idx = np.arange(0, N, k)
-    U0 = w["U0"].reshape(-1, 2)[idx].ravel()
-    cs = coords[idx]
-    wl = w["winsize_list"][idx]
-    orc.icgn6(U0, cs, Df, f, g, wl, TOL)
-    t0 = time.perf_counter()
-    nconv, reps = 0, 0
-    while reps < 20 and (time.perf_counter() - t0) < 10.0:
-        U, F, Hp, conv, mark = orc.icgn6(U0, cs, Df, f, g, wl, TOL)
-        nconv += int(((conv >= 1) & (conv <= 100)).sum())
-        reps += 1
-    dt = time.perf_counter() - t0
-    return {"value": nconv / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d of %d nodes of %s (every %d-th) x %d repeats, FP64, OpenMP %d threads" % (
-                idx.size, N, name, k, reps, cores)}
 
 
 if __name__ == "__main__":

@@ -64,9 +64,11 @@ enum { STDIC_F64 = 0, STDIC_F32 = 1 };
 /* precision/form of the IC-GN solvers */
 enum {
   STDIC_PLAIN_F64 = 0,   /* one subset per CTA, FP64, reproduces the reference */
-  STDIC_BATCHED_F32 = 1  /* persistent kernel over a size-sorted queue, FP32
-                            interpolation/residual/Hessian sums with FP64
-                            cross-thread reduction and FP64 solves */
+  STDIC_BATCHED_F32 = 1  /* persistent kernel over a size-sorted queue: FP32
+                            interpolation and residuals, per-lane FP32 FMA sums
+                            reduced across lanes in FP32, the 6x6 (2x2) system
+                            factorised and inverted in FP64 and applied in
+                            double-float arithmetic */
 };
 
 typedef struct stdic_ctx stdic_ctx;
@@ -94,6 +96,12 @@ const char* stdic_last_error(const stdic_ctx* ctx);
 /* Number of kernels this context launched since creation (instrumentation;
  * no counterpart in the reference). */
 long long stdic_kernel_launches(const stdic_ctx* ctx);
+/* Bound, in polls, of every grid-barrier wait of the cooperative Subpb2 PCG
+ * run by this context (stdic_subpb2, stdic_admm); 0 restores the default of
+ * 2^24.  A wait that runs out makes the call return STDIC_E_TIMEOUT and leaves
+ * the context usable.  Instrumentation and failure-detection testing; no
+ * counterpart in the reference. */
+int stdic_ctx_set_wait_limit(stdic_ctx* ctx, long long polls);
 /* Device time in ms of the last IC-GN solver kernel (plain or batched), from
  * CUDA events on the launching stream; -1 if none ran.  Waits for that kernel.
  * Instrumentation; no counterpart in the reference. */
@@ -267,9 +275,11 @@ int stdic_icgn_adjoint(stdic_ctx* ctx, const stdic_frame* fr, const double* coor
  * (NULL: the default stream) and returns after that stream has finished it.
  * iters (host, may be NULL) receives the PCG count; err (may be NULL) receives
  * a message of at most err_len bytes.  Two calls in flight on one device at
- * once race on the shared array: serialise them.  The first call on each
- * device looks the array up (cudaGetSymbolAddress): make it before any stream
- * capture begins. */
+ * once race on the shared array: serialise them.  Every call looks the array's
+ * address up (cudaGetSymbolAddress) in the current device's context, so a
+ * context torn down and created again is followed; the first call on a device
+ * may load the module.  The call synchronises its stream, so it is never
+ * capturable: on a capturing stream it returns STDIC_E_UNSUPPORTED. */
 int stdic_subpb2_noalloc(const double* coords, int N, const int32_t* elems, int E,
                          const int32_t* dirichlet, int nd, const double* neumann, int nn,
                          int gauss_order, double beta, double mu, const double* U,

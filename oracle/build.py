@@ -15,7 +15,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("STAQDIC_REFERENCE", "/root/reference")
+# The STAQ-DIC checkout whose ba_interp2.cpp is compiled: STAQDIC_REFERENCE,
+# else the read-only mount where this recipe's build environment keeps it.
+# Where neither exists the reference checker is simply not built.
+REF_SRC = os.environ.get("STAQDIC_REFERENCE") or "/root/reference"
 
 CXXFLAGS = ["-O3", "-fPIC", "-shared", "-ffp-contract=off", "-std=c++17"]
 

@@ -212,7 +212,7 @@ __global__ void k_sub(const double* __restrict__ a, const double* __restrict__ b
 
 int grid_for(long long n, int threads) {
   long long b = (n + threads - 1) / threads;
-  return (int)std::max<long long>(1, std::min<long long>(b, 152 * 8));
+  return (int)std::max<long long>(1, std::min<long long>(b, 8ll * current_sm_count()));
 }
 
 }  // namespace

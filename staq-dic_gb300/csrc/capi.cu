@@ -36,6 +36,7 @@ struct stdic_ctx {
   std::map<std::tuple<int, int, int, int>, int> tune;
   int tuning = 1;
   bool capturing = false;  // the stream is being captured into a CUDA graph
+  long long wait_limit = 0;  // polls of a PCG grid-barrier wait (0: the default)
 };
 
 namespace {
@@ -228,6 +229,12 @@ int stdic_ctx_set_stream(stdic_ctx* c, void* s) {
 const char* stdic_last_error(const stdic_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
 long long stdic_kernel_launches(const stdic_ctx* c) { return c ? c->launches : 0; }
+
+int stdic_ctx_set_wait_limit(stdic_ctx* c, long long polls) {
+  if (!c || polls < 0) return STDIC_E_ARG;
+  c->wait_limit = polls;
+  return STDIC_OK;
+}
 
 double stdic_last_solver_ms(stdic_ctx* c) {
   if (!c || !c->solver_timed) return -1.0;
@@ -531,13 +538,16 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
   const int nb = Ntot <= 0 ? 0 : (int)std::ceil(std::log2((double)Ntot));
   const auto key = std::make_tuple(nb, b.a.npx_max, (int)two, b.frames);
   auto it = c->tune.find(key);
+  if (it == c->tune.end() && c->capturing) {
+    // no timing inside a capture: the first shape (or the fixed one) for this
+    // launch only, not cached, so the next uncaptured call still tunes
+    const int pick = tune_pick();
+    return launch(cands[pick >= 0 ? std::min(pick, (int)cands.size() - 1) : 0]);
+  }
   if (it == c->tune.end()) {
     int best = 0;
     const int pick = tune_pick();
-    if (c->capturing) {
-      // no timing inside a capture: the first shape, or the fixed one
-      best = pick >= 0 ? std::min(pick, (int)cands.size() - 1) : 0;
-    } else if (pick >= 0) {
+    if (pick >= 0) {
       best = std::min(pick, (int)cands.size() - 1);
     } else if (c->tuning && Ntot > 0 && cands.size() > 1) {
       float bt = 1e30f;
@@ -1028,6 +1038,7 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
   s2.coords = dcoords; s2.N = N; s2.elems = delems; s2.E = E; s2.dirichlet = ddir; s2.nd = nd;
   s2.neumann = nullptr; s2.nn = 0; s2.gauss_order = 2; s2.beta = beta; s2.mu = mu; s2.alpha = 0.0;
   s2.winstepsize = 1.0; s2.U = oU1; s2.F = F1; s2.tol = 1e-10; s2.maxit = 10000; s2.Uhat = oU2;
+  s2.spin_limit = c->wait_limit;
 
   auto body = [&]() -> int {
     int r = STDIC_OK;
@@ -1154,6 +1165,7 @@ int stdic_subpb2(stdic_ctx* c, const double* coords, int N, const int32_t* elems
   a.beta = beta; a.mu = mu; a.alpha = alpha; a.winstepsize = winstepsize;
   a.tol = tol > 0 ? tol : 1e-10;
   a.maxit = maxit > 0 ? maxit : 10000;
+  a.spin_limit = c->wait_limit;
   if (N > 0) {
     long long nl = 0;
     cudaError_t e = stdic::run_subpb2(a, wsp, c->scal + 2, c->scald, c->scal + 3, c->stream, &nl);

@@ -6,6 +6,10 @@
 
 namespace stdic {
 
+// SM count of the current device (queried once per device ordinal; 152 on
+// GB300), for grid-stride launches sized as a multiple of the SMs.
+int current_sm_count();
+
 // Arguments of the IC-GN kernels (6-DOF first pass and 2-DOF Subpb1).
 struct IcgnArgs {
   const void* f;
@@ -187,6 +191,9 @@ struct Subpb2Args {
   double tol;
   int maxit;
   double* Uhat;
+  // polls a PCG block waits at a grid barrier before it gives up with status
+  // 2 (STDIC_E_TIMEOUT); 0 takes the default of 2^24
+  long long spin_limit;
 };
 // workspace: caller-provided device memory of subpb2_workspace_bytes(N, E)
 size_t subpb2_workspace_bytes(int N, int E);

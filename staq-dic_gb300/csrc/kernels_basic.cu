@@ -43,7 +43,8 @@ cudaError_t launch_interp(const void* F, long long M, long long N, long long P, 
   if (n <= 0) return cudaSuccess;
   const int threads = 256;
   long long blocks = (n + threads - 1) / threads;
-  if (blocks > 152 * 32) blocks = 152 * 32;
+  const long long cap = 32ll * current_sm_count();
+  if (blocks > cap) blocks = cap;
   if (dtype == 0)
     interp_kernel<double><<<(int)blocks, threads, 0, s>>>((const double*)F, M, N, P,
                                                           (const double*)X, (const double*)Y, n,
@@ -103,7 +104,8 @@ __global__ void __launch_bounds__(256) gradient_kernel(const REAL* __restrict__ 
 // completing on an mbarrier.  The copy starts at the tile origin, whose x is a
 // multiple of 32 elements (TMA's 16-byte rule); elements beyond the image are
 // filled with zeros by the copy.  The wait is bounded: after 2^24 polls the
-// CTA sets *err and leaves its outputs unwritten.
+// CTA sets *err, polls once more for a bounded interval so that it does not
+// exit with the copy in flight, and leaves its outputs unwritten.
 template <class REAL>
 __global__ void __launch_bounds__(256) gradient_tma_kernel(const __grid_constant__ CUtensorMap tmap,
                                                            const uint8_t* __restrict__ mask, int W,
@@ -129,16 +131,24 @@ __global__ void __launch_bounds__(256) gradient_tma_kernel(const __grid_constant
         ::"r"(dst), "l"(reinterpret_cast<unsigned long long>(&tmap)), "r"(bx), "r"(by), "r"(sbar)
         : "memory");
   }
-  bool ok = false;
-  for (int it = 0; it < (1 << 24) && !ok; ++it) {
-    unsigned done;
-    asm volatile(
-        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-        : "=r"(done) : "r"(sbar), "r"(0u) : "memory");
-    ok = done != 0;
-  }
-  if (!ok) {
+  auto wait = [&](int polls) {
+    bool d = false;
+    for (int it = 0; it < polls && !d; ++it) {
+      unsigned done;
+      asm volatile(
+          "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+          : "=r"(done) : "r"(sbar), "r"(0u) : "memory");
+      d = done != 0;
+    }
+    return d;
+  };
+  if (!wait(1 << 24)) {
+    // Last resort: the copy has not landed after 2^24 polls.  The error is
+    // recorded, and the CTA keeps polling for a second bounded interval so
+    // that it does not leave while the copy may still be writing its shared
+    // memory; its outputs stay unwritten either way.
     if (threadIdx.x == 0 && err) atomicExch(err, 1);
+    wait(1 << 24);
     return;
   }
   const int lx = threadIdx.x % TX, ly = threadIdx.x / TX;
@@ -510,7 +520,7 @@ cudaError_t launch_badpoints(int32_t* conv, int N, double* U, double* F, int two
   if (N <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(tmp_dev, 0, 5 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  const int blocks = (int)std::min<long long>(((long long)N + 255) / 256, 152 * 4);
+  const int blocks = (int)std::min<long long>(((long long)N + 255) / 256, 4ll * current_sm_count());
   badpoints_stats_kernel<<<blocks, 256, 0, s>>>(conv, N, tmp_dev);
   badpoints_apply_kernel<<<blocks, 256, 0, s>>>(conv, N, U, F, two_dof, tmp_dev, badnum_dev);
   return cudaGetLastError();
@@ -523,10 +533,28 @@ __global__ void to_f32_kernel(const double* __restrict__ in, float* __restrict__
     out[k] = (float)in[k];
 }
 
+int current_sm_count() {
+  static int cached[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 152;
+  }
+  if (dev >= 0 && dev < 64 && cached[dev] > 0) return cached[dev];
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    n = 152;
+  }
+  if (dev >= 0 && dev < 64) cached[dev] = n;
+  return n;
+}
+
 cudaError_t launch_to_f32(const double* in, float* out, long long n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   long long blocks = (n + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  const long long cap = 16ll * current_sm_count();
+  if (blocks > cap) blocks = cap;
   to_f32_kernel<<<(int)blocks, 256, 0, s>>>(in, out, n);
   return cudaGetLastError();
 }

@@ -397,7 +397,9 @@ struct PcgArgs {
   int* status;
 };
 
-STDIC_DEV bool grid_barrier(int* count, volatile int* gen, int nblocks, int* status) {
+// Bounded grid barrier: a block that waits longer than `limit` polls sets
+// *status = 2 and every block leaves at its next barrier check.
+STDIC_DEV bool grid_barrier(int* count, volatile int* gen, int nblocks, int* status, long long limit) {
   __syncthreads();
   if (threadIdx.x == 0) {
     const int g = *gen;
@@ -409,7 +411,7 @@ STDIC_DEV bool grid_barrier(int* count, volatile int* gen, int nblocks, int* sta
     } else {
       long long spins = 0;
       while (*gen == g) {
-        if (++spins > kSpinLimit) { atomicExch(status, 2); break; }
+        if (++spins > limit) { atomicExch(status, 2); break; }
         __nanosleep(64);
       }
     }
@@ -458,6 +460,7 @@ __global__ void __launch_bounds__(256) k_pcg(PcgArgs P) {
   const int nb = gridDim.x;
   int* cnt = &w.misc[2];
   int* gen = &w.misc[3];
+  const long long spin_limit = a.spin_limit > 0 ? a.spin_limit : kSpinLimit;
   const int tid0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
   // invalid node index (misc[4]) or a node in more than kMaxElemPerNode
   // elements (misc[5]): report and stop before any barrier
@@ -482,7 +485,7 @@ __global__ void __launch_bounds__(256) k_pcg(PcgArgs P) {
     v[2] += ru * ru; v[3] += rv * rv;            // |b|^2
   }
   block_partials(v, 4, part0, red);
-  if (!grid_barrier(cnt, gen, nb, P.status)) return;
+  if (!grid_barrier(cnt, gen, nb, P.status, spin_limit)) return;
   double t0[4];
   totals(part0, 4, t0, red);
   double rz[2] = {t0[0], t0[1]};
@@ -509,7 +512,7 @@ __global__ void __launch_bounds__(256) k_pcg(PcgArgs P) {
       q[0] += w.p[n] * su; q[1] += w.p[N + n] * sv;
     }
     block_partials(q, 2, part1, red);
-    if (!grid_barrier(cnt, gen, nb, P.status)) return;
+    if (!grid_barrier(cnt, gen, nb, P.status, spin_limit)) return;
     double pAp[2];
     totals(part1, 2, pAp, red);
     double al[2];
@@ -528,7 +531,7 @@ __global__ void __launch_bounds__(256) k_pcg(PcgArgs P) {
       }
     }
     block_partials(s, 4, part2, red);
-    if (!grid_barrier(cnt, gen, nb, P.status)) return;
+    if (!grid_barrier(cnt, gen, nb, P.status, spin_limit)) return;
     double t[4];
     totals(part2, 4, t, red);
     double be[2];
@@ -545,7 +548,7 @@ __global__ void __launch_bounds__(256) k_pcg(PcgArgs P) {
         w.p[k] = w.z[k] + be[c] * w.p[k];
       }
     }
-    if (!grid_barrier(cnt, gen, nb, P.status)) return;
+    if (!grid_barrier(cnt, gen, nb, P.status, spin_limit)) return;
   }
   // Uhat: solution on free nodes, U on Dirichlet nodes, 0 elsewhere
   for (int n = tid0; n < N; n += stride) {
@@ -574,7 +577,8 @@ cudaError_t run_subpb2(const Subpb2Args& a, void* workspace, int* iters_dev, dou
   if (a.N <= 0) return cudaSuccess;
   Ws w = carve(workspace, a.N, a.E, nullptr);
   const int T = 256;
-  auto blocks = [&](long long n) { return (int)std::min<long long>((n + T - 1) / T, 152 * 8); };
+  const long long max_blocks = 8ll * current_sm_count();
+  auto blocks = [&](long long n) { return (int)std::min<long long>((n + T - 1) / T, max_blocks); };
   long long nl = 0;
   if (phase & kSubpb2Structure) {
     // node graph, CSR pattern, Dirichlet flags and reference tables: they

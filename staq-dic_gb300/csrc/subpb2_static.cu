@@ -22,14 +22,18 @@
 //   * one array per device: two calls in flight on one device at the same time
 //     (two streams, two host threads) share it and corrupt each other's result,
 //     so the caller serialises them;
-//   * the first call on each device looks the array's address up with
-//     cudaGetSymbolAddress (this may load the module) and caches it; make that
-//     first call before any stream capture begins.
+//   * every call looks the array's address up with cudaGetSymbolAddress while
+//     the caller's device is current (the first call on a device may load the
+//     module).  Nothing is cached across calls, so a context that was torn down
+//     and created again (cudaDeviceReset, a primary-context release), which can
+//     reload the module at another address, is picked up by the next call;
+//   * the call ends with a read-back of its status and a stream synchronise,
+//     so it can never be captured into a CUDA graph: on a stream that is being
+//     captured it returns STDIC_E_UNSUPPORTED without touching the stream.
 #include <cuda_runtime.h>
 
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/staqdic.h"
 #include "kernels.h"
@@ -38,13 +42,9 @@ namespace {
 
 constexpr size_t kStaticScratchBytes = (size_t)16 << 20;  // 16 MiB
 constexpr size_t kHeaderBytes = 256;                       // device scalars, then the workspace
-constexpr int kMaxDevices = 64;
 
 // [0, 256): int iters, int status, double resid; [256, end): Subpb2 workspace
 __device__ __align__(256) unsigned char g_subpb2_scratch[kStaticScratchBytes];
-
-std::mutex g_lookup_mu;
-unsigned char* g_scratch_addr[kMaxDevices] = {};
 
 void put_err(char* err, int err_len, const char* msg) {
   if (err && err_len > 0) {
@@ -103,21 +103,25 @@ extern "C" int stdic_subpb2_noalloc(const double* coords, int N, const int32_t* 
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_err(err, err_len, "cudaGetDevice", e);
-  if (dev < 0 || dev >= kMaxDevices) {
-    put_err(err, err_len, "stdic_subpb2_noalloc: device ordinal above 63");
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(s, &cap);
+  if (e != cudaSuccess) return cuda_err(err, err_len, "cudaStreamIsCapturing", e);
+  if (cap != cudaStreamCaptureStatusNone) {
+    put_err(err, err_len,
+            "stdic_subpb2_noalloc: the stream is being captured; this entry synchronises its "
+            "stream and cannot be part of a CUDA graph");
     return STDIC_E_UNSUPPORTED;
   }
+  // The array's device address in the current device's context, looked up on
+  // every call (a host-side table lookup once the module is loaded).  The
+  // symbol itself is only a host-side stand-in and is never passed to a kernel.
   unsigned char* base = nullptr;
   {
-    // one lookup per device, made while that device is current
-    std::lock_guard<std::mutex> lk(g_lookup_mu);
-    if (!g_scratch_addr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_subpb2_scratch);
-      if (e != cudaSuccess) return cuda_err(err, err_len, "cudaGetSymbolAddress", e);
-      g_scratch_addr[dev] = (unsigned char*)p;
-    }
-    base = g_scratch_addr[dev];
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_subpb2_scratch);
+    if (e != cudaSuccess) return cuda_err(err, err_len, "cudaGetSymbolAddress", e);
+    base = (unsigned char*)p;
   }
 
   const void* arrays[] = {coords, elems, dirichlet, neumann, U, F, Uhat};
@@ -130,7 +134,6 @@ extern "C" int stdic_subpb2_noalloc(const double* coords, int N, const int32_t* 
     }
   }
 
-  cudaStream_t s = (cudaStream_t)cuda_stream;
   int* iters_dev = (int*)base;
   int* status_dev = (int*)base + 1;
   double* resid_dev = (double*)(base + 8);

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder from the reference checkout.
 
 Run here (where the reference checkout and oracle/_ref exist):
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/STAQ-DIC   (or STAQDIC_REFERENCE=...)
 
 Writes
   circular_hole_pair.npz  the shipped 400x400 plate-with-hole pair (frames 000
@@ -112,4 +112,8 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("STAQDIC_REFERENCE")
+    if not ref or not os.path.isdir(ref):
+        sys.exit("make_golden.py: give the STAQ-DIC checkout as the first argument or in "
+                 "STAQDIC_REFERENCE (got %r)" % (ref,))
+    main(ref)

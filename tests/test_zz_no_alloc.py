@@ -112,3 +112,106 @@ def test_noalloc_rejects_oversize_and_host_memory(torch_cuda, meshes):
                                 1e-3, 1e-3, p, p, 0.0, 16.0, 1e-10, 0, p, None, None, err, len(err))
     assert rc == _lib.STDIC_E_ARG
     assert b"device memory" in err.value
+
+
+def test_noalloc_reports_invalid_node_index(torch_cuda, meshes):
+    """An element that names a node outside 1..N is reported as STDIC_E_ARG by
+    the solve itself (the set-up kernels skip the index; the PCG stops before
+    its first grid barrier)."""
+    from staqdic import _lib
+    torch = torch_cuda
+    L = _lib.load()
+    m = dict(meshes[1])
+    el = np.array(m["elems"], dtype=np.int32, copy=True)
+    el[3, 2] = m["coords"].shape[0] + 5
+    m["elems"] = el
+    N = m["coords"].shape[0]
+    d = {k: _dev(torch, m[k], np.float64) for k in ("coords", "U", "F")}
+    eld = _dev(torch, el, np.int32)
+    di = _dev(torch, m["dirichlet"], np.int32)
+    Uhat = torch.zeros(2 * N, dtype=torch.float64, device="cuda")
+    err = ctypes.create_string_buffer(256)
+    stream = torch.cuda.Stream()
+    rc = L.stdic_subpb2_noalloc(d["coords"].data_ptr(), N, eld.data_ptr(), el.shape[0], di.data_ptr(),
+                                di.numel(), None, 0, 2, 1e-2, 1e-3, d["U"].data_ptr(), d["F"].data_ptr(),
+                                0.0, 16.0, 1e-10, 0, Uhat.data_ptr(), None, stream.cuda_stream, err, len(err))
+    assert rc == _lib.STDIC_E_ARG
+    assert b"invalid node index" in err.value
+    # the array is usable again right after
+    Un, itn = _noalloc(torch, L, meshes[1], stream)
+    assert np.all(np.isfinite(Un)) and itn > 0
+
+
+def test_noalloc_matches_direct_sparse_solve(torch_cuda, oracle, meshes):
+    """The oracle's direct solve (SuperLU on A(Free,Free)) against the
+    no-allocation entry, to the PCG tolerance (1e-6 px)."""
+    from staqdic import _lib
+    torch = torch_cuda
+    L = _lib.load()
+    m = meshes[0]
+    Un, _ = _noalloc(torch, L, m, torch.cuda.Stream())
+    Uo = oracle.Subpb2Quadtree(m["coords"], m["elems"], m["dirichlet"], None, m["gauss"], m["beta"],
+                               m["mu"], m["U"], m["F"], m["alpha"], m["step"])
+    assert np.max(np.abs(Un - Uo)) < 1e-6
+
+
+_RESET_SCRIPT = r'''
+import ctypes, sys
+import numpy as np
+sys.path[:0] = sys.argv[1:3]
+from staqdic import _lib, workloads
+L = _lib.load()
+rt = ctypes.CDLL("libcudart.so.13")
+w = workloads.uniform256(seed=0)
+coords = np.asfortranarray(w["coordinatesFEM"], np.float64)
+elems = np.asfortranarray(w["elementsFEM"], np.int32)
+N, E = coords.shape[0], elems.shape[0]
+rng = np.random.default_rng(3)
+U = rng.normal(0, 0.5, 2 * N)
+F = rng.normal(0, 0.01, 4 * N)
+dirichlet = np.array([1, 2, 3, 100], np.int32)
+
+def dev(a):
+    p = ctypes.c_void_p()
+    assert rt.cudaMalloc(ctypes.byref(p), ctypes.c_size_t(a.nbytes)) == 0
+    assert rt.cudaMemcpy(p, a.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(a.nbytes), 1) == 0
+    return p
+
+def solve():
+    assert rt.cudaSetDevice(0) == 0
+    ptrs = [dev(np.ascontiguousarray(a.ravel(order="F"))) for a in (coords, elems, dirichlet, U, F)]
+    out = np.zeros(2 * N)
+    po = dev(out)
+    err = ctypes.create_string_buffer(256)
+    it = ctypes.c_int(0)
+    rc = L.stdic_subpb2_noalloc(ptrs[0], N, ptrs[1], E, ptrs[2], dirichlet.size, None, 0, 2, 1e-2, 1e-3,
+                                ptrs[3], ptrs[4], 0.0, 16.0, 1e-10, 0, po, ctypes.byref(it), None, err, 256)
+    assert rc == 0, err.value
+    assert rt.cudaMemcpy(out.ctypes.data_as(ctypes.c_void_p), po, ctypes.c_size_t(out.nbytes), 2) == 0
+    for p in ptrs + [po]:
+        rt.cudaFree(p)
+    return out, it.value
+
+a, ia = solve()
+assert rt.cudaDeviceReset() == 0
+b, ib = solve()
+assert np.all(np.isfinite(a)) and ia > 0
+assert np.max(np.abs(a - b)) < 1e-7 and abs(ia - ib) <= 2
+print("reset ok")
+'''
+
+
+def test_noalloc_after_context_reset(torch_cuda):
+    """A context torn down (cudaDeviceReset ends only this process's own
+    context) and created again reloads the module; the next call looks the
+    array up again and solves as before.  Run in a child process so that the
+    reset does not touch the test session's context."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    r = subprocess.run([sys.executable, "-c", _RESET_SCRIPT, os.path.join(root, "staq-dic_gb300"), root],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "reset ok" in r.stdout

@@ -666,8 +666,8 @@ def main():
                     help="skip the 1024^2 pass, the ADMM iterations, the adjoint and the multi-frame launch")
     ap.add_argument("--only", choices=["c2", "admm", "adjoint", "c5"],
                     help="run one secondary measurement alone and print it (for profiling)")
-    ap.add_argument("--profile", action="store_true",
-                    help="only the headline workload's batched passes (warm-up + steps), for ncu captures")
+    ap.add_argument("--profile", choices=["batched", "plain"],
+                    help="only the headline workload's passes of one form (warm-up + steps), for ncu captures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -712,10 +712,14 @@ def main():
     run = LocalRun(ctx, w)
     W, H, N, ws_list = run.W, run.H, run.N, run.ws_list
     if args.profile:
+        fr, prec = (run.fr32, _lib.STDIC_BATCHED_F32) if args.profile == "batched" else (run.fr64, _lib.STDIC_PLAIN_F64)
+        ms = []
         for _ in range(args.warmup + args.steps):
-            run.solve(run.fr32, _lib.STDIC_BATCHED_F32)
+            run.solve(fr, prec)
+            ms.append(ctx.last_solver_ms())
         torch.cuda.synchronize()
-        print(json.dumps({"profile": args.workload, "passes": args.warmup + args.steps}), flush=True)
+        print(json.dumps({"profile": args.workload, "form": args.profile, "passes": args.warmup + args.steps,
+                          "solver_ms": ms}), flush=True)
         ctx.close()
         return 0
 

@@ -24,7 +24,8 @@ struct stdic_ctx {
   size_t ws_size = 0;
   int* scal = nullptr;  // device scalars: [1] badnum, [2] iters, [3] status, [4..5] queue heads, [6] queue split,
                         // [7] adjoint queue head, [8..9] iteration-list counts,
-                        // [10] gradient tile-copy time-out flag, [24..33] bad-point code statistics (5 x int64),
+                        // [10] gradient tile-copy time-out flag, [12..19] plain IC-GN size-class ranges,
+                        // [24..33] bad-point code statistics (5 x int64),
                         // [64..575] work-queue histogram and bin cursors
   double* scald = nullptr;  // device double scalars: [0] residual
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -417,6 +418,7 @@ bool frame_ok(const stdic_frame* fr) {
 // warps, the rest on single warps (queue in decreasing size).
 struct BatchedCand {
   int tw, threads, split, smem_per_warp, gtile_per_warp, blocks, smem_px, smem_px_small;
+  int blocks1;  // grid of the 6-DOF set-up stage (fewer registers, more resident CTAs)
   size_t scratch;
 };
 
@@ -440,14 +442,17 @@ std::vector<BatchedCand> batched_candidates(stdic_ctx* c, bool two, int npx_max,
     int smem_px = (int)((per_warp * tw - 512 - 32 * 4 * tw) / bpp);
     smem_px = std::max(64, std::min(smem_px, npx_max));
     const int gtile = gt_warp * tw;
-    const int per_sm = stdic::batched_blocks_per_sm(tw, two, threads, smem_px, gtile);
+    const int per_sm = stdic::batched_blocks_per_sm(tw, two, threads, smem_px, gtile, 2);
     if (per_sm <= 0) continue;
-    int blocks = c->nsm * per_sm;
+    const int per_sm1 = two ? per_sm : std::max(per_sm, stdic::batched_blocks_per_sm(tw, two, threads, smem_px, gtile, 1));
     const int units_per_block = split ? threads / 32 : teams_per_block;
-    blocks = std::max(1, std::min(blocks, (Ntot + units_per_block - 1) / units_per_block));
-    const long long warps = (long long)blocks * (threads / 32);
+    const int max_blocks = (Ntot + units_per_block - 1) / units_per_block;
+    const int blocks = std::max(1, std::min(c->nsm * per_sm, max_blocks));
+    const int blocks1 = std::max(1, std::min(c->nsm * per_sm1, max_blocks));
+    // global scratch slices for every warp of the larger of the two grids
+    const long long warps = (long long)std::max(blocks, blocks1) * (threads / 32);
     const int small_px = split ? stdic::batched_small_px(smem_px, two, tw, gtile) : 0;
-    out.push_back({tw, threads, split, per_warp, gt_warp, blocks, smem_px, small_px,
+    out.push_back({tw, threads, split, per_warp, gt_warp, blocks, smem_px, small_px, blocks1,
                    stdic::batched_scratch_bytes(npx_max, two, warps)});
   }
   return out;
@@ -524,7 +529,8 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
       cudaError_t e = cudaMemsetAsync(b.queue_head, 0, 2 * sizeof(int), c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "queue reset");
       b.stage = stages[k];
-      rc = check_launch(c, stdic::launch_icgn_batched(b, cd.blocks, cd.threads, c->stream), "IC-GN batched");
+      rc = check_launch(c, stdic::launch_icgn_batched(b, b.stage == 1 ? cd.blocks1 : cd.blocks, cd.threads, c->stream),
+                        "IC-GN batched");
       if (rc) return rc;
       if (!two && k == 0) {
         rc = check_launch(c, stdic::launch_factor6((const stdic::SubsetState6*)b.st6, b.H6, b.Hinv6, Ntot, c->stream),
@@ -614,10 +620,10 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
   stdic::SubsetState6* st6 = nullptr;
   double *H6 = nullptr, *Hinv6 = nullptr;
   int32_t* order2 = nullptr;
+  pl.scratch((size_t)std::max(N, 1), &order);
   if (batched) {
     const size_t nt = std::max(NT, (size_t)1);
     cands = batched_candidates(c, false, npx_max, (int)NT);
-    pl.scratch((size_t)std::max(N, 1), &order);
     pl.scratch(batched_scratch_need(cands), &bscr);
     pl.scratch(nt, &st6);
     pl.scratch(21 * nt, &H6);
@@ -633,7 +639,10 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
   if (N > 0) {
     if (!batched) {
       cudaEventRecord(c->es0, c->stream);
-      rc = check_launch(c, stdic::launch_icgn6_plain(a, c->stream), "IC-GN plain");
+      int nk = 0;
+      rc = check_launch(c, stdic::launch_icgn6_plain(a, order, c->scal + 64, c->scal + 12, c->stream, &nk),
+                        "IC-GN plain", 0);
+      c->launches += nk;
       cudaEventRecord(c->es1, c->stream);
       c->solver_timed = rc == STDIC_OK;
     } else {
@@ -749,9 +758,9 @@ static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, 
   unsigned char* bscr = nullptr;
   const int npx_max = stdic::grown_tile_pixels(wmax);
   std::vector<BatchedCand> cands;
+  pl.scratch((size_t)std::max(N, 1), &order);
   if (batched) {
     cands = batched_candidates(c, true, npx_max, N);
-    pl.scratch((size_t)std::max(N, 1), &order);
     pl.scratch(batched_scratch_need(cands), &bscr);
   }
   int rc = pl.commit(c);
@@ -762,7 +771,10 @@ static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, 
   if (N > 0) {
     if (!batched) {
       cudaEventRecord(c->es0, c->stream);
-      rc = check_launch(c, stdic::launch_icgn2_plain(a, c->stream), "Subpb1 plain");
+      int nk = 0;
+      rc = check_launch(c, stdic::launch_icgn2_plain(a, order, c->scal + 64, c->scal + 12, c->stream, &nk),
+                        "Subpb1 plain", 0);
+      c->launches += nk;
       cudaEventRecord(c->es1, c->stream);
       c->solver_timed = rc == STDIC_OK;
     } else {
@@ -1003,9 +1015,9 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
   int32_t* order = nullptr;
   const int npx_max = stdic::grown_tile_pixels(wmax);
   std::vector<BatchedCand> cands;
+  pl.scratch((size_t)N, &order);
   if (batched) {
     cands = batched_candidates(c, true, npx_max, N);
-    pl.scratch((size_t)N, &order);
     pl.scratch(batched_scratch_need(cands), &bscr);
   }
   int rc = pl.commit(c);
@@ -1043,7 +1055,12 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
   auto body = [&]() -> int {
     int r = STDIC_OK;
     if (batched) r = run_batched(c, b, N, cands, QueueKeys{nullptr, dwl, 0});
-    else r = check_launch(c, stdic::launch_icgn2_plain(a, c->stream), "Subpb1 plain");
+    else {
+      int nk = 0;
+      r = check_launch(c, stdic::launch_icgn2_plain(a, order, c->scal + 64, c->scal + 12, c->stream, &nk),
+                       "Subpb1 plain", 0);
+      c->launches += nk;
+    }
     if (!r) r = check_launch(c, stdic::launch_badpoints(conv, N, oU1, nullptr, 1, dsc, (unsigned long long*)(dsc + 4), c->stream), "bad points", 2);
     if (!r) r = check_launch(c, stdic::launch_fill_nans(N, delems, E, ptr, list, oU1, tmp, c->stream), "NaN fill", 2);
     if (!r) {

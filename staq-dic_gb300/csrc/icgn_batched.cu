@@ -464,6 +464,19 @@ STDIC_DEV float dot_df(const float* hh, const float* hl, const float* x) {
   return __fadd_rn(S, E);
 }
 
+// kg += J t for the 6-DOF steepest-descent images J = [dx gx, dx gy, dy gx,
+// dy gy, gx, gy] of a pixel with masked gradients g2 = (gx, gy) at offset
+// (dx, dy) from the node: (gx t, gy t) once, then scaled by dx and dy.
+STDIC_DEV void add_jt6(float (&kg)[6], float2 g2, float dx, float dy, float t) {
+  const float a = g2.x * t, b = g2.y * t;
+  kg[0] = fmaf(dx, a, kg[0]);
+  kg[1] = fmaf(dx, b, kg[1]);
+  kg[2] = fmaf(dy, a, kg[2]);
+  kg[3] = fmaf(dy, b, kg[3]);
+  kg[4] += a;
+  kg[5] += b;
+}
+
 // Team slot layout: per-pixel arrays, the staged g footprint, the control
 // block and the reduction scratch.
 // Bytes per tile pixel: 6-DOF: the masked gradients (float2) cached for the
@@ -907,21 +920,24 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     const float p0 = 1.f + P[0], p1 = P[1], p2 = P[2], p3 = 1.f + P[3];
     const float dx0 = (float)(int)(x1 - x0), dy0 = (float)(int)(y1 - y0);
     const float shift = meanf;  // one-pass variance around meanf
-    // one pass: interpolation, zero/NaN counts, g statistics and sum J g
-    // zero count, NaN flag, sum g and sum g^2 (shifted), count, sum J g
-    constexpr int NR = 5 + NQ;
+    // one pass: interpolation, zero count, g statistics and sum J g.
+    // Slots: zero count, sum g and sum g^2 (shifted), count, sum J g.  A NaN
+    // in the interpolated tile shows in sum gx g (the kR + NQ - 2 slot): every
+    // J holds gx or gy of a finite gradient times the selection (0 or 1), and
+    // 0 * NaN is NaN, so that sum is NaN exactly when a tile value is.
+    constexpr int kR = 4;  // first sum J g slot
+    constexpr int NR = kR + NQ;
     float red[NR];
     {
-      int zg = 0, nang = 0;
+      int zg = 0;
       float sg = 0.f, qg = 0.f;
       float kg[NQ];
 #pragma unroll
       for (int k = 0; k < NQ; ++k) kg[k] = 0.f;
       float ng = 0.f;
       PixIter it(pstart, mx);
-      auto one = [&](int p, int i, int j, float t) {
+      auto one = [&](int p, float dx, float dy, int i, int j, float t) {
         tg[p] = t;
-        if (t != t) nang = 1;
         if (t == 0.f) ++zg;
         if (fabsf(t) > 1e-10f) {
           const float d = t - shift;
@@ -929,11 +945,14 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
           qg = fmaf(d, d, qg);
           ng += 1.f;
         }
-        float J[NQ];
-        if constexpr (TWO) jac(i, j, bw ? (float)bw[p] : 1.f, J);
-        else jacq(p, i, j, J);
+        if constexpr (TWO) {
+          float J[NQ];
+          jac(i, j, bw ? (float)bw[p] : 1.f, J);
 #pragma unroll
-        for (int k = 0; k < NQ; ++k) kg[k] = fmaf(J[k], t, kg[k]);
+          for (int k = 0; k < NQ; ++k) kg[k] = fmaf(J[k], t, kg[k]);
+        } else {
+          add_jt6(*reinterpret_cast<float(*)[6]>(kg), gq[p], dx, dy, t);
+        }
       };
       // Stage the warped footprint of g in shared memory when it fits: the
       // tap range follows from the four corners (the warp is affine), with a
@@ -985,21 +1004,21 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         const float dxb = dx0 + (float)ib, dyb = dy0 + (float)jb;
         const float ta = sample(fu + p0 * dxa + p2 * dya, fv0 + p1 * dxa + p3 * dya);
         const float tb2 = sample(fu + p0 * dxb + p2 * dyb, fv0 + p1 * dxb + p3 * dyb);
-        one(p, ia, ja, ta);
-        one(p + tm.TT, ib, jb, tb2);
+        one(p, dxa, dya, ia, ja, ta);
+        one(p + tm.TT, dxb, dyb, ib, jb, tb2);
       }
       if (p < npx) {
         const float dx = dx0 + (float)it.i, dy = dy0 + (float)it.j;
         const float t = sample(fu + p0 * dx + p2 * dy, fv0 + p1 * dx + p3 * dy);
-        one(p, it.i, it.j, t);
+        one(p, dx, dy, it.i, it.j, t);
       }
-      red[0] = (float)zg; red[1] = (float)nang;
-      red[2] = sg; red[3] = qg; red[4] = ng;
+      red[0] = (float)zg;
+      red[1] = sg; red[2] = qg; red[3] = ng;
 #pragma unroll
-      for (int k = 0; k < NQ; ++k) red[5 + k] = kg[k];
+      for (int k = 0; k < NQ; ++k) red[kR + k] = kg[k];
     }
     tm.template sumf16<NR>(red, fscr);
-    if (red[1] > 0.f) { err = true; break; }
+    if (isnan(red[kR + NQ - 2])) { err = true; break; }
     if (cntf > 0 || red[0] > 0.f) {
       for (int p = tm.tl; p < npx; p += tm.TT) tmp[p] = tg[p] != 0.f;
       tm.sync();
@@ -1036,9 +1055,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         // kept pixels: only the removed pixels' parts are summed and taken off.
         int cnt = 0, rem = 0;
         float rsg = 0.f, rqg = 0.f;
-        float rkg[NQ];
-#pragma unroll
-        for (int k = 0; k < NQ; ++k) rkg[k] = 0.f;
+        float rkg[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         float rng = 0.f;
         PixIter it(pstart, mx);
         for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
@@ -1055,23 +1072,20 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
                 rqg = fmaf(d, d, rqg);
                 rng += 1.f;
               }
-              float J[NQ];
-              jacq(p, it.i, it.j, J);
-#pragma unroll
-              for (int k = 0; k < NQ; ++k) rkg[k] = fmaf(J[k], t, rkg[k]);
+              add_jt6(rkg, gq[p], dx0 + (float)it.i, dy0 + (float)it.j, t);
             }
           }
         }
         cg = tm.sum_int(cnt, iscr);
         if (tm.any(rem, iscr)) {
           float rr[NR];
-          rr[0] = 0.f; rr[1] = 0.f;
-          rr[2] = rsg; rr[3] = rqg; rr[4] = rng;
+          rr[0] = 0.f;
+          rr[1] = rsg; rr[2] = rqg; rr[3] = rng;
 #pragma unroll
-          for (int k = 0; k < NQ; ++k) rr[5 + k] = rkg[k];
+          for (int k = 0; k < NQ; ++k) rr[kR + k] = rkg[k < 6 ? k : 0];
           tm.template sumf16<NR>(rr, fscr);
 #pragma unroll
-          for (int k = 2; k < NR; ++k) red[k] -= rr[k];
+          for (int k = 1; k < NR; ++k) red[k] -= rr[k];
         }
         red[0] = (float)cg;
       } else {
@@ -1099,18 +1113,18 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
 #pragma unroll
           for (int k = 0; k < NQ; ++k) kg[k] = fmaf(J[k], t, kg[k]);
         }
-        red[0] = (float)cnt; red[1] = 0.f;
-        red[2] = sg; red[3] = qg; red[4] = ng;
+        red[0] = (float)cnt;
+        red[1] = sg; red[2] = qg; red[3] = ng;
 #pragma unroll
-        for (int k = 0; k < NQ; ++k) red[5 + k] = kg[k];
+        for (int k = 0; k < NQ; ++k) red[kR + k] = kg[k];
         tm.template sumf16<NR>(red, fscr);
         cg = (int)red[0];
       }
     }
     // g statistics from the shifted one-pass sums: mean and
     // sqrt((n-1) var) = sqrt(max(s2 - s1^2/n, 0)) (NaN for n = 0, 0 for n = 1)
-    const float cntg = red[4];
-    const float s1 = red[2], s2 = red[3];
+    const float cntg = red[3];
+    const float s1 = red[1], s2 = red[2];
     const float icnt = 1.f / cntg;
     const float meang = shift + s1 * icnt;
     float bg2 = fmaxf(s2 - s1 * s1 * icnt, 0.f);
@@ -1127,7 +1141,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     float b2[NQ];
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
-      const float jg = red[5 + k];
+      const float jg = red[kR + k];
       b2[k] = jf[k] * ibf - (jg - meang * j1[k]) * ibg;
     }
     // convergence test (FP32) and the update, identical on every lane
@@ -1250,7 +1264,7 @@ STDIC_DEV void team_loop(const BatchedArgs& B, const Team<TW>& tm, int* head, in
 // reduction and runs the same update on them, so all warps carry bit-identical
 // P without a shared-memory broadcast.
 template <int TW, bool TWO, int STAGE>
-__global__ void __launch_bounds__(256, 2) icgn_batched_kernel(BatchedArgs B) {
+__global__ void __launch_bounds__(256, STAGE == 1 ? 3 : 2) icgn_batched_kernel(BatchedArgs B) {
   extern __shared__ __align__(16) unsigned char dsm[];
   const int nf = B.frames > 0 ? B.frames : 1;
   const int Ntot = B.a.N * nf;
@@ -1437,8 +1451,9 @@ cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, c
 }
 
 // Resident blocks per SM of one configuration (for grid sizing and the
-// autotuner); the iteration stage (or the fused 2-DOF form) is the reference.
-int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px, int gtile) {
+// autotuner): of the 6-DOF set-up stage (stage 1), or of the iteration stage
+// (any other stage) and the fused 2-DOF form.
+int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px, int gtile, int stage) {
   const int teams = threads / (tw * 32);
   const size_t smem = batched_team_bytes(smem_px, two, tw, gtile) * teams;
   if (smem > 227 * 1024) return 0;
@@ -1450,11 +1465,12 @@ int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px, int gtile)
   if (e == cudaSuccess)                                                                          \
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, icgn_batched_kernel<TWv, TWOv, STv>,  \
                                                       threads, smem);
+  const bool s1 = !two && stage == 1;
   switch (tw) {
-    case 1: if (two) { STDIC_OCC(1, true, 0) } else { STDIC_OCC(1, false, 2) } break;
-    case 2: if (two) { STDIC_OCC(2, true, 0) } else { STDIC_OCC(2, false, 2) } break;
-    case 4: if (two) { STDIC_OCC(4, true, 0) } else { STDIC_OCC(4, false, 2) } break;
-    case 8: if (two) { STDIC_OCC(8, true, 0) } else { STDIC_OCC(8, false, 2) } break;
+    case 1: if (two) { STDIC_OCC(1, true, 0) } else if (s1) { STDIC_OCC(1, false, 1) } else { STDIC_OCC(1, false, 2) } break;
+    case 2: if (two) { STDIC_OCC(2, true, 0) } else if (s1) { STDIC_OCC(2, false, 1) } else { STDIC_OCC(2, false, 2) } break;
+    case 4: if (two) { STDIC_OCC(4, true, 0) } else if (s1) { STDIC_OCC(4, false, 1) } else { STDIC_OCC(4, false, 2) } break;
+    case 8: if (two) { STDIC_OCC(8, true, 0) } else if (s1) { STDIC_OCC(8, false, 1) } else { STDIC_OCC(8, false, 2) } break;
     default: return 0;
   }
 #undef STDIC_OCC

@@ -5,6 +5,8 @@
 // size-mismatch error of the 6-DOF pass) and result codes.  Per-pixel values
 // (warped positions, interpolated g) are rounded exactly as the reference
 // rounds them; only the order of the block-wide sums differs from a serial loop.
+#include <algorithm>
+
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -93,21 +95,20 @@ struct Shared {
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// 6-DOF first pass.  Dynamic shared memory: npx_max doubles (tempg) + 4
-// npx_max bytes (mask tile, bw_f, bw_g, scratch bitmap).
+// 6-DOF first pass.  Dynamic shared memory: npx_cap doubles (tempg) + 4
+// npx_cap bytes (mask tile, bw_f, bw_g, scratch bitmap).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) icgn6_plain_kernel(IcgnArgs a) {
-  extern __shared__ __align__(16) unsigned char dsm[];
-  __shared__ Shared sh;
-  const int node = blockIdx.x;
-  if (node >= a.N) return;
+// One node on the whole CTA; npx_cap is the tile capacity of the CTA's
+// dynamic shared memory (the grown tile of the largest subset of its class).
+__device__ void plain6_node(const IcgnArgs& a, const int node, unsigned char* dsm, Shared& sh,
+                            const int npx_cap) {
   Frame64 fr{(const double*)a.f, (const double*)a.g, a.mask, (const double*)a.dfdx,
              (const double*)a.dfdy, a.W, a.H};
   double* tg = (double*)dsm;
-  uint8_t* mtile = (uint8_t*)(tg + a.npx_max);
-  uint8_t* bwf = mtile + a.npx_max;
-  uint8_t* bwg = bwf + a.npx_max;
-  uint8_t* tmp = bwg + a.npx_max;
+  uint8_t* mtile = (uint8_t*)(tg + npx_cap);
+  uint8_t* bwf = mtile + npx_cap;
+  uint8_t* bwg = bwf + npx_cap;
+  uint8_t* tmp = bwg + npx_cap;
 
   const double cx = a.coords[node], cy = a.coords[a.N + node];
   const long long x0 = llround(cx), y0 = llround(cy);
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(256) icgn6_plain_kernel(IcgnArgs a) {
     ws = (int)grow_window(npx0, npx0 - (double)cntf, ws);
     x1 = x0 - ws / 2; x3 = x0 + ws / 2; y1 = y0 - ws / 2; y3 = y0 + ws / 2;
     if (!mask_crop_ok(fr, x1, x3, y1, y3) || !crop_ok(fr, x1, x3, y1, y3) ||
-        (ws + 1) * (ws + 1) > a.npx_max) {
+        (ws + 1) * (ws + 1) > npx_cap) {
       finish(-1, true, P, nullptr);
       return;
     }
@@ -325,21 +326,18 @@ __global__ void __launch_bounds__(256) icgn6_plain_kernel(IcgnArgs a) {
 
 // ---------------------------------------------------------------------------
 // 2-DOF augmented-Lagrangian Subpb1 (funICGN_Subpb1.m).  Dynamic shared
-// memory as for the 6-DOF kernel plus npx_max doubles for tempf.
+// memory as for the 6-DOF kernel plus npx_cap doubles for tempf.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) icgn2_plain_kernel(IcgnArgs a) {
-  extern __shared__ __align__(16) unsigned char dsm[];
-  __shared__ Shared sh;
-  const int node = blockIdx.x;
-  if (node >= a.N) return;
+__device__ void plain2_node(const IcgnArgs& a, const int node, unsigned char* dsm, Shared& sh,
+                            const int npx_cap) {
   Frame64 fr{(const double*)a.f, (const double*)a.g, a.mask, (const double*)a.dfdx,
              (const double*)a.dfdy, a.W, a.H};
   double* tg = (double*)dsm;
-  double* tf = tg + a.npx_max;
-  uint8_t* mtile = (uint8_t*)(tf + a.npx_max);
-  uint8_t* bwf = mtile + a.npx_max;
-  uint8_t* bwg = bwf + a.npx_max;
-  uint8_t* tmp = bwg + a.npx_max;
+  double* tf = tg + npx_cap;
+  uint8_t* mtile = (uint8_t*)(tf + npx_cap);
+  uint8_t* bwf = mtile + npx_cap;
+  uint8_t* bwg = bwf + npx_cap;
+  uint8_t* tmp = bwg + npx_cap;
 
   const long long x0 = llround(a.coords[node]), y0 = llround(a.coords[a.N + node]);
   int wx = a.wsl2[node], wy = a.wsl2[a.N + node];
@@ -358,7 +356,7 @@ __global__ void __launch_bounds__(256) icgn2_plain_kernel(IcgnArgs a) {
   };
   long long x1 = x0 - wx / 2, x3 = x0 + wx / 2, y1 = y0 - wy / 2, y3 = y0 + wy / 2;
   if ((wx & 1) || (wy & 1) || wx < 0 || wy < 0 || !mask_crop_ok(fr, x1, x3, y1, y3) ||
-      !crop_ok(fr, x1, x3, y1, y3) || (wx + 1) * (wy + 1) > a.npx_max) {
+      !crop_ok(fr, x1, x3, y1, y3) || (wx + 1) * (wy + 1) > npx_cap) {
     finish(0, true);
     return;
   }
@@ -387,7 +385,7 @@ __global__ void __launch_bounds__(256) icgn2_plain_kernel(IcgnArgs a) {
     }
     x1 = x0 - wx / 2; x3 = x0 + wx / 2; y1 = y0 - wy / 2; y3 = y0 + wy / 2;
     if (!mask_crop_ok(fr, x1, x3, y1, y3) || !crop_ok(fr, x1, x3, y1, y3) ||
-        (wx + 1) * (wy + 1) > a.npx_max) {
+        (wx + 1) * (wy + 1) > npx_cap) {
       finish(0, true);
       return;
     }
@@ -518,6 +516,126 @@ __global__ void __launch_bounds__(256) icgn2_plain_kernel(IcgnArgs a) {
   block_sum<1>(v, sh.red);
   if (v[0] < 1e-6) st = kMaxIter + 3;
   finish(st, false);
+}
+
+// ---------------------------------------------------------------------------
+// Size classes.  Every node runs on one CTA, as in the reference's per-node
+// loop; the nodes are sorted by subset size and each class runs with a CTA
+// sized to its tiles (fewer idle threads, and shared memory for its own grown
+// tile instead of the largest one of the call), so that many more small
+// subsets are in flight on an SM.  Persistent CTAs stride over their class.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct PlainClass {
+  const int32_t* order;  // node order (sorted by size); nullptr: nodes 0..N-1
+  const int* range;      // [lo, hi) of this class in order; nullptr: [0, N)
+  int npx_cap;           // tile capacity of the CTA's shared memory
+};
+
+template <int T, bool TWO>
+__global__ void __launch_bounds__(T) icgn_plain_class_kernel(IcgnArgs a, PlainClass cl) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ Shared sh;
+  const int lo = cl.range ? cl.range[0] : 0, hi = cl.range ? cl.range[1] : a.N;
+  for (int q = lo + blockIdx.x; q < hi; q += gridDim.x) {
+    const int node = cl.order ? cl.order[q] : q;
+    if constexpr (TWO) plain2_node(a, node, dsm, sh, cl.npx_cap);
+    else plain6_node(a, node, dsm, sh, cl.npx_cap);
+    __syncthreads();  // thread 0's output writes read sh before the next node reuses it
+  }
+}
+
+// Class k covers subset edges (kClassEdge[k-1], kClassEdge[k]]; the last class
+// takes everything larger.
+constexpr int kClasses = 4;
+constexpr int kClassEdge[kClasses] = {8, 16, 32, 255};
+constexpr int kClassThreads[kClasses] = {64, 128, 256, 256};
+
+// Queue positions of each class from the histogram of subset edges of an
+// ascending queue (bin b = edge b).
+__global__ void plain_class_ranges_kernel(const int* __restrict__ hist, int* ranges, int4 edges) {
+  if (threadIdx.x != 0) return;
+  const int e[kClasses] = {edges.x, edges.y, edges.z, edges.w};
+  int pos = 0, b = 0;
+  for (int k = 0; k < kClasses; ++k) {
+    ranges[2 * k] = pos;
+    for (; b <= e[k]; ++b) pos += hist[b];
+    ranges[2 * k + 1] = pos;
+  }
+}
+
+template <int T, bool TWO>
+cudaError_t launch_class(const IcgnArgs& a, const PlainClass& cl, int nodes_hint, cudaStream_t s) {
+  const size_t smem = (size_t)cl.npx_cap * (TWO ? 2 * sizeof(double) + 4 : sizeof(double) + 4);
+  cudaError_t e = cudaFuncSetAttribute(icgn_plain_class_kernel<T, TWO>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  // resident CTAs per SM for this shared-memory size, queried once (the
+  // first call of a loop runs before any graph capture of it)
+  static int cached_smem[64] = {}, cached_per_sm[64] = {};
+  int per_sm = 0;
+  for (int k = 0; k < 64 && cached_smem[k]; ++k)
+    if (cached_smem[k] == (int)smem) { per_sm = cached_per_sm[k]; break; }
+  if (per_sm == 0) {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, icgn_plain_class_kernel<T, TWO>, T, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    for (int k = 0; k < 64; ++k)
+      if (!cached_smem[k]) { cached_smem[k] = (int)smem; cached_per_sm[k] = per_sm; break; }
+  }
+  int blocks = current_sm_count() * per_sm;
+  if (nodes_hint > 0 && nodes_hint < blocks) blocks = nodes_hint;
+  icgn_plain_class_kernel<T, TWO><<<blocks, T, smem, s>>>(a, cl);
+  return cudaGetLastError();
+}
+
+template <bool TWO>
+cudaError_t launch_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,
+                         int* kernels) {
+  *kernels = 0;
+  if (a.N <= 0) return cudaSuccess;
+  const bool per_node = TWO ? a.wsl2 != nullptr : a.ws_list != nullptr;
+  if (!per_node) {
+    // one subset size: one class
+    const int ws = a.ws_all;
+    PlainClass cl{nullptr, nullptr, a.npx_max};
+    *kernels = 1;
+    if (ws <= 8) return launch_class<64, TWO>(a, cl, a.N, s);
+    if (ws <= 16) return launch_class<128, TWO>(a, cl, a.N, s);
+    return launch_class<256, TWO>(a, cl, a.N, s);
+  }
+  cudaError_t e = launch_build_queue(TWO ? nullptr : a.ws_list, TWO ? a.wsl2 : nullptr, a.ws_all, a.N, order,
+                                     nullptr, qscratch, s, 1, 0);
+  if (e != cudaSuccess) return e;
+  plain_class_ranges_kernel<<<1, 32, 0, s>>>(
+      qscratch, ranges, make_int4(kClassEdge[0], kClassEdge[1], kClassEdge[2], kClassEdge[3]));
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  *kernels = 4;
+  for (int k = 0; k < kClasses && e == cudaSuccess; ++k) {
+    PlainClass cl{order, ranges + 2 * k, k + 1 < kClasses ? std::min(grown_tile_pixels(kClassEdge[k]), a.npx_max)
+                                                           : a.npx_max};
+    switch (kClassThreads[k]) {
+      case 64: e = launch_class<64, TWO>(a, cl, a.N, s); break;
+      case 128: e = launch_class<128, TWO>(a, cl, a.N, s); break;
+      default: e = launch_class<256, TWO>(a, cl, a.N, s); break;
+    }
+    ++*kernels;
+  }
+  return e;
+}
+
+}  // namespace
+
+cudaError_t launch_icgn6_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,
+                               int* kernels) {
+  return launch_plain<false>(a, order, qscratch, ranges, s, kernels);
+}
+
+cudaError_t launch_icgn2_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,
+                               int* kernels) {
+  return launch_plain<true>(a, order, qscratch, ranges, s, kernels);
 }
 
 }  // namespace stdic

@@ -103,7 +103,7 @@ cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hin
 int batched_tile_px_bytes(bool two);
 size_t batched_team_bytes(int sm_px, bool two, int tw, int gtile);
 size_t batched_scratch_bytes(int npx_max, bool two, long long warps);
-int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px, int gtile);
+int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px, int gtile, int stage);
 
 cudaError_t launch_interp(const void* F, long long M, long long N, long long P, const void* X,
                           const void* Y, long long n, void* out, int dtype, cudaStream_t s);
@@ -114,8 +114,14 @@ cudaError_t launch_intsearch(const double* f, const double* g, int W, int H, int
                              double gx0, double gy0, int nx, int ny, int wsx, int wsy, int stepx,
                              int stepy, double* x, double* y, double* u, double* v, double* cc,
                              int32_t* peak, cudaStream_t s);
-cudaError_t launch_icgn6_plain(const IcgnArgs& a, cudaStream_t s);
-cudaError_t launch_icgn2_plain(const IcgnArgs& a, cudaStream_t s);
+// Plain FP64 IC-GN, one CTA per node, in subset-size classes (CTA size and
+// shared memory per class).  order: N device ints; qscratch: 512 device ints
+// (the queue histogram and cursors); ranges: 8 device ints (class ranges).
+// *kernels receives the number of kernels launched.
+cudaError_t launch_icgn6_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,
+                               int* kernels);
+cudaError_t launch_icgn2_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,
+                               int* kernels);
 // tmp_dev: five device 64-bit integers of scratch (the code statistics)
 cudaError_t launch_badpoints(int32_t* conv, int N, double* U, double* F, int two_dof,
                              int* badnum_dev, unsigned long long* tmp_dev, cudaStream_t s);

@@ -424,32 +424,6 @@ cudaError_t launch_intsearch(const double* f, const double* g, int W, int H, int
 }
 
 // ---------------------------------------------------------------------------
-// IC-GN plain launchers (kernels in icgn_plain.cu)
-// ---------------------------------------------------------------------------
-__global__ void icgn6_plain_kernel(IcgnArgs a);
-__global__ void icgn2_plain_kernel(IcgnArgs a);
-
-cudaError_t launch_icgn6_plain(const IcgnArgs& a, cudaStream_t s) {
-  if (a.N <= 0) return cudaSuccess;
-  const size_t smem = (size_t)a.npx_max * (sizeof(double) + 4);
-  cudaError_t e = cudaFuncSetAttribute(icgn6_plain_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  icgn6_plain_kernel<<<a.N, 256, smem, s>>>(a);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_icgn2_plain(const IcgnArgs& a, cudaStream_t s) {
-  if (a.N <= 0) return cudaSuccess;
-  const size_t smem = (size_t)a.npx_max * (2 * sizeof(double) + 4);
-  cudaError_t e = cudaFuncSetAttribute(icgn2_plain_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  icgn2_plain_kernel<<<a.N, 256, smem, s>>>(a);
-  return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
 // Bad-subset filter after the per-node loop.  LocalICGNQuadtree: bad =
 // conv<0 | conv>99, then also conv > max(mean+std, 6) of the good codes;
 // Subpb1Quadtree: max(mean+0.25 std, 10).  U (and F for the first pass) become

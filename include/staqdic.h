@@ -129,11 +129,16 @@ int stdic_integer_search_grid(int W, int H, const int S[2], const double gridx[2
  * f, g are W x H double.  Outputs are ny x nx (row = y index) column-major;
  * cc is cc.max.  peak_rc (optional, 2 x ny x nx planes) receives the 1-based
  * integer argmax (row, col) of each cropped (2S+3)^2 correlation map; 0 where
- * normxcorr2 throws (constant template), where u, v, cc are NaN. */
+ * normxcorr2 throws (constant template), where u, v, cc are NaN.  qfactors
+ * (optional, (ny nx) x 2 column-major, rows in the reference's point order,
+ * x fastest) receives cc.qfactors (funIntegerSearch.m:129-131,156,175-176,
+ * 211-264): the peak-to-correlation-energy and peak-to-entropy ratios of each
+ * point's full normxcorr2 map, each column shifted to start at 0 and divided
+ * by its largest value, Inf before the normalisation where normxcorr2 throws. */
 int stdic_integer_search(stdic_ctx* ctx, const double* f, const double* g, int W, int H,
                          const int S[2], const double gridx[2], const double gridy[2],
                          const int winsize[2], const int winstepsize[2], double* x, double* y,
-                         double* u, double* v, double* cc, int32_t* peak_rc);
+                         double* u, double* v, double* cc, int32_t* peak_rc, double* qfactors);
 
 /* LocalICGNQuadtree(U0, coordinatesFEM, Df, ImgRef, ImgDef, DICpara, 'GaussNewton', tol)
  * without its NaN-fill tail (out of this path): U (2N) and F (4N) carry NaN at

@@ -161,6 +161,24 @@ def funIntegerSearch(f, g, S, gridx, gridy, winsize, winstepsize):
     return x, y, u, v, cc, peak
 
 
+def integer_search_qfactors(f, g, S, gridx, gridy, winsize, winstepsize):
+    """cc.qfactors of funIntegerSearch (funIntegerSearch.m:129-131,156,175-176,
+    211-264): (raw, normalised), each (ny*nx) x 2 with rows in the reference's
+    point order (x fastest); raw holds each point's PCE and PPE (Inf where
+    normxcorr2 throws)."""
+    W, H = f.shape
+    S, ws, st = _pair(S), _pair(winsize), _pair(winstepsize)
+    _, _, nx, ny = intsearch_grid(W, H, S, gridx, gridy, ws, st)
+    fa, ga = _F(f), _F(g)
+    raw = np.empty((nx * ny, 2), order="F")
+    qf = np.empty((nx * ny, 2), order="F")
+    gx_in = (ctypes.c_double * 2)(*map(float, gridx))
+    gy_in = (ctypes.c_double * 2)(*map(float, gridy))
+    lib().orc_integer_search_qfactors(_p(fa, _d), _p(ga, _d), _L(W), _L(H), int(S[0]), int(S[1]), gx_in, gy_in,
+                                      int(ws[0]), int(ws[1]), int(st[0]), int(st[1]), _p(raw, _d), _p(qf, _d))
+    return raw, qf
+
+
 # --------------------------------------------------------------------------
 # LocalICGNQuadtree / funICGNQuadtree
 # --------------------------------------------------------------------------

@@ -1021,6 +1021,122 @@ extern "C" void orc_integer_search(const double* f, const double* g, long W, lon
 }
 
 // ---------------------------------------------------------------------------
+// cc.qfactors of funIntegerSearch (funIntegerSearch.m:129-131, 156, 175-176,
+// compute_qFactor :211-264): for each grid point the full normxcorr2 map
+// (every lag with an overlap), cc_min = cc - min(cc), peak = max(cc_min),
+// PCE = peak^2 / mean(cc_min^2) and PPE = 1 / entropy of histcounts(cc_min,30)
+// (30 uniform bins over [0, peak], the last closed); [Inf Inf] where
+// normxcorr2 throws.  Each column is then shifted by its minimum and divided
+// by its largest shifted value (NaN ignored, as MATLAB's min and max do).
+// Rows follow the reference's point sequence (x fastest).  qf is npt x 2.
+// ---------------------------------------------------------------------------
+static void qfactor_point(const double* f, const double* g, long W, long ii, long jj, int Sx, int Sy, int wsx,
+                          int wsy, double* pce, double* ppe) {
+  const int m = wsx + 1, n = wsy + 1, am = wsx + 1 + 2 * Sx, an = wsy + 1 + 2 * Sy;
+  const double mn = (double)m * (double)n;
+  std::vector<double> T((size_t)m * n), A((size_t)am * an);
+  for (int b = 0; b < n; ++b)
+    for (int a = 0; a < m; ++a) T[a + b * m] = f[(jj - 1 + b) * W + (ii - 1 + a)];
+  for (int q = 0; q < an; ++q)
+    for (int p = 0; p < am; ++p) A[p + q * am] = g[(jj - 1 - Sy + q) * W + (ii - 1 - Sx + p)];
+  bool fin = true;
+  for (double t : T) fin = fin && std::isfinite(t);
+  for (double t : A) fin = fin && std::isfinite(t);
+  double sumT = 0;
+  for (double t : T) sumT += t;
+  const double meanT = sumT / mn;
+  double q2 = 0;
+  for (double t : T) { const double d = t - meanT; q2 += d * d; }
+  const double stdT = std::sqrt(q2 / (mn - 1));
+  if (!fin || !(stdT != 0)) { *pce = INFINITY; *ppe = INFINITY; return; }
+  const double denomT = std::sqrt(mn - 1) * stdT;
+  const int R = m + am - 1, C = n + an - 1;
+  std::vector<double> num((size_t)R * C), den((size_t)R * C);
+  double dmax = 0;
+  for (int j = 0; j < C; ++j)
+    for (int i = 0; i < R; ++i) {
+      const int dr = i - (m - 1), dc = j - (n - 1);
+      double xc = 0, sA = 0, sA2 = 0;
+      for (int b = 0; b < n; ++b) {
+        const int qq = b + dc;
+        if (qq < 0 || qq >= an) continue;
+        for (int a = 0; a < m; ++a) {
+          const int pp = a + dr;
+          if (pp < 0 || pp >= am) continue;
+          const double av = A[pp + qq * am];
+          xc += T[a + b * m] * av;
+          sA += av;
+          sA2 += av * av;
+        }
+      }
+      const double dl = sA2 - (sA * sA) / mn;
+      num[i + j * R] = xc - sA * sumT / mn;
+      den[i + j * R] = denomT * std::sqrt(dl > 0 ? dl : 0.0);
+      if (std::fabs(den[i + j * R]) > dmax) dmax = std::fabs(den[i + j * R]);
+    }
+  const double tolc = std::sqrt(matlab_eps(dmax));
+  const double clip = std::sqrt(matlab_eps(1.0));
+  const size_t nl = (size_t)R * C;
+  double cmin = INFINITY, cmax = -INFINITY;
+  for (size_t k = 0; k < nl; ++k) {
+    double cv = den[k] > tolc ? num[k] / den[k] : 0.0;
+    if ((std::fabs(cv) - 1) > clip) cv = 0;
+    num[k] = cv;
+    cmin = std::min(cmin, cv);
+    cmax = std::max(cmax, cv);
+  }
+  const double peak = cmax - cmin, bw = peak / 30.0;
+  double e2 = 0;
+  long hist[30] = {0};
+  for (size_t k = 0; k < nl; ++k) {
+    const double x = num[k] - cmin;
+    e2 += x * x;
+    int bin = 0;
+    if (peak > 0) {
+      // the last edge whose value is <= x, the 30th bin closed at peak
+      bin = 29;
+      for (int e = 1; e < 30; ++e)
+        if (x < e * bw) { bin = e - 1; break; }
+    }
+    ++hist[bin];
+  }
+  *pce = peak * peak / (e2 / (double)nl);
+  double ent = 0;
+  for (int b = 0; b < 30; ++b) {
+    const double pb = (double)hist[b] / (double)nl;
+    if (pb != 0) ent += pb * std::log(1.0 / pb);
+  }
+  *ppe = 1.0 / ent;
+}
+
+extern "C" void orc_integer_search_qfactors(const double* f, const double* g, long W, long H, int Sx, int Sy,
+                                            const double gridx[2], const double gridy[2], int wsx, int wsy,
+                                            int stepx, int stepy, double* qraw, double* qf) {
+  double gx[2], gy[2];
+  long nx, ny;
+  orc_intsearch_grid(W, H, Sx, Sy, gridx, gridy, wsx, wsy, stepx, stepy, gx, gy, &nx, &ny);
+  const long npt = nx * ny;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (long t = 0; t < npt; ++t) {
+    const long ix = t % nx, iy = t / nx;
+    const long ii = (long)gx[0] + ix * stepx, jj = (long)gy[0] + iy * stepy;
+    qfactor_point(f, g, W, ii, jj, Sx, Sy, wsx, wsy, &qraw[t], &qraw[npt + t]);
+  }
+  for (int k = 0; k < 2; ++k) {
+    const double* q = qraw + k * npt;
+    double mn = INFINITY;
+    for (long t = 0; t < npt; ++t)
+      if (!std::isnan(q[t])) mn = std::min(mn, q[t]);
+    double mx = -INFINITY;
+    for (long t = 0; t < npt; ++t) {
+      const double d = q[t] - mn;
+      if (!std::isnan(d)) mx = std::max(mx, d);
+    }
+    for (long t = 0; t < npt; ++t) qf[k * npt + t] = (q[t] - mn) / mx;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Adjoint of the subset ZNSSD cost (no counterpart in the reference).  The cost
 // is the criterion funICGNQuadtree.m minimises, taken on the square window:
 //   C_n = sum_i (a_i - b_i)^2,   a = (f - fbar) / |f - fbar|,

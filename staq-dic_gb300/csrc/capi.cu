@@ -330,7 +330,7 @@ int stdic_integer_search_grid(int W, int H, const int S[2], const double gridx[2
 int stdic_integer_search(stdic_ctx* c, const double* f, const double* g, int W, int H, const int S[2],
                          const double gridx[2], const double gridy[2], const int winsize[2],
                          const int winstepsize[2], double* x, double* y, double* u, double* v,
-                         double* cc, int32_t* peak_rc) {
+                         double* cc, int32_t* peak_rc, double* qfactors) {
   if (!c) return STDIC_E_ARG;
   int nx, ny;
   if (stdic_integer_search_grid(W, H, S, gridx, gridy, winsize, winstepsize, &nx, &ny) ||
@@ -349,6 +349,12 @@ int stdic_integer_search(stdic_ctx* c, const double* f, const double* g, int W, 
   pl.out(x, npt, &dx); pl.out(y, npt, &dy); pl.out(u, npt, &du); pl.out(v, npt, &dv);
   pl.out(cc, npt, &dc);
   pl.out(peak_rc, 2 * npt, &dp);
+  double *dq = nullptr, *qscr = nullptr;
+  if (qfactors) {
+    pl.out(qfactors, 2 * npt, &dq);
+    pl.scratch(stdic::intsearch_qfactor_scratch_bytes(nx, ny, S[0], S[1], winsize[0], winsize[1]) / sizeof(double),
+               &qscr);
+  }
   int rc = pl.commit(c);
   if (rc) return rc;
   if (npt > 0) {
@@ -357,6 +363,13 @@ int stdic_integer_search(stdic_ctx* c, const double* f, const double* g, int W, 
                                                  dv, dc, dp, c->stream),
                       "funIntegerSearch");
     if (rc) return rc;
+    if (qfactors) {
+      rc = check_launch(c, stdic::launch_intsearch_qfactors(df, dg, W, S[0], S[1], gx[0], gy[0], nx, ny, winsize[0],
+                                                            winsize[1], winstepsize[0], winstepsize[1], qscr, dq,
+                                                            c->stream),
+                        "funIntegerSearch quality factors", 2);
+      if (rc) return rc;
+    }
   }
   return pl.finish(c);
 }

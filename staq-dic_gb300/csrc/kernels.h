@@ -118,6 +118,13 @@ cudaError_t launch_intsearch(const double* f, const double* g, int W, int H, int
 // shared memory per class).  order: N device ints; qscratch: 512 device ints
 // (the queue histogram and cursors); ranges: 8 device ints (class ranges).
 // *kernels receives the number of kernels launched.
+// cc.qfactors of the integer search: PCE and PPE of each grid point's full
+// normxcorr2 map, normalised over the points; qf is npt x 2 (column-major),
+// scratch holds intsearch_qfactor_scratch_bytes(...) bytes.
+size_t intsearch_qfactor_scratch_bytes(int nx, int ny, int Sx, int Sy, int wsx, int wsy);
+cudaError_t launch_intsearch_qfactors(const double* f, const double* g, int W, int Sx, int Sy, double gx0,
+                                      double gy0, int nx, int ny, int wsx, int wsy, int stepx, int stepy,
+                                      double* scratch, double* qf, cudaStream_t s);
 cudaError_t launch_icgn6_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,
                                int* kernels);
 cudaError_t launch_icgn2_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,

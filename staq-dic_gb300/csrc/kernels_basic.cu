@@ -424,6 +424,244 @@ cudaError_t launch_intsearch(const double* f, const double* g, int W, int H, int
 }
 
 // ---------------------------------------------------------------------------
+// Quality factors of the integer search (funIntegerSearch.m:129-131, 211-264):
+// for each grid point the FULL normxcorr2 map (every lag with any overlap,
+// (m + am - 1) x (n + an - 1)), then
+//   cc_min = cc - min(cc), peak = max(cc_min),
+//   PCE = peak^2 / mean(cc_min^2),
+//   PPE = 1 / entropy of the 30-bin histogram of cc_min (p log(1/p) summed
+//         over the non-empty bins),
+// and [Inf Inf] where normxcorr2 throws (constant or non-finite template or
+// window).  The histogram takes 30 bins of uniform width over [0, peak], the
+// last one closed, which is the documented behaviour of histcounts(X, 30);
+// MATLAB's own placement of those edges is internal to it.  One CTA per grid
+// point; the map is written to scratch (R x C doubles per point) between the
+// two passes.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) intsearch_qfactor_kernel(
+    const double* __restrict__ f, const double* __restrict__ g, int W, int Sx, int Sy, double gx0, double gy0,
+    int nx, int ny, int wsx, int wsy, int stepx, int stepy, double* __restrict__ maps, double* __restrict__ qraw) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ double red[32 * 4];
+  __shared__ int hist[30];
+  const int t = blockIdx.x;
+  const int ix = t % nx, iy = t / nx;
+  const long long ii = (long long)gx0 + (long long)ix * stepx;
+  const long long jj = (long long)gy0 + (long long)iy * stepy;
+  const int m = wsx + 1, n = wsy + 1, am = wsx + 1 + 2 * Sx, an = wsy + 1 + 2 * Sy;
+  const int R = m + am - 1, Cn = n + an - 1, nl = R * Cn;
+  const double mn = (double)m * (double)n;
+  double* T = (double*)dsm;
+  double* A = T + m * n;
+  // the point's map, column-major R x Cn (the cc of the full lag range),
+  // with room for the numerators after it
+  double* map = maps + (long long)t * 2 * nl;
+  // row of cc.qfactors: the reference's point sequence, x fastest
+  // (PtPosSeq from ndgrid(XList, YList), funIntegerSearch.m:90-95)
+  const long long o = ix + (long long)iy * nx;
+  const long long npt = (long long)nx * ny;
+  int bad = 0;
+  for (int q = threadIdx.x; q < m * n; q += blockDim.x) {
+    const int a = q % m, b = q / m;
+    const double val = f[(jj - 1 + b) * W + (ii - 1 + a)];
+    T[q] = val;
+    if (!isfinite(val)) bad = 1;
+  }
+  for (int q = threadIdx.x; q < am * an; q += blockDim.x) {
+    const int pp = q % am, r = q / am;
+    const double val = g[(jj - 1 - Sy + r) * W + (ii - 1 - Sx + pp)];
+    A[q] = val;
+    if (!isfinite(val)) bad = 1;
+  }
+  bad = __syncthreads_or(bad);
+  double s[1] = {0};
+  for (int q = threadIdx.x; q < m * n; q += blockDim.x) s[0] += T[q];
+  block_sum<1>(s, red);
+  const double sumT = s[0];
+  const double meanT = sumT / mn;
+  double q2[1] = {0};
+  for (int q = threadIdx.x; q < m * n; q += blockDim.x) {
+    const double d = T[q] - meanT;
+    q2[0] += d * d;
+  }
+  block_sum<1>(q2, red);
+  const double stdT = sqrt(q2[0] / (mn - 1));
+  if (bad || !(stdT != 0)) {
+    if (threadIdx.x == 0) {
+      qraw[o] = INFINITY;
+      qraw[npt + o] = INFINITY;
+    }
+    return;
+  }
+  const double denomT = sqrt(mn - 1) * stdT;
+  // pass 1: numerator and denominator of every lag; lag (dr, dc) puts the
+  // template's first element on A(dr, dc) (0-based, may be negative)
+  double dmax = 0;
+  double* den = map;  // the denominators first, then the values in place
+  for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+    const int dr = k % R - (m - 1), dc = k / R - (n - 1);
+    const int a0 = dr < 0 ? -dr : 0, a1 = (am - dr) < m ? (am - dr) : m;
+    const int b0 = dc < 0 ? -dc : 0, b1 = (an - dc) < n ? (an - dc) : n;
+    double xc = 0, sA = 0, sA2 = 0;
+    for (int b = b0; b < b1; ++b) {
+      const double* Tr = T + b * m;
+      const double* Ar = A + (b + dc) * am + dr;
+      for (int a = a0; a < a1; ++a) {
+        const double av = Ar[a];
+        xc = fma(Tr[a], av, xc);
+        sA += av;
+        sA2 = fma(av, av, sA2);
+      }
+    }
+    const double nm = xc - sA * sumT / mn;
+    const double dl = sA2 - (sA * sA) / mn;
+    const double dv = denomT * sqrt(dl > 0 ? dl : 0.0);
+    // keep the numerator in the upper half of the slot pair: den[k], then the
+    // numerator after all denominators
+    den[k] = dv;
+    map[nl + k] = nm;
+    dmax = fmax(dmax, fabs(dv));
+  }
+  for (int off = 16; off > 0; off >>= 1) dmax = fmax(dmax, __shfl_down_sync(0xffffffffu, dmax, off));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dmax;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t2 = threadIdx.x < (blockDim.x + 31) / 32 ? red[threadIdx.x] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) t2 = fmax(t2, __shfl_down_sync(0xffffffffu, t2, off));
+    if (threadIdx.x == 0) red[0] = t2;
+  }
+  __syncthreads();
+  const double tolc = sqrt(eps_of(red[0]));
+  const double clip = sqrt(eps_of(1.0));
+  __syncthreads();
+  // pass 2: the values, their min and max
+  double vmin = INFINITY, vmax = -INFINITY;
+  for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+    const double dv = den[k];
+    double cv = dv > tolc ? map[nl + k] / dv : 0.0;
+    if ((fabs(cv) - 1) > clip) cv = 0;
+    map[k] = cv;
+    vmin = fmin(vmin, cv);
+    vmax = fmax(vmax, cv);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    vmin = fmin(vmin, __shfl_down_sync(0xffffffffu, vmin, off));
+    vmax = fmax(vmax, __shfl_down_sync(0xffffffffu, vmax, off));
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = vmin; red[32 + (threadIdx.x >> 5)] = vmax; }
+  if (threadIdx.x < 30) hist[threadIdx.x] = 0;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nw = (blockDim.x + 31) / 32;
+    double a = threadIdx.x < nw ? red[threadIdx.x] : INFINITY;
+    double b = threadIdx.x < nw ? red[32 + threadIdx.x] : -INFINITY;
+    for (int off = 16; off > 0; off >>= 1) {
+      a = fmin(a, __shfl_down_sync(0xffffffffu, a, off));
+      b = fmax(b, __shfl_down_sync(0xffffffffu, b, off));
+    }
+    if (threadIdx.x == 0) { red[64] = a; red[65] = b; }
+  }
+  __syncthreads();
+  const double cmin = red[64];
+  const double peak = red[65] - cmin;
+  const double bw = peak / 30.0;
+  // pass 3: sum of cc_min^2 and the histogram
+  double e2[1] = {0};
+  for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+    const double x = map[k] - cmin;
+    e2[0] = fma(x, x, e2[0]);
+    int bin = 0;
+    if (peak > 0) {
+      bin = (int)floor(x / bw);
+      bin = bin < 0 ? 0 : (bin > 29 ? 29 : bin);
+      // edges k * bw (k < 30) and peak: move across an edge the division rounded past
+      if (bin > 0 && x < bin * bw) --bin;
+      if (bin < 29 && x >= (bin + 1) * bw) ++bin;
+    }
+    atomicAdd(&hist[bin], 1);
+  }
+  block_sum<1>(e2, red);
+  if (threadIdx.x == 0) {
+    const double pce = peak * peak / (e2[0] / (double)nl);
+    double ent = 0;
+    for (int b = 0; b < 30; ++b) {
+      const double pb = (double)hist[b] / (double)nl;
+      if (pb != 0) ent += pb * log(1.0 / pb);
+    }
+    qraw[o] = pce;
+    qraw[npt + o] = 1.0 / ent;
+  }
+}
+
+// cc.qfactors(:,k) = (q - min q) / max(q - min q) over all grid points, with
+// MATLAB's min and max (NaN ignored); one CTA.
+__global__ void __launch_bounds__(256) qfactor_normalise_kernel(const double* __restrict__ qraw, long long npt,
+                                                                 double* __restrict__ qf) {
+  __shared__ double red[32];
+  for (int k = 0; k < 2; ++k) {
+    const double* q = qraw + k * npt;
+    double mn = INFINITY;
+    for (long long i = threadIdx.x; i < npt; i += blockDim.x)
+      if (!isnan(q[i])) mn = fmin(mn, q[i]);
+    for (int off = 16; off > 0; off >>= 1) mn = fmin(mn, __shfl_down_sync(0xffffffffu, mn, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mn;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double v = INFINITY;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = fmin(v, red[w]);
+      red[0] = v;
+    }
+    __syncthreads();
+    const double qmin = red[0];
+    __syncthreads();
+    double mx = -INFINITY;
+    for (long long i = threadIdx.x; i < npt; i += blockDim.x) {
+      const double d = q[i] - qmin;
+      if (!isnan(d)) mx = fmax(mx, d);
+    }
+    for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double v = -INFINITY;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = fmax(v, red[w]);
+      red[0] = v;
+    }
+    __syncthreads();
+    const double dmax = red[0];
+    __syncthreads();
+    for (long long i = threadIdx.x; i < npt; i += blockDim.x) qf[k * npt + i] = (q[i] - qmin) / dmax;
+  }
+}
+
+size_t intsearch_qfactor_scratch_bytes(int nx, int ny, int Sx, int Sy, int wsx, int wsy) {
+  const size_t R = (size_t)2 * wsx + 2 * Sx + 1, C = (size_t)2 * wsy + 2 * Sy + 1;
+  return ((size_t)nx * ny * (2 * R * C + 2)) * sizeof(double);
+}
+
+cudaError_t launch_intsearch_qfactors(const double* f, const double* g, int W, int Sx, int Sy, double gx0,
+                                      double gy0, int nx, int ny, int wsx, int wsy, int stepx, int stepy,
+                                      double* scratch, double* qf, cudaStream_t s) {
+  if (nx <= 0 || ny <= 0) return cudaSuccess;
+  const size_t m = wsx + 1, n = wsy + 1, am = wsx + 1 + 2 * Sx, an = wsy + 1 + 2 * Sy;
+  const size_t smem = sizeof(double) * (m * n + am * an);
+  if (smem > 200 * 1024) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaFuncSetAttribute(intsearch_qfactor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  const long long npt = (long long)nx * ny;
+  const size_t nl = (m + am - 1) * (n + an - 1);
+  double* qraw = scratch;
+  double* maps = scratch + 2 * npt;
+  intsearch_qfactor_kernel<<<(int)npt, 256, smem, s>>>(f, g, W, Sx, Sy, gx0, gy0, nx, ny, (int)wsx, (int)wsy,
+                                                       stepx, stepy, maps, qraw);
+  (void)nl;
+  qfactor_normalise_kernel<<<1, 256, 0, s>>>(qraw, npt, qf);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Bad-subset filter after the per-node loop.  LocalICGNQuadtree: bad =
 // conv<0 | conv>99, then also conv > max(mean+std, 6) of the good codes;
 // Subpb1Quadtree: max(mean+0.25 std, 10).  U (and F for the first pass) become

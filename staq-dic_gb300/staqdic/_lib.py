@@ -83,7 +83,7 @@ def load(build_if_missing=True):
     L.stdic_integer_search_grid.argtypes = [_c.c_int, _c.c_int, _i32, _d, _d, _i32, _i32,
                                             _c.POINTER(_c.c_int), _c.POINTER(_c.c_int)]
     L.stdic_integer_search.argtypes = [_vp, _vp, _vp, _c.c_int, _c.c_int, _i32, _d, _d, _i32, _i32,
-                                       _vp, _vp, _vp, _vp, _vp, _vp]
+                                       _vp, _vp, _vp, _vp, _vp, _vp, _vp]
     L.stdic_icgn_local.argtypes = [_vp, _c.POINTER(Frame), _vp, _vp, _c.c_int, _c.c_int, _vp,
                                    _c.c_double, _vp, _vp, _vp, _vp, _vp, _vp, _c.c_int]
     L.stdic_icgn_subsets.argtypes = [_vp, _c.POINTER(Frame), _vp, _vp, _c.c_int, _c.c_int, _vp,

@@ -142,11 +142,14 @@ def _pair(v):
 
 
 def funIntegerSearch(f, g, tempSizeOfSearchRegion, gridx, gridy, winsize, winstepsize,
-                     tempNoOfInitPt=0, *varargin, ctx=None):
+                     tempNoOfInitPt=0, *varargin, ctx=None, qfactors=True):
     """[x,y,u,v,cc] = funIntegerSearch(f,g,S,gridx,gridy,winsize,winstepsize,0,..).
 
-    cc is a dict with 'max' (cc.max) and 'peak' (the 1-based integer argmax
-    (row, col) of each cropped correlation map, ny x nx x 2)."""
+    cc is a dict with 'max' (cc.max), 'qfactors' (cc.qfactors: (ny*nx) x 2, the
+    normalised PCE and PPE of each point's full correlation map, rows in the
+    reference's point order, x fastest; omitted with qfactors=False) and 'peak'
+    (the 1-based integer argmax (row, col) of each cropped correlation map,
+    ny x nx x 2)."""
     if tempNoOfInitPt != 0:
         raise NotImplementedError("only the whole-field mode (tempNoOfInitPt = 0) is on this path")
     c = _ctx(ctx)
@@ -166,10 +169,14 @@ def funIntegerSearch(f, g, tempSizeOfSearchRegion, gridx, gridy, winsize, winste
     pf, pg = b.ptr(f, np.float64), b.ptr(g, np.float64)
     outs = [b.out(None, (ny, nx), np.float64) for _ in range(5)]
     peak, pp = b.out(None, (ny, nx, 2), np.int32)
+    qf, pq = b.out(None, (nx * ny, 2), np.float64) if qfactors else (None, None)
     c.check(c.L.stdic_integer_search(c.h, pf, pg, W, H, I(S), D(gx), D(gy), I(ws), I(st),
-                                     *[o[1] for o in outs], pp), "funIntegerSearch")
+                                     *[o[1] for o in outs], pp, pq), "funIntegerSearch")
     x, y, u, v, cm = (o[0] for o in outs)
-    return x, y, u, v, {"max": cm, "peak": peak}
+    cc = {"max": cm, "peak": peak}
+    if qfactors:
+        cc["qfactors"] = qf
+    return x, y, u, v, cc
 
 
 # ---------------------------------------------------------------------------

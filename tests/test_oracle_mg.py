@@ -117,3 +117,51 @@ def test_multigrid_search_recovers_large_translation(mg):
     assert uG.shape == xG.shape and uG.size > 20
     assert np.max(np.abs(uG - shift[0])) < 0.5 and np.max(np.abs(vG - shift[1])) < 0.5
     assert np.min(pG) > 0.5
+
+
+def test_qfactors_restatement_matches_full_map_definition(oracle):
+    """cc.qfactors of the oracle (direct sums in C++) against the definition
+    written out on the FFT-based full normxcorr2 map of this module: PCE =
+    peak^2 / mean(cc_min^2) and PPE = 1 / entropy of the 30-bin histogram of
+    cc_min over [0, peak] (numpy's histogram has the same uniform bins, the
+    last one closed), then each column shifted and scaled to [0, 1]."""
+    from oracle import mg
+    from staqdic import workloads
+    w = workloads.uniform256(seed=0, size=128)
+    f, g = w["g"], w["f"]
+    S, ws, st = 6, 32, 16
+    raw, qf = oracle.integer_search_qfactors(f, g, S, (1, 128), (1, 128), ws, st)
+    gx, gy, nx, ny = oracle.intsearch_grid(128, 128, (S, S), (1, 128), (1, 128), (ws, ws), (st, st))
+    assert raw.shape == (nx * ny, 2) and nx * ny > 0
+    for t in range(nx * ny):
+        ix, iy = t % nx, t // nx
+        ii, jj = int(gx[0]) + ix * st, int(gy[0]) + iy * st
+        C = f[ii - 1:ii + ws, jj - 1:jj + ws]
+        D = g[ii - 1 - S:ii + ws + S, jj - 1 - S:jj + ws + S]
+        X = mg.normxcorr2_full(C, D)
+        cm = X - X.min()
+        peak = cm.max()
+        pce = peak ** 2 / np.mean(cm ** 2)
+        h, _ = np.histogram(cm, bins=30, range=(0.0, peak))
+        p = h[h > 0] / cm.size
+        ppe = 1.0 / np.sum(p * np.log(1.0 / p))
+        assert abs(raw[t, 0] - pce) <= 1e-8 * pce
+        assert abs(raw[t, 1] - ppe) <= 1e-8 * ppe
+    for k in range(2):
+        q = raw[:, k] - np.nanmin(raw[:, k])
+        assert np.allclose(qf[:, k], q / np.nanmax(q), rtol=0, atol=1e-12)
+
+
+def test_qfactors_constant_template_gives_inf_then_nan(oracle):
+    """A point where normxcorr2 throws holds [Inf Inf] before the
+    normalisation; Inf - min is Inf and Inf / Inf is NaN, so that point is
+    NaN and every other point 0 (funIntegerSearch.m:156,175-176)."""
+    from staqdic import workloads
+    w = workloads.uniform256(seed=0, size=128)
+    f = np.array(w["g"], copy=True, order="F")
+    f[:60, :60] = 0.5  # the first grid point's template is constant
+    raw, qf = oracle.integer_search_qfactors(f, w["f"], 6, (1, 128), (1, 128), 32, 16)
+    assert np.isinf(raw[0]).all()
+    assert np.isnan(qf[0]).all()
+    fin = ~np.isinf(raw[:, 0])
+    assert np.all(qf[fin] == 0)

@@ -12,6 +12,8 @@
  *   stdic_subpb1_subsets   func/funICGN_Subpb1.m:1-474 (N nodes at once)
  *   stdic_subpb1           func_quadtree/Subpb1Quadtree.m:1-191
  *   stdic_subpb2           func_quadtree/Subpb2Quadtree.m:1-413
+ *   stdic_quadtree_mesh    func_quadtree/GenerateQuadtreeMesh.m:18-133 (+ MeshSetUp.m,
+ *                          refinement/QrefineR.m)
  *   stdic_icgn_adjoint     no counterpart in the reference (gradient of the
  *                          ZNSSD cost of the IC-GN subsets)
  *
@@ -194,6 +196,27 @@ int stdic_subpb2(stdic_ctx* ctx, const double* coords, int N, const int32_t* ele
                  int gauss_order, double beta, double mu, const double* U, const double* F,
                  double alpha, double winstepsize, double tol, int maxit, double* Uhat,
                  int* iters);
+
+/* [DICmesh] of GenerateQuadtreeMesh.m:18-133 (func_quadtree/), started from
+ * the uniform mesh MeshSetUp.m builds on the search grid and refined with
+ * QrefineR.m (func_quadtree/refinement/): elements whose bounding box holds
+ * both mask values are split into four until their smaller side is at most
+ * element_min_size (DICmesh.elementMinSize), with at most one hanging node per
+ * edge; corners are reordered, hanging nodes stored in columns 5-8, elements
+ * with less than half their box in the mask removed, and the Dirichlet set
+ * markCoordHoleEdge built (refined and border elements, grown twice).  mask
+ * is DICpara.ImgRefMask (W x H, 0/1); x0, y0 are the ny x nx grids passed to
+ * MeshSetUp (row = y, whole pixels); winstepsize is max(DICpara.winstepsize).
+ * Outputs (each may be NULL; capacity[k] gives the rows each holds) are
+ * column-major: coords N x 2 (coordinatesFEM), elems E x 8 (elementsFEM),
+ * irregular nI x 3 (DICmesh.irregular) and dirichlet nd (ascending).  counts
+ * (host, 4) always receives N, E, nI and nd, so a call with NULL outputs sizes
+ * them.  Node and element numbering is the reference's. */
+int stdic_quadtree_mesh(stdic_ctx* ctx, const uint8_t* mask, int W, int H, const double* x0,
+                        const double* y0, int ny, int nx, double winstepsize,
+                        double element_min_size, double* coords, int32_t* elems,
+                        int32_t* irregular, int32_t* dirichlet, const int64_t* capacity,
+                        int64_t* counts);
 
 /* No reference counterpart (the batching of the chosen form across frame
  * pairs): funICGNQuadtree over N nodes for `frames` deformed frames at once,

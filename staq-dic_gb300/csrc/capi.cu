@@ -38,6 +38,8 @@ struct stdic_ctx {
   int tuning = 1;
   bool capturing = false;  // the stream is being captured into a CUDA graph
   long long wait_limit = 0;  // polls of a PCG grid-barrier wait (0: the default)
+  void* aux = nullptr;       // grow-only device scratch of the mesh generation
+  size_t aux_size = 0;
 };
 
 namespace {
@@ -210,6 +212,7 @@ int stdic_ctx_destroy(stdic_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->ws) cudaFree(c->ws);
+  if (c->aux) cudaFree(c->aux);
   if (c->scal) cudaFree(c->scal);
   if (c->scald) cudaFree(c->scald);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1216,6 +1219,94 @@ int stdic_subpb2(stdic_ctx* c, const double* coords, int N, const int32_t* elems
   if (hs[1] == 2) return fail(c, STDIC_E_TIMEOUT, "Subpb2Quadtree: grid barrier wait gave up");
   if (hs[1] == 3) return fail(c, STDIC_E_ARG, "Subpb2Quadtree: invalid node index or node in >16 elements");
   if (hs[1] == 1) return fail(c, STDIC_E_NOTCONV, "Subpb2Quadtree: PCG did not reach the tolerance");
+  return STDIC_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// GenerateQuadtreeMesh.m:18-133 on the uniform mesh of MeshSetUp.m.
+int stdic_quadtree_mesh(stdic_ctx* c, const uint8_t* mask, int W, int H, const double* x0, const double* y0,
+                        int ny, int nx, double winstepsize, double element_min_size, double* coords,
+                        int32_t* elems, int32_t* irregular, int32_t* dirichlet, const int64_t* capacity,
+                        int64_t* counts) {
+  if (!c) return STDIC_E_ARG;
+  if (!mask || W < 1 || H < 1 || !x0 || !y0 || ny < 2 || nx < 2 || !(winstepsize > 0) || !counts ||
+      ((coords || elems || irregular || dirichlet) && !capacity))
+    return fail(c, STDIC_E_ARG, "GenerateQuadtreeMesh: bad arguments (a grid of at least 2 x 2, step > 0)");
+  cudaSetDevice(c->device);
+  Plan pl;
+  const uint8_t* dm;
+  pl.in(mask, (size_t)W * H, (uint8_t**)&dm);
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  // the grids are read on the host
+  const size_t ng = (size_t)nx * ny;
+  std::vector<double> gx(ng), gy(ng);
+  for (int k = 0; k < 2; ++k) {
+    const double* src = k ? y0 : x0;
+    double* dst = k ? gy.data() : gx.data();
+    if (is_device_ptr(src)) {
+      cudaError_t e = cudaMemcpyAsync(dst, src, ng * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "GenerateQuadtreeMesh grid read");
+    } else {
+      std::memcpy(dst, src, ng * sizeof(double));
+    }
+  }
+  for (size_t k = 0; k < ng; ++k)
+    if (!std::isfinite(gx[k]) || !std::isfinite(gy[k]) || gx[k] != std::floor(gx[k]) || gy[k] != std::floor(gy[k]))
+      return fail(c, STDIC_E_ARG, "GenerateQuadtreeMesh: grid positions must be whole pixels");
+  auto grow = [c](size_t bytes) -> void* {
+    if (bytes > c->aux_size) {
+      if (c->aux) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->aux);
+        c->aux = nullptr;
+        c->aux_size = 0;
+      }
+      const size_t want = std::max(bytes, c->aux_size * 2);
+      if (cudaMalloc(&c->aux, want) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+      }
+      c->aux_size = want;
+    }
+    return c->aux;
+  };
+  stdic::QuadtreeMeshOut out;
+  const char* err = nullptr;
+  rc = stdic::quadtree_mesh_generate(dm, W, H, gx.data(), gy.data(), ny, nx, winstepsize, element_min_size, &out,
+                                     grow, c->stream, &c->launches, &err);
+  if (rc) return fail(c, rc, std::string("GenerateQuadtreeMesh: ") + (err ? err : "failed"));
+  const int64_t N = (int64_t)out.x.size(), E = (int64_t)out.elems.size(), nI = (int64_t)out.irregular.size(),
+                nd = (int64_t)out.dirichlet.size();
+  counts[0] = N; counts[1] = E; counts[2] = nI; counts[3] = nd;
+  const int64_t need[4] = {N, E, nI, nd};
+  void* const dst[4] = {coords, elems, irregular, dirichlet};
+  for (int k = 0; k < 4; ++k)
+    if (dst[k] && capacity[k] < need[k])
+      return fail(c, STDIC_E_ARG, "GenerateQuadtreeMesh: an output holds fewer rows than the mesh (see counts)");
+  // column-major host images of the outputs, then one copy each
+  std::vector<double> hc((size_t)2 * N);
+  for (int64_t k = 0; k < N; ++k) { hc[k] = out.x[k]; hc[N + k] = out.y[k]; }
+  std::vector<int32_t> he((size_t)8 * E), hi((size_t)3 * nI), hd(out.dirichlet.begin(), out.dirichlet.end());
+  for (int64_t e = 0; e < E; ++e)
+    for (int k = 0; k < 8; ++k) he[k * E + e] = out.elems[e][k];
+  for (int64_t i = 0; i < nI; ++i)
+    for (int k = 0; k < 3; ++k) hi[k * nI + i] = out.irregular[i][k];
+  const void* src[4] = {hc.data(), he.data(), hi.data(), hd.data()};
+  const size_t bytes[4] = {hc.size() * sizeof(double), he.size() * sizeof(int32_t), hi.size() * sizeof(int32_t),
+                           hd.size() * sizeof(int32_t)};
+  for (int k = 0; k < 4; ++k) {
+    if (!dst[k] || bytes[k] == 0) continue;
+    if (is_device_ptr(dst[k])) {
+      cudaError_t e = cudaMemcpyAsync(dst[k], src[k], bytes[k], cudaMemcpyHostToDevice, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "GenerateQuadtreeMesh output copy");
+    } else {
+      std::memcpy(dst[k], src[k], bytes[k]);
+    }
+  }
   return STDIC_OK;
 }
 

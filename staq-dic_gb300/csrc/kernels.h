@@ -1,7 +1,11 @@
 // Internal kernel interface of libstaqdic (not part of the public C ABI).
 #pragma once
+#include <array>
 #include <cstddef>
 #include <cstdint>
+#include <functional>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 namespace stdic {
@@ -186,6 +190,22 @@ cudaError_t launch_fill_nans(int N, const int32_t* elems, int E, const int* ptr,
 cudaError_t launch_copy_marked(const uint8_t* mark, int N, int width, const double* src, double* dst,
                                cudaStream_t s);
 cudaError_t launch_sub(const double* a, const double* b, double* out, long long n, cudaStream_t s);
+
+// Quadtree mesh generation (GenerateQuadtreeMesh.m with MeshSetUp.m).
+struct QuadtreeMeshOut {
+  std::vector<double> x, y;                       // node coordinates
+  std::vector<std::array<int, 8>> elems;          // elementsFEM rows
+  std::vector<std::array<int, 3>> irregular;      // [node_a node_b midnode]
+  std::vector<int> dirichlet;                     // markCoordHoleEdge, ascending
+};
+// mask: W x H device memory (0/1); gx, gy: the ny x nx search grids (host,
+// column-major, row = y) as MeshSetUp receives them; grow(bytes) returns
+// device scratch of at least that size.  Returns 0 or a STDIC_E_* code with
+// *err set.
+int quadtree_mesh_generate(const uint8_t* mask, int W, int H, const double* gx, const double* gy, int ny, int nx,
+                           double winstepsize, double element_min_size, QuadtreeMeshOut* out,
+                           const std::function<void*(size_t)>& grow, cudaStream_t s, long long* launches,
+                           const char** err);
 
 // Subpb2 (FEM).  All pointers are device pointers.
 struct Subpb2Args {

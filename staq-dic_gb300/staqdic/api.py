@@ -10,6 +10,7 @@ on the GPU through the C ABI (include/staqdic.h):
   LocalICGNQuadtree     func_quadtree/LocalICGNQuadtree.m:1-177
   Subpb1Quadtree        func_quadtree/Subpb1Quadtree.m:1-191
   Subpb2Quadtree        func_quadtree/Subpb2Quadtree.m:1-413
+  GenerateQuadtreeMesh  func_quadtree/GenerateQuadtreeMesh.m:18-133 (with MeshSetUp.m)
 
 Array conventions are MATLAB's: NumPy arrays indexed like the MATLAB array
 (0-based), laid out column-major (Fortran order) exactly as MATLAB stores them;
@@ -354,6 +355,37 @@ def Subpb2Quadtree(DICmesh, GaussPtOrder, beta, mu, U, F, udual, vdual, alpha, w
     if return_iters:
         return Uhat, int(iters.value)
     return Uhat
+
+
+def GenerateQuadtreeMesh(x0, y0, ImgRefMask, winstepsize, elementMinSize=2, ctx=None):
+    """DICmesh of GenerateQuadtreeMesh.m (stdic_quadtree_mesh): the uniform
+    mesh MeshSetUp.m builds on the search grids x0, y0 (N x M, row = y, as
+    MeshSetUp receives them), refined at the edges of ImgRefMask.  Returns a
+    dict with coordinatesFEM (N x 2), elementsFEM (E x 8 int32), irregular
+    (nI x 3), dirichlet and markCoordHoleEdge (the same set) and
+    elementMinSize, numbered as the reference numbers them."""
+    c = _ctx(ctx)
+    x0 = np.asfortranarray(x0, dtype=np.float64)
+    y0 = np.asfortranarray(y0, dtype=np.float64)
+    ny, nx = x0.shape
+    m = np.asfortranarray((np.asarray(ImgRefMask) != 0).astype(np.uint8))
+    W, H = m.shape
+    step = float(np.max(np.atleast_1d(winstepsize)))
+    counts = np.zeros(4, dtype=np.int64)
+    P = lambda a: a.ctypes.data if a is not None else None
+    c.check(c.L.stdic_quadtree_mesh(c.h, P(m), W, H, P(x0), P(y0), ny, nx, step, float(elementMinSize), None,
+                                    None, None, None, None, P(counts)), "GenerateQuadtreeMesh")
+    N, E, nI, nd = (int(v) for v in counts)
+    coords = np.empty((N, 2), order="F")
+    elems = np.empty((E, 8), dtype=np.int32, order="F")
+    irr = np.empty((nI, 3), dtype=np.int32, order="F")
+    dirichlet = np.empty(nd, dtype=np.int32)
+    cap = counts.copy()
+    c.check(c.L.stdic_quadtree_mesh(c.h, P(m), W, H, P(x0), P(y0), ny, nx, step, float(elementMinSize),
+                                    P(coords), P(elems), P(irr), P(dirichlet), P(cap), P(counts)),
+            "GenerateQuadtreeMesh")
+    return {"coordinatesFEM": coords, "elementsFEM": elems, "irregular": irr, "dirichlet": dirichlet,
+            "markCoordHoleEdge": dirichlet.copy(), "elementMinSize": elementMinSize}
 
 
 ADJ_MODES = {"recompute": _lib.STDIC_ADJ_RECOMPUTE, "store": _lib.STDIC_ADJ_STORE}

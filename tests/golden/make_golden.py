@@ -6,8 +6,10 @@ Run here (where the reference checkout and oracle/_ref exist):
 Writes
   circular_hole_pair.npz  the shipped 400x400 plate-with-hole pair (frames 000
       and 001 with their masks, decoded from the PackBits TIFFs) and, from
-      ``results_Circular_hole 040_ws32_st16.mat``, the quadtree DICmesh and the
-      reference's final U, F and ALSub1BadPtNum for that pair.
+      ``results_Circular_hole 040_ws32_st16.mat``, the quadtree DICmesh (with
+      the uniform grid x0, y0 it was refined from, elementMinSize and the
+      hanging-node list irregular) and the reference's final U, F and
+      ALSub1BadPtNum for that pair.
   ba_interp2_golden.npz   inputs and outputs of the reference's own
       ba_interp2.cpp (compiled unmodified in oracle/_ref) in double and single.
 """
@@ -90,7 +92,12 @@ def main(ref):
         U=np.asarray(m["ResultDisp"][0].U, dtype=np.float64),
         F=np.asarray(m["ResultDefGrad"][0].F, dtype=np.float64),
         ALSub1BadPtNum=np.asarray(m["ResultDisp"][0].ALSub1BadPtNum, dtype=np.int32),
-        winsize=np.int32(dp.winsize), winstepsize=np.int32(dp.winstepsize))
+        winsize=np.int32(dp.winsize), winstepsize=np.int32(dp.winstepsize),
+        # GenerateQuadtreeMesh's input (the uniform MeshSetUp grid and
+        # elementMinSize) and its hanging-node list
+        x0=np.asarray(dm.x0, dtype=np.float64), y0=np.asarray(dm.y0, dtype=np.float64),
+        elementMinSize=np.float64(dm.elementMinSize),
+        irregular=np.asarray(dm.irregular, dtype=np.int32).reshape(-1, 3))
 
     from oracle import oracle as orc
     from oracle import build as ob

@@ -362,3 +362,39 @@ def test_plain_is_deterministic(sd, ctx, golden):
     b = sd.icgn_subsets(d["U"], d["coordinatesFEM"], Dref, f, g, 32, 1e-2, precision="plain", ctx=ctx)
     for x, y in zip(a, b):
         assert np.array_equal(x, y, equal_nan=True)
+
+
+# ------------------------------------------------------- quadtree mesh generation
+def test_quadtree_mesh_reproduces_reference_mesh(sd, ctx):
+    """stdic_quadtree_mesh on the uniform grid, mask and step stored in the
+    reference's shipped result file gives that file's DICmesh exactly:
+    coordinatesFEM (numbering included), elementsFEM with its hanging-node
+    columns, irregular and the Dirichlet set."""
+    d = np.load(os.path.join(GOLD, "circular_hole_pair.npz"))
+    mesh = sd.GenerateQuadtreeMesh(d["x0"].T, d["y0"].T, d["ImgRefMask"], int(d["winstepsize"]),
+                                   float(d["elementMinSize"]), ctx=ctx)
+    assert np.array_equal(mesh["coordinatesFEM"], d["coordinatesFEM"])
+    assert np.array_equal(mesh["elementsFEM"], d["elementsFEM"])
+    assert np.array_equal(mesh["irregular"], d["irregular"])
+    assert np.array_equal(mesh["dirichlet"], d["dirichlet"])
+
+
+def test_quadtree_mesh_matches_oracle_on_synthetic_hole(sd, ctx):
+    """The 2048^2 plate with a hole on a 16 px grid against the oracle's
+    restatement (oracle/quadtree.py): identical mesh, hanging nodes and
+    Dirichlet set; every element at least elementMinSize on its smaller side."""
+    from oracle import quadtree as q
+    from staqdic import workloads
+    w = workloads.hole2048(size=1024)
+    mask = w["maskf"]
+    W, H = mask.shape
+    xs = np.arange(20, W - 20 + 1, 16, dtype=np.float64)
+    ys = np.arange(20, H - 20 + 1, 16, dtype=np.float64)
+    x0, y0 = np.meshgrid(xs, ys)  # N x M, row = y
+    mesh = sd.GenerateQuadtreeMesh(x0, y0, mask, 16, 2, ctx=ctx)
+    co, eo, io, do = q.generate_quadtree_mesh(x0, y0, mask, 16, 2)
+    assert mesh["elementsFEM"].shape[0] > 5000
+    assert np.array_equal(mesh["coordinatesFEM"], co)
+    assert np.array_equal(mesh["elementsFEM"], eo)
+    assert np.array_equal(mesh["irregular"], io)
+    assert np.array_equal(mesh["dirichlet"], do)

@@ -231,3 +231,20 @@ def test_oracle_fill_nans_rules(oracle):
     V2 = np.concatenate([U, [np.nan, np.nan]])
     out2 = oracle.fill_nans(c2, el, V2)
     assert np.all(np.isnan(out2[-2:]))
+
+
+def test_quadtree_mesh_restatement_reproduces_reference_mesh():
+    """GenerateQuadtreeMesh.m restated (oracle/quadtree.py) on the uniform grid,
+    mask, step and elementMinSize stored in the reference's shipped result file
+    gives that file's quadtree mesh exactly: the coordinates (node numbering
+    included), elementsFEM with its hanging-node columns, the irregular list
+    and the Dirichlet set markCoordHoleEdge."""
+    from oracle import quadtree as q
+    d = np.load(os.path.join(GOLD, "circular_hole_pair.npz"))
+    # DICmesh.x0/y0 are stored transposed by MeshSetUp.m
+    coords, els, irr, dirichlet = q.generate_quadtree_mesh(d["x0"].T, d["y0"].T, d["ImgRefMask"],
+                                                           int(d["winstepsize"]), float(d["elementMinSize"]))
+    assert np.array_equal(coords, d["coordinatesFEM"])
+    assert np.array_equal(els, d["elementsFEM"])
+    assert np.array_equal(irr, d["irregular"])
+    assert np.array_equal(dirichlet, d["dirichlet"])

@@ -14,6 +14,7 @@
  *   stdic_subpb2           func_quadtree/Subpb2Quadtree.m:1-413
  *   stdic_quadtree_mesh    func_quadtree/GenerateQuadtreeMesh.m:18-133 (+ MeshSetUp.m,
  *                          refinement/QrefineR.m)
+ *   stdic_por_gpr          func/funPOR_GPR.m:1-99
  *   stdic_icgn_adjoint     no counterpart in the reference (gradient of the
  *                          ZNSSD cost of the IC-GN subsets)
  *
@@ -217,6 +218,22 @@ int stdic_quadtree_mesh(stdic_ctx* ctx, const uint8_t* mask, int W, int H, const
                         double element_min_size, double* coords, int32_t* elems,
                         int32_t* irregular, int32_t* dirichlet, const int64_t* capacity,
                         int64_t* counts);
+
+/* [u_pred, alpha, beta_POD, beta_GPR] = funPOR_GPR(T_snap, t_train, t_pre, nB)
+ * (func/funPOR_GPR.m:1-99), the initial guess of the next frame that
+ * main_ALDIC_Quadtree_v2.m:185-196 predicts from the last five frames (once
+ * for u, once for v).  T_snap is nT x np (one snapshot per row), u_pred
+ * nT1 x np, both column-major; t_train (nT), t_pre (nT1), alpha, beta_pod and
+ * beta_gpr (nT1) are host memory (the scalars may be NULL).  The proper
+ * orthogonal decomposition is the reference's (its trapezoid inner product,
+ * nB leading modes); the regression of each mode coefficient over time
+ * follows fitrgp's documented model ('linear' basis, exact fit and
+ * prediction, squared-exponential kernel, noise sigma >= 2e-5, the documented
+ * starting point) with hyperparameters from a Nelder-Mead search of the
+ * exact marginal likelihood; MATLAB's optimiser itself is not reproduced. */
+int stdic_por_gpr(stdic_ctx* ctx, const double* T_snap, int nT, int64_t np, const double* t_train,
+                  const double* t_pre, int nT1, int nB, double* u_pred, double* alpha,
+                  double* beta_pod, double* beta_gpr);
 
 /* No reference counterpart (the batching of the chosen form across frame
  * pairs): funICGNQuadtree over N nodes for `frames` deformed frames at once,

@@ -1310,4 +1310,30 @@ int stdic_quadtree_mesh(stdic_ctx* c, const uint8_t* mask, int W, int H, const d
   return STDIC_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// funPOR_GPR.m: the next frame's field predicted from earlier frames.
+int stdic_por_gpr(stdic_ctx* c, const double* T_snap, int nT, int64_t np, const double* t_train,
+                  const double* t_pre, int nT1, int nB, double* u_pred, double* alpha, double* beta_pod,
+                  double* beta_gpr) {
+  if (!c) return STDIC_E_ARG;
+  if (!T_snap || !t_train || !t_pre || !u_pred || nT < 2 || np < 2 || nT1 < 1 || nB < 1)
+    return fail(c, STDIC_E_ARG, "funPOR_GPR: bad arguments");
+  cudaSetDevice(c->device);
+  Plan pl;
+  const double* dT;
+  double* dU;
+  unsigned char* ws;
+  pl.in(T_snap, (size_t)nT * np, (double**)&dT);
+  pl.out(u_pred, (size_t)nT1 * np, &dU);
+  pl.scratch(stdic::por_workspace_bytes(np, nT, nB), &ws);
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  const char* err = nullptr;
+  rc = stdic::por_gpr(dT, nT, np, t_train, t_pre, nT1, nB, dU, alpha, beta_pod, beta_gpr, ws, c->stream,
+                      &c->launches, &err);
+  if (rc) return fail(c, rc, err ? err : "funPOR_GPR failed");
+  return pl.finish(c);
+}
+
 }  // extern "C"

@@ -207,6 +207,13 @@ int quadtree_mesh_generate(const uint8_t* mask, int W, int H, const double* gx, 
                            const std::function<void*(size_t)>& grow, cudaStream_t s, long long* launches,
                            const char** err);
 
+// funPOR_GPR: T (nT x np) and u_pred (nT1 x np) device, column-major; t_train,
+// t_pre and the scalar outputs host; ws holds por_workspace_bytes(np, nT, nB).
+size_t por_workspace_bytes(long long np, int nT, int nB);
+int por_gpr(const double* T, int nT, long long np, const double* t_train, const double* t_pre, int nT1, int nB,
+            double* u_pred, double* alpha, double* beta_pod, double* beta_gpr, void* ws, cudaStream_t s,
+            long long* launches, const char** err);
+
 // Subpb2 (FEM).  All pointers are device pointers.
 struct Subpb2Args {
   const double* coords;

@@ -11,6 +11,7 @@ on the GPU through the C ABI (include/staqdic.h):
   Subpb1Quadtree        func_quadtree/Subpb1Quadtree.m:1-191
   Subpb2Quadtree        func_quadtree/Subpb2Quadtree.m:1-413
   GenerateQuadtreeMesh  func_quadtree/GenerateQuadtreeMesh.m:18-133 (with MeshSetUp.m)
+  funPOR_GPR            func/funPOR_GPR.m:1-99
 
 Array conventions are MATLAB's: NumPy arrays indexed like the MATLAB array
 (0-based), laid out column-major (Fortran order) exactly as MATLAB stores them;
@@ -386,6 +387,33 @@ def GenerateQuadtreeMesh(x0, y0, ImgRefMask, winstepsize, elementMinSize=2, ctx=
             "GenerateQuadtreeMesh")
     return {"coordinatesFEM": coords, "elementsFEM": elems, "irregular": irr, "dirichlet": dirichlet,
             "markCoordHoleEdge": dirichlet.copy(), "elementMinSize": elementMinSize}
+
+
+def funPOR_GPR(T_snap, t_train, t_pre, nB, ctx=None):
+    """[u_pred, alpha, beta_POD, beta_GPR] = funPOR_GPR(T_snap, t_train, t_pre, nB)
+    (stdic_por_gpr): T_snap is nT x np, u_pred nT1 x np.  A torch CUDA
+    T_snap keeps u_pred on the device."""
+    c = _ctx(ctx)
+    b = _Bufs()
+    if _is_torch(T_snap):
+        nT, npt = int(T_snap.shape[0]), int(T_snap.shape[1])
+        Tp = b.ptr(T_snap.t().contiguous().view(-1), np.float64)  # column-major
+    else:
+        T = np.asfortranarray(T_snap, dtype=np.float64)
+        nT, npt = T.shape
+        Tp = b.ptr(T, np.float64)
+    tt = np.ascontiguousarray(np.asarray(t_train, dtype=np.float64).ravel())
+    tp = np.ascontiguousarray(np.asarray(t_pre, dtype=np.float64).ravel())
+    nT1 = tp.size
+    like = T_snap if _is_torch(T_snap) else None
+    U, pU = b.out(like, (nT1, npt), np.float64)
+    alpha, bpod = _lib._c.c_double(0), _lib._c.c_double(0)
+    bgpr = np.empty(nT1)
+    c.check(c.L.stdic_por_gpr(c.h, Tp, nT, npt, tt.ctypes.data, tp.ctypes.data, nT1, int(nB), pU,
+                              _lib._c.byref(alpha), _lib._c.byref(bpod), bgpr.ctypes.data), "funPOR_GPR")
+    if _is_torch(U):
+        U = U.view(npt, nT1).t()
+    return U, alpha.value, bpod.value, bgpr
 
 
 ADJ_MODES = {"recompute": _lib.STDIC_ADJ_RECOMPUTE, "store": _lib.STDIC_ADJ_STORE}

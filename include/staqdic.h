@@ -90,7 +90,12 @@ typedef struct {
   int dtype;
 } stdic_frame;
 
-/* Context on CUDA device `device`. */
+/* Context on CUDA device `device`.  Its own stream is a blocking stream:
+ * work on it is ordered with the legacy default stream, so device buffers
+ * produced or consumed there (the default stream of most frameworks) need no
+ * extra synchronisation.  A call that stages host buffers returns after its
+ * results are on the host; a call on device buffers only returns after its
+ * work is queued on the context's stream. */
 int stdic_ctx_create(stdic_ctx** ctx, int device);
 int stdic_ctx_destroy(stdic_ctx* ctx);
 /* Use an external cudaStream_t (NULL restores the context's own stream). */

@@ -190,7 +190,9 @@ int stdic_ctx_create(stdic_ctx** out, int device) {
   c->device = device;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  // a blocking stream: ordered with the legacy default stream, on which the
+  // caller's framework usually produces and consumes device buffers
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamDefault);
   if (e == cudaSuccess) e = cudaMalloc(&c->scal, (64 + 512) * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c->scald, 8 * sizeof(double));
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);

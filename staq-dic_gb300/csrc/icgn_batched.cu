@@ -390,6 +390,24 @@ STDIC_DEV bool mask_crop_ok32(const Frame32& fr, long long x1, long long x3, lon
   return x1 >= 1 && x3 <= fr.W && y1 >= 1 && y3 <= fr.H;
 }
 
+// Keys (a = -1/2) weights of the four taps at fractional offset d in [0, 1),
+// in factored form: w0 = -d (1-d)^2 / 2, w1 = (1-d)(2 + 2d - 3d^2) / 2,
+// w2 = d (1 + 4d - 3d^2) / 2, w3 = -d^2 (1-d) / 2.  They equal the expanded
+// polynomials of ba_interp2.cpp, but in FP32 the expanded w0, w1 and w3 cancel
+// catastrophically as d -> 1 (terms of order 1 summing to order (1-d)^2):
+// there a weight of 1e-8 can come out as exactly 0, and an interpolated value
+// that is tiny but nonzero in FP64 becomes 0, which changes the subset's
+// selection of nonzero g pixels.  The factored forms keep every weight to a
+// few FP32 ulps of its value, and a weight is exactly 0 only where it is 0 in
+// exact arithmetic (d = 0).  1 - d is exact for d >= 1/2.
+STDIC_DEV void keys_weights(float d, float& w0, float& w1, float& w2, float& w3) {
+  const float e = 1.f - d, hd = 0.5f * d;
+  w0 = -hd * e * e;
+  w1 = 0.5f * e * fmaf(d, fmaf(-3.f, d, 2.f), 2.f);
+  w2 = hd * fmaf(d, fmaf(-3.f, d, 4.f), 1.f);
+  w3 = -hd * d * e;
+}
+
 // Bicubic sample of g at (iu + su, iv + sv): integer base + FP32 offset.
 STDIC_DEV float cubic32(const float* __restrict__ g, int W, int H, int iu, float su, int iv,
                         float sv) {
@@ -399,11 +417,9 @@ STDIC_DEV float cubic32(const float* __restrict__ g, int W, int H, int iu, float
   // [3, W-2] x [3, H-2], the clamp only guards FP32 rounding at that edge
   const int xb = min(max(iu + (int)fu - 2, 0), W - 4);
   const int yb = min(max(iv + (int)fv - 2, 0), H - 4);
-  const float dx2 = dx * dx, dx3 = dx2 * dx, dy2 = dy * dy, dy3 = dy2 * dy;
-  const float wx0 = 0.5f * (-dx + 2.f * dx2 - dx3), wx1 = 0.5f * (2.f - 5.f * dx2 + 3.f * dx3);
-  const float wx2 = 0.5f * (dx + 4.f * dx2 - 3.f * dx3), wx3 = 0.5f * (-dx2 + dx3);
-  const float wy0 = 0.5f * (-dy + 2.f * dy2 - dy3), wy1 = 0.5f * (2.f - 5.f * dy2 + 3.f * dy3);
-  const float wy2 = 0.5f * (dy + 4.f * dy2 - 3.f * dy3), wy3 = 0.5f * (-dy2 + dy3);
+  float wx0, wx1, wx2, wx3, wy0, wy1, wy2, wy3;
+  keys_weights(dx, wx0, wx1, wx2, wx3);
+  keys_weights(dy, wy0, wy1, wy2, wy3);
   const float* r = g + (long long)yb * W + xb;
   const float s0 = wx0 * __ldg(r) + wx1 * __ldg(r + 1) + wx2 * __ldg(r + 2) + wx3 * __ldg(r + 3);
   r += W;
@@ -517,11 +533,9 @@ STDIC_DEV float cubic_tile(const float* __restrict__ gt, int gtw, int gth, int g
   const int xb = min(max(iu + (int)fu - 2, 0), W - 4);
   const int yb = min(max(iv + (int)fv - 2, 0), H - 4);
   const int lx = min(max(xb - gx0, 0), gtw - 4), ly = min(max(yb - gy0, 0), gth - 4);
-  const float dx2 = dx * dx, dx3 = dx2 * dx, dy2 = dy * dy, dy3 = dy2 * dy;
-  const float wx0 = 0.5f * (-dx + 2.f * dx2 - dx3), wx1 = 0.5f * (2.f - 5.f * dx2 + 3.f * dx3);
-  const float wx2 = 0.5f * (dx + 4.f * dx2 - 3.f * dx3), wx3 = 0.5f * (-dx2 + dx3);
-  const float wy0 = 0.5f * (-dy + 2.f * dy2 - dy3), wy1 = 0.5f * (2.f - 5.f * dy2 + 3.f * dy3);
-  const float wy2 = 0.5f * (dy + 4.f * dy2 - 3.f * dy3), wy3 = 0.5f * (-dy2 + dy3);
+  float wx0, wx1, wx2, wx3, wy0, wy1, wy2, wy3;
+  keys_weights(dx, wx0, wx1, wx2, wx3);
+  keys_weights(dy, wy0, wy1, wy2, wy3);
   const float* r = gt + ly * gtw + lx;
   const float s0 = wx0 * r[0] + wx1 * r[1] + wx2 * r[2] + wx3 * r[3];
   r += gtw;

@@ -129,6 +129,7 @@ class Context:
             raise StdicError(rc, "stdic_ctx_create failed (no CUDA device %d?)" % device)
         self.h = h
         self.device = device
+        self._torch_stream = None
 
     def check(self, rc, what):
         if rc != STDIC_OK:
@@ -136,7 +137,11 @@ class Context:
             raise StdicError(rc, "%s: %s" % (what, msg))
 
     def set_stream(self, stream_ptr):
+        """Run the library's work on the cudaStream_t stream_ptr (None or 0:
+        the context's own stream, which is ordered with the legacy default
+        stream)."""
         self.check(self.L.stdic_ctx_set_stream(self.h, _vp(stream_ptr or 0)), "set_stream")
+        self._torch_stream = stream_ptr or None
 
     def set_wait_limit(self, polls):
         """Bound (polls) of the Subpb2 PCG grid-barrier waits; 0 = default 2^24."""

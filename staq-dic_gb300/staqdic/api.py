@@ -46,15 +46,30 @@ def _is_torch(a):
 
 
 class _Bufs:
-    """Keeps the buffers of one call alive and hands out raw pointers."""
+    """Keeps the buffers of one call alive and hands out raw pointers.
 
-    def __init__(self):
+    A torch CUDA buffer binds the context to torch's current stream first, so
+    torch's producers of the inputs and consumers of the outputs are ordered
+    with the call without a synchronisation (the library synchronises only
+    when it stages host buffers).  torch's default stream is the legacy
+    default stream, which the context's own (blocking) stream is already
+    ordered with: that case keeps the context's own stream."""
+
+    def __init__(self, ctx):
         self.keep = []
+        self.ctx = ctx
+
+    def _bind(self, t):
+        if t.is_cuda:
+            s = torch.cuda.current_stream(t.device).cuda_stream or None
+            if getattr(self.ctx, "_torch_stream", None) != s:
+                self.ctx.set_stream(s)
 
     def ptr(self, a, dtype):
         if a is None:
             return None
         if _is_torch(a):
+            self._bind(a)
             tdt = {np.float64: torch.float64, np.float32: torch.float32, np.int32: torch.int32,
                    np.uint8: torch.uint8}[np.dtype(dtype).type]
             if a.dtype != tdt or not a.is_contiguous():
@@ -68,6 +83,7 @@ class _Bufs:
     def out(self, like, shape, dtype):
         """Output buffer on the device when `like` is a CUDA tensor, else NumPy."""
         if _is_torch(like) and like.is_cuda:
+            self._bind(like)
             tdt = {np.float64: torch.float64, np.float32: torch.float32, np.int32: torch.int32,
                    np.uint8: torch.uint8}[np.dtype(dtype).type]
             t = torch.empty(int(np.prod(shape)), dtype=tdt, device=like.device)
@@ -108,7 +124,7 @@ def ba_interp2(F, X, Y, method="cubic", ctx=None):
     P = int(np.prod(shp[2:])) if len(shp) > 2 else 1
     xs = tuple(X.shape)
     n = int(np.prod(xs))
-    b = _Bufs()
+    b = _Bufs(c)
     pF, pX, pY = b.ptr(F, dt), b.ptr(X, dt), b.ptr(Y, dt)
     out_shape = xs + tuple(shp[2:])
     Z, pZ = b.out(X, out_shape, dt)
@@ -125,7 +141,7 @@ def funImgGradient(ImgRef, ImgDef=None, ImgRefMask=None, ctx=None, dtype=None):
         ImgRefMask = np.ones((W, H), dtype=np.uint8, order="F")
     if dtype is None:
         dtype = np.float32 if ImgRef.dtype == np.float32 else np.float64
-    b = _Bufs()
+    b = _Bufs(c)
     pi = b.ptr(ImgRef, dtype)
     pm = b.ptr((np.asarray(ImgRefMask) != 0).astype(np.uint8), np.uint8)
     dx, pdx = b.out(None, (W - 6, H - 6), dtype)
@@ -167,7 +183,7 @@ def funIntegerSearch(f, g, tempSizeOfSearchRegion, gridx, gridy, winsize, winste
     c.check(c.L.stdic_integer_search_grid(W, H, I(S), D(gx), D(gy), I(ws), I(st),
                                           _lib._c.byref(nx), _lib._c.byref(ny)), "grid")
     nx, ny = nx.value, ny.value
-    b = _Bufs()
+    b = _Bufs(c)
     pf, pg = b.ptr(f, np.float64), b.ptr(g, np.float64)
     outs = [b.out(None, (ny, nx), np.float64) for _ in range(5)]
     peak, pp = b.out(None, (ny, nx, 2), np.int32)
@@ -216,7 +232,7 @@ def LocalICGNQuadtree(U0, coordinatesFEM, Df, ImgRef, ImgDef, DICpara, ICGNmetho
     prec = PRECISIONS[precision]
     dtype = _data_dtype(prec, ImgRef)
     N = _nodes(coordinatesFEM)
-    b = _Bufs()
+    b = _Bufs(c)
     fr = _frame(b, Df, ImgRef, ImgDef, dtype)
     wl = DICpara.get("winsize_per_node")
     ws = int(DICpara["winsize"]) if wl is None else int(max(int(DICpara["winsize"]), int(np.max(wl))))
@@ -264,7 +280,7 @@ def icgn_subsets(U0, coordinatesFEM, Df, ImgRef, ImgDef, winsize, tol, precision
     prec = PRECISIONS[precision]
     dtype = _data_dtype(prec, ImgRef)
     N = _nodes(coordinatesFEM)
-    b = _Bufs()
+    b = _Bufs(c)
     fr = _frame(b, Df, ImgRef, ImgDef, dtype)
     ws = int(winsize) if ws_list is None else int(max(int(winsize), int(np.max(ws_list))))
     like = U0 if _is_torch(U0) else None
@@ -286,7 +302,7 @@ def subpb1_subsets(UOld, FOld, vdual, coordinatesFEM, Df, ImgRef, ImgDef, winsiz
     prec = PRECISIONS[precision]
     dtype = _data_dtype(prec, ImgRef)
     N = _nodes(coordinatesFEM)
-    b = _Bufs()
+    b = _Bufs(c)
     fr = _frame(b, Df, ImgRef, ImgDef, dtype)
     like = UOld if _is_torch(UOld) else None
     U, pU = b.out(like, (2 * N,), np.float64)
@@ -312,7 +328,7 @@ def Subpb1Quadtree(UOld, FOld, udual, vdual, coordinatesFEM, Df, ImgRef, ImgDef,
     prec = PRECISIONS[precision]
     dtype = _data_dtype(prec, ImgRef)
     N = _nodes(coordinatesFEM)
-    b = _Bufs()
+    b = _Bufs(c)
     fr = _frame(b, Df, ImgRef, ImgDef, dtype)
     wl = DICpara["winsize_List"]
     like = UOld if _is_torch(UOld) else None
@@ -342,7 +358,7 @@ def Subpb2Quadtree(DICmesh, GaussPtOrder, beta, mu, U, F, udual, vdual, alpha, w
     E = int(elems.shape[0])
     nd = 0 if dirichlet is None else int(np.asarray(dirichlet).size) if not _is_torch(dirichlet) else dirichlet.numel()
     nn = 0 if neumann is None or np.asarray(neumann).size == 0 else int(np.asarray(neumann).reshape(-1, 4).shape[0])
-    b = _Bufs()
+    b = _Bufs(c)
     like = U if _is_torch(U) else None
     Uhat, pu = b.out(like, (2 * N,), np.float64)
     iters = _lib._c.c_int(0)
@@ -394,7 +410,7 @@ def funPOR_GPR(T_snap, t_train, t_pre, nB, ctx=None):
     (stdic_por_gpr): T_snap is nT x np, u_pred nT1 x np.  A torch CUDA
     T_snap keeps u_pred on the device."""
     c = _ctx(ctx)
-    b = _Bufs()
+    b = _Bufs(c)
     if _is_torch(T_snap):
         nT, npt = int(T_snap.shape[0]), int(T_snap.shape[1])
         Tp = b.ptr(T_snap.t().contiguous().view(-1), np.float64)  # column-major
@@ -430,7 +446,7 @@ def icgn_adjoint(U, F, coordinatesFEM, ImgRef, ImgDef, winsize, ImgRefMask=None,
     dtype = _data_dtype(prec, ImgRef)
     N = _nodes(coordinatesFEM)
     W, H = size if size is not None else _shape2(ImgRef)
-    b = _Bufs()
+    b = _Bufs(c)
     fr = Frame()
     fr.f = b.ptr(ImgRef, dtype)
     fr.g = b.ptr(ImgDef, dtype)
@@ -466,7 +482,7 @@ def icgn_subsets_frames(U0_list, coordinatesFEM, Df, ImgRef, ImgDef_list, winsiz
     P = len(ImgDef_list)
     N = _nodes(coordinatesFEM)
     dtype = np.float32
-    b = _Bufs()
+    b = _Bufs(c)
     g = np.concatenate([np.asarray(x, dtype=dtype).ravel(order="F") for x in ImgDef_list])
     fr = _frame(b, Df, ImgRef, g, dtype)
     U0 = np.concatenate([np.asarray(u, dtype=np.float64).ravel() for u in U0_list])
@@ -487,7 +503,7 @@ def nodal_strain(coordinatesFEM, elementsFEM, U, GaussPtOrder=2, ctx=None):
     """F (4N) = [du/dx dv/dx du/dy dv/dy] per node from the element Gauss-point
     strains (stdic_nodal_strain)."""
     c = _ctx(ctx)
-    b = _Bufs()
+    b = _Bufs(c)
     N = _nodes(coordinatesFEM)
     E = int(np.asarray(elementsFEM).shape[0])
     like = U if _is_torch(U) else None
@@ -500,7 +516,7 @@ def nodal_strain(coordinatesFEM, elementsFEM, U, GaussPtOrder=2, ctx=None):
 def fill_nans(coordinatesFEM, elementsFEM, U, ctx=None):
     """U (2N) with its NaN nodes filled from their mesh neighbours (stdic_fill_nans)."""
     c = _ctx(ctx)
-    b = _Bufs()
+    b = _Bufs(c)
     N = _nodes(coordinatesFEM)
     E = int(np.asarray(elementsFEM).shape[0])
     out = np.array(U, dtype=np.float64).ravel().copy()
@@ -516,7 +532,7 @@ def admm(DICmesh, Df, ImgRef, ImgDef, winsize_List, U2, F2, udual, vdual, mu, be
     c = _ctx(ctx)
     prec = PRECISIONS[precision]
     dtype = _data_dtype(prec, ImgRef)
-    b = _Bufs()
+    b = _Bufs(c)
     fr = _frame(b, Df, ImgRef, ImgDef, dtype)
     coords = DICmesh["coordinatesFEM"]
     elems = DICmesh["elementsFEM"]

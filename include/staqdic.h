@@ -7,6 +7,7 @@
  *   stdic_interp_bicubic   ba_interp2.cpp:318-335 (mexFunction) / :184-234
  *   stdic_img_gradient     func/funImgGradient.m:1-88
  *   stdic_integer_search   func/funIntegerSearch.m:3-203 + func/findpeak.m:1-68
+ *   stdic_integer_search_mg func/funIntegerSearchMg.m:3-343 (+ findpeak.m, gridfit.m 'springs')
  *   stdic_icgn_subsets     func_quadtree/funICGNQuadtree.m:1-451 (N nodes at once)
  *   stdic_icgn_local       func_quadtree/LocalICGNQuadtree.m:1-177
  *   stdic_subpb1_subsets   func/funICGN_Subpb1.m:1-474 (N nodes at once)
@@ -147,6 +148,29 @@ int stdic_integer_search(stdic_ctx* ctx, const double* f, const double* g, int W
                          const int S[2], const double gridx[2], const double gridy[2],
                          const int winsize[2], const int winstepsize[2], double* x, double* y,
                          double* u, double* v, double* cc, int32_t* peak_rc, double* qfactors);
+
+/* [xGrid, yGrid, uGrid, vGrid, cc] = funIntegerSearchMg(f, g, gridx, gridy, winsize,
+ * winstepsize) (func/funIntegerSearchMg.m:3-343, the multigrid search that
+ * IntegerSearch.m:125 calls for large displacements): normxcorr2 of the whole
+ * region, then blocks halved level by level, each searched within +-5 px of
+ * its parent's shift, and the block-centre displacements fitted to the node
+ * grid by gridfit with the springs regularizer.  f, g are W x H double;
+ * gridx, gridy the [first last] region (1-based); winstepsize [x y].  The node
+ * grid is chosen inside the routine: counts receives [nx ny], and x, y, u, v,
+ * cc (cc.max; each optional) receive ny x nx column-major arrays (row = y).
+ * capacity is the number of elements each given output holds;
+ * (floor((gridx[1]-gridx[0])/winstepsize[0]) + 1) *
+ * (floor((gridy[1]-gridy[0])/winstepsize[1]) + 1) always suffices.  The
+ * reference's cc.qfactors (quality factors of the last level's maps) are not
+ * produced: its caller on this path does not read them.  Errors where the
+ * reference raises: a region too small for the border gaps or wider than 4096
+ * px, a constant or non-finite region at level 1, fewer than 3 blocks for
+ * gridfit (STDIC_E_ARG); STDIC_E_NOTCONV if the gridfit solve misses its
+ * tolerance. */
+int stdic_integer_search_mg(stdic_ctx* ctx, const double* f, const double* g, int W, int H,
+                            const double gridx[2], const double gridy[2], int winsize,
+                            const double winstepsize[2], double* x, double* y, double* u, double* v,
+                            double* cc, int64_t capacity, int32_t counts[2]);
 
 /* LocalICGNQuadtree(U0, coordinatesFEM, Df, ImgRef, ImgDef, DICpara, 'GaussNewton', tol)
  * without its NaN-fill tail (out of this path): U (2N) and F (4N) carry NaN at

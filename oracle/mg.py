@@ -281,8 +281,9 @@ def funIntegerSearchMg(f, g, gridx, gridy, winsize, winstepsize):
             nxf, nyf = list(bxf), list(byf)
             nxg = [bxf[0] + cu, bxf[1] + cu]
             nyg = [byf[0] + cv, byf[1] + cv]
-            if np.isfinite(cu) and np.isfinite(cv):
-                clamp(nxf, nxg, nyf, nyg)
+            # the reference runs the clamp for every block: NaN comparisons
+            # are false, and the odd-width fix still trims the f range
+            clamp(nxf, nxg, nyf, nyg)
             blocks.append((nxf, nxg, nyf, nyg, cu, cv))
         wx, wy = wxn, wyn
         ratio = wx / wy
@@ -292,8 +293,9 @@ def funIntegerSearchMg(f, g, gridx, gridy, winsize, winstepsize):
     tu, tv, tp = np.array(us), np.array(vs), np.array(phis)
     ix1, ix2 = int(np.argmin(tx)), int(np.argmax(tx))
     iy1, iy2 = int(np.argmin(ty)), int(np.argmax(ty))
-    gx1 = math.ceil(1 + 1.25 * winsize + tu[ix1]); gx2 = math.ceil(1 + 1.25 * winsize + tu[ix2])
-    gy1 = math.ceil(1 + 1.25 * winsize + tv[iy1]); gy2 = math.ceil(1 + 1.25 * winsize + tv[iy2])
+    # np.ceil keeps a NaN shift NaN (MATLAB's ceil), and NaN comparisons are false
+    gx1 = np.ceil(1 + 1.25 * winsize + tu[ix1]); gx2 = np.ceil(1 + 1.25 * winsize + tu[ix2])
+    gy1 = np.ceil(1 + 1.25 * winsize + tv[iy1]); gy2 = np.ceil(1 + 1.25 * winsize + tv[iy2])
     if gridx[0] < gx1: gridx[0] = gx1
     if gridy[0] < gy1: gridy[0] = gy1
     if gridx[1] > W - gx2 + 1: gridx[1] = W - gx2 + 1

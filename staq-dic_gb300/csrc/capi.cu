@@ -1314,6 +1314,80 @@ int stdic_quadtree_mesh(stdic_ctx* c, const uint8_t* mask, int W, int H, const d
 
 
 // ---------------------------------------------------------------------------
+// funIntegerSearchMg.m: multigrid integer search, node grid chosen inside.
+int stdic_integer_search_mg(stdic_ctx* c, const double* f, const double* g, int W, int H, const double gridx[2],
+                            const double gridy[2], int winsize, const double winstepsize[2], double* x, double* y,
+                            double* u, double* v, double* cc, int64_t capacity, int32_t counts[2]) {
+  if (!c) return STDIC_E_ARG;
+  if (!f || !g || W < 8 || H < 8 || !gridx || !gridy || winsize < 2 || !winstepsize || !(winstepsize[0] > 0) ||
+      !(winstepsize[1] > 0) || !counts || ((x || y || u || v || cc) && capacity < 4))
+    return fail(c, STDIC_E_ARG, "funIntegerSearchMg: bad arguments");
+  cudaSetDevice(c->device);
+  Plan pl;
+  const double *df, *dg;
+  unsigned char* fixed;
+  pl.in(f, (size_t)W * H, (double**)&df);
+  pl.in(g, (size_t)W * H, (double**)&dg);
+  pl.scratch(stdic::mg_fixed_workspace_bytes(W, H), &fixed);
+  int rc = pl.commit(c);
+  if (rc) return rc;
+  auto grow = [c](size_t bytes) -> void* {
+    if (bytes > c->aux_size) {
+      if (c->aux) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->aux);
+        c->aux = nullptr;
+        c->aux_size = 0;
+      }
+      const size_t want = std::max(bytes, c->aux_size * 2);
+      if (cudaMalloc(&c->aux, want) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+      }
+      c->aux_size = want;
+    }
+    return c->aux;
+  };
+  stdic::MgSearchOut out;
+  const char* err = nullptr;
+  rc = stdic::integer_search_mg(df, dg, W, H, gridx, gridy, winsize, winstepsize, fixed, grow, c->stream,
+                                &c->launches, &out, &err);
+  if (rc) {
+    const int code = rc == -1 ? STDIC_E_ARG
+                     : rc == -3 ? STDIC_E_NOMEM
+                     : rc == -5 ? STDIC_E_TIMEOUT
+                     : rc == -6 ? STDIC_E_NOTCONV
+                                : STDIC_E_CUDA;
+    return fail(c, code, std::string("funIntegerSearchMg: ") + (err ? err : "failed"));
+  }
+  counts[0] = out.nx;
+  counts[1] = out.ny;
+  const int64_t ng = (int64_t)out.nx * out.ny;
+  if ((x || y || u || v || cc) && capacity < ng)
+    return fail(c, STDIC_E_ARG, "funIntegerSearchMg: the outputs hold fewer elements than the node grid (see counts)");
+  // ny x nx column-major (row = y), as meshgrid(xList, yList) and gridfit give them
+  std::vector<double> hx(ng), hy(ng);
+  for (int i = 0; i < out.nx; ++i)
+    for (int j = 0; j < out.ny; ++j) {
+      hx[j + (int64_t)out.ny * i] = out.xnodes[i];
+      hy[j + (int64_t)out.ny * i] = out.ynodes[j];
+    }
+  const double* src[5] = {hx.data(), hy.data(), out.x3.data(), out.x3.data() + ng, out.x3.data() + 2 * ng};
+  double* dst[5] = {x, y, u, v, cc};
+  for (int k = 0; k < 5; ++k) {
+    if (!dst[k]) continue;
+    if (is_device_ptr(dst[k])) {
+      cudaError_t e = cudaMemcpyAsync(dst[k], src[k], sizeof(double) * ng, cudaMemcpyHostToDevice, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "funIntegerSearchMg output copy");
+    } else {
+      std::memcpy(dst[k], src[k], sizeof(double) * ng);
+    }
+  }
+  return STDIC_OK;
+}
+
+// ---------------------------------------------------------------------------
 // funPOR_GPR.m: the next frame's field predicted from earlier frames.
 int stdic_por_gpr(stdic_ctx* c, const double* T_snap, int nT, int64_t np, const double* t_train,
                   const double* t_pre, int nT1, int nB, double* u_pred, double* alpha, double* beta_pod,

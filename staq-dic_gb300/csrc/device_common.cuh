@@ -42,6 +42,37 @@ STDIC_DEV void cta_exclusive_scan(const int* in, int* out, int n) {
   if (threadIdx.x == blockDim.x - 1) out[n] = acc;
 }
 
+// findpeak.m:40-68 on the 3 x 3 neighbourhood of a correlation maximum,
+// v9[(dr+1) + 3 (dc+1)] at row offset dr and column offset dc: the least-
+// squares quadratic [1 x y xy x^2 y^2] (x = column, y = row offset) in the
+// closed form of that fixed 9-point design, its stationary point (xo, yo)
+// and value there.  Returns false (the peak stays on the sample) when the fit
+// moves it by more than one sample; otherwise the offsets are rounded to
+// 1/1000 first, as the reference does, and the value is taken there.
+STDIC_DEV bool findpeak_fit3(const double* v9, double* xo_out, double* yo_out, double* maxf) {
+  double s0 = 0, sx = 0, sy = 0, sxy = 0, sxx = 0, syy = 0;
+  for (int dc = -1; dc <= 1; ++dc)
+    for (int dr = -1; dr <= 1; ++dr) {
+      const double uu = v9[(dr + 1) + 3 * (dc + 1)];
+      s0 += uu; sx += dc * uu; sy += dr * uu; sxy += dc * dr * uu;
+      sxx += dc * dc * uu; syy += dr * dr * uu;
+    }
+  const double A2 = sx / 6, A3 = sy / 6, A4 = sxy / 4;
+  const double Sv = (sxx + syy) / 2 - (2.0 / 3.0) * s0;
+  const double Dd = (sxx - syy) / 2;
+  const double A5 = (Sv + Dd) / 2, A6 = (Sv - Dd) / 2;
+  const double A1 = (s0 - 6 * Sv) / 9;
+  double xo = (-A3 * A4 + 2 * A6 * A2) / (A4 * A4 - 4 * A5 * A6);
+  double yo = -1 / (A4 * A4 - 4 * A5 * A6) * (A4 * A2 - 2 * A5 * A3);
+  if (fabs(xo) > 1 || fabs(yo) > 1) return false;
+  xo = round(1000 * xo) / 1000;
+  yo = round(1000 * yo) / 1000;
+  *xo_out = xo;
+  *yo_out = yo;
+  *maxf = A1 + xo * A2 + yo * A3 + xo * yo * A4 + xo * xo * A5 + yo * yo * A6;
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // Keys cubic (a = -1/2) interpolation with clamp-to-edge borders, evaluated in
 // the exact operation order of ba_interp2.cpp:188-233 with every product and

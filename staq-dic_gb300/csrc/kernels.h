@@ -191,6 +191,34 @@ cudaError_t launch_copy_marked(const uint8_t* mark, int N, int width, const doub
                                cudaStream_t s);
 cudaError_t launch_sub(const double* a, const double* b, double* out, long long n, cudaStream_t s);
 
+// FP64 complex FFTs (fft.cu): tw holds L/2 twiddles exp(-2 pi i k / L) made
+// by launch_fft_twiddles; rows transforms of length L (a power of two, at most
+// kFftMaxLen) in place, the inverse unscaled; out = in^T (rows x cols in).
+constexpr int kFftMaxLen = 8192;
+cudaError_t launch_fft_twiddles(double2* tw, int L, cudaStream_t s);
+cudaError_t launch_fft_rows(double2* data, long long rows, int L, const double2* tw, bool inverse, cudaStream_t s);
+cudaError_t launch_transpose_c(const double2* in, double2* out, int rows, int cols, cudaStream_t s);
+
+// Multigrid integer search (funIntegerSearchMg.m).  fixed_ws holds
+// mg_fixed_workspace_bytes(W, H) bytes (the integral images); grow(bytes)
+// returns device scratch of at least that size (it may move between calls).
+// Returns 0, -1 (argument or a MATLAB error of the reference, *err says
+// which), -2 (CUDA), -3 (allocation), -5 (a bounded wait gave up) or -6 (the
+// gridfit solve did not converge).
+struct MgSearchOut {
+  int nx = 0, ny = 0;                // node grid
+  std::vector<double> xnodes, ynodes;
+  std::vector<double> x3;            // u, v, cc.max on the grid, each ny x nx column-major
+  std::vector<double> blocks;        // 5 x nblocks: final-level block centre x, y and u, v, cc.max
+  long long nblocks = 0;
+  double level1_u = 0, level1_v = 0; // the whole-region shift of level 1
+  int cg_iters = 0;
+};
+size_t mg_fixed_workspace_bytes(int W, int H);
+int integer_search_mg(const double* f, const double* g, int W, int H, const double gridx[2], const double gridy[2],
+                      int winsize, const double step[2], void* fixed_ws, const std::function<void*(size_t)>& grow,
+                      cudaStream_t s, long long* launches, MgSearchOut* out, const char** err);
+
 // Quadtree mesh generation (GenerateQuadtreeMesh.m with MeshSetUp.m).
 struct QuadtreeMeshOut {
   std::vector<double> x, y;                       // node coordinates

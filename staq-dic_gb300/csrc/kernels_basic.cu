@@ -375,26 +375,14 @@ __global__ void __launch_bounds__(256) intsearch_kernel(const double* __restrict
   const int yp = imax % nr + 1, xp = imax / nr + 1;
   double ypeak = yp, xpeak = xp, maxf = cmax;
   if (!(xp == 1 || xp == nc || yp == 1 || yp == nr)) {
-    double s0 = 0, sx = 0, sy = 0, sxy = 0, sxx = 0, syy = 0;
+    double v9[9];
     for (int dc = -1; dc <= 1; ++dc)
-      for (int dr = -1; dr <= 1; ++dr) {
-        const double uu = C[(yp - 1 + dr) + (xp - 1 + dc) * nr];
-        s0 += uu; sx += dc * uu; sy += dr * uu; sxy += dc * dr * uu;
-        sxx += dc * dc * uu; syy += dr * dr * uu;
-      }
-    const double A2 = sx / 6, A3 = sy / 6, A4 = sxy / 4;
-    const double Sv = (sxx + syy) / 2 - (2.0 / 3.0) * s0;
-    const double Dd = (sxx - syy) / 2;
-    const double A5 = (Sv + Dd) / 2, A6 = (Sv - Dd) / 2;
-    const double A1 = (s0 - 6 * Sv) / 9;
-    double xo = (-A3 * A4 + 2 * A6 * A2) / (A4 * A4 - 4 * A5 * A6);
-    double yo = -1 / (A4 * A4 - 4 * A5 * A6) * (A4 * A2 - 2 * A5 * A3);
-    if (!(fabs(xo) > 1 || fabs(yo) > 1)) {
-      xo = round(1000 * xo) / 1000;
-      yo = round(1000 * yo) / 1000;
+      for (int dr = -1; dr <= 1; ++dr) v9[(dr + 1) + 3 * (dc + 1)] = C[(yp - 1 + dr) + (xp - 1 + dc) * nr];
+    double xo, yo, mf;
+    if (findpeak_fit3(v9, &xo, &yo, &mf)) {
       xpeak += xo;
       ypeak += yo;
-      maxf = A1 + xo * A2 + yo * A3 + xo * yo * A4 + xo * xo * A5 + yo * yo * A6;
+      maxf = mf;
     }
   }
   u[o] = ypeak - ceil(nr / 2.0);

@@ -34,7 +34,7 @@ EXPORTS = [
     "stdic_integer_search_grid", "stdic_integer_search", "stdic_icgn_subsets", "stdic_icgn_local",
     "stdic_subpb1_subsets", "stdic_subpb1", "stdic_subpb2", "stdic_subpb2_noalloc",
     "stdic_icgn_adjoint", "stdic_icgn_subsets_frames", "stdic_nodal_strain", "stdic_fill_nans",
-    "stdic_admm", "stdic_ctx_set_wait_limit", "stdic_quadtree_mesh", "stdic_por_gpr",
+    "stdic_admm", "stdic_ctx_set_wait_limit", "stdic_quadtree_mesh", "stdic_por_gpr", "stdic_integer_search_mg",
 ]
 
 
@@ -78,6 +78,8 @@ def load(build_if_missing=True):
     L.stdic_last_solver_ms.restype = _c.c_double
     L.stdic_ctx_set_wait_limit.argtypes = [_vp, _c.c_longlong]
     L.stdic_por_gpr.argtypes = [_vp, _vp, _c.c_int, _c.c_int64, _vp, _vp, _c.c_int, _c.c_int, _vp, _vp, _vp, _vp]
+    L.stdic_integer_search_mg.argtypes = [_vp, _vp, _vp, _c.c_int, _c.c_int, _vp, _vp, _c.c_int, _vp, _vp, _vp,
+                                          _vp, _vp, _vp, _c.c_int64, _vp]
     L.stdic_quadtree_mesh.argtypes = [_vp, _vp, _c.c_int, _c.c_int, _vp, _vp, _c.c_int, _c.c_int, _c.c_double,
                                       _c.c_double, _vp, _vp, _vp, _vp, _vp, _vp]
     L.stdic_interp_bicubic.argtypes = [_vp, _vp, _c.c_int64, _c.c_int64, _c.c_int64, _vp, _vp,

@@ -197,6 +197,32 @@ def funIntegerSearch(f, g, tempSizeOfSearchRegion, gridx, gridy, winsize, winste
     return x, y, u, v, cc
 
 
+def funIntegerSearchMg(f, g, gridx, gridy, winsize, winstepsize, *varargin, ctx=None):
+    """[xGrid,yGrid,uGrid,vGrid,cc] = funIntegerSearchMg(f,g,gridx,gridy,winsize,winstepsize)
+    (stdic_integer_search_mg): the multigrid search for large displacements.
+    Outputs are ny x nx (row = y); cc is a dict with 'max' (cc.max).  The
+    reference's cc.qfactors are not produced (its caller on this path,
+    IntegerSearch.m, does not read them)."""
+    c = _ctx(ctx)
+    W, H = _shape2(f)
+    st = np.asarray(_pair(winstepsize), dtype=np.float64)
+    gx = np.asarray([gridx[0], gridx[-1]], dtype=np.float64)
+    gy = np.asarray([gridy[0], gridy[-1]], dtype=np.float64)
+    cap = (int((gx[1] - gx[0]) // st[0]) + 1) * (int((gy[1] - gy[0]) // st[1]) + 1)
+    cap = max(cap, 4)
+    b = _Bufs(c)
+    pf, pg = b.ptr(f, np.float64), b.ptr(g, np.float64)
+    outs = [np.empty(cap) for _ in range(5)]
+    counts = np.zeros(2, dtype=np.int32)
+    D = lambda a: a.ctypes.data_as(_lib._d)
+    c.check(c.L.stdic_integer_search_mg(c.h, pf, pg, W, H, D(gx), D(gy), int(_pair(winsize)[0]), D(st),
+                                        *[o.ctypes.data for o in outs], cap, counts.ctypes.data),
+            "funIntegerSearchMg")
+    nx, ny = int(counts[0]), int(counts[1])
+    x, y, u, v, cm = (o[:nx * ny].reshape((ny, nx), order="F") for o in outs)
+    return x, y, u, v, {"max": cm}
+
+
 # ---------------------------------------------------------------------------
 def _frame(b, Df, ImgRef, ImgDef, dtype, frames=1):
     W, H = Df["imgSize"]

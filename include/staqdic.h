@@ -166,11 +166,16 @@ int stdic_integer_search(stdic_ctx* ctx, const double* f, const double* g, int W
  * reference raises: a region too small for the border gaps or wider than 4096
  * px, a constant or non-finite region at level 1, fewer than 3 blocks for
  * gridfit (STDIC_E_ARG); STDIC_E_NOTCONV if the gridfit solve misses its
- * tolerance. */
+ * tolerance.  blocks (optional, nblocks x 5 column-major, block_capacity rows)
+ * receives the last level's blocks before the fit -- centre x, centre y, u,
+ * v and cc.max, the reference's tempx, tempy, tempu, tempv, tempPhi
+ * (:300-306), NaN u, v and cc.max 0 where a block's search failed; nblocks
+ * (optional) receives their number. */
 int stdic_integer_search_mg(stdic_ctx* ctx, const double* f, const double* g, int W, int H,
                             const double gridx[2], const double gridy[2], int winsize,
                             const double winstepsize[2], double* x, double* y, double* u, double* v,
-                            double* cc, int64_t capacity, int32_t counts[2]);
+                            double* cc, int64_t capacity, int32_t counts[2], double* blocks,
+                            int64_t block_capacity, int64_t* nblocks);
 
 /* LocalICGNQuadtree(U0, coordinatesFEM, Df, ImgRef, ImgDef, DICpara, 'GaussNewton', tol)
  * without its NaN-fill tail (out of this path): U (2N) and F (4N) carry NaN at

@@ -171,7 +171,7 @@ def gridfit_springs(x, y, z, xnodes, ynodes, smoothness=1.0):
     return sol.reshape((ny, nx), order="F")
 
 
-def funIntegerSearchMg(f, g, gridx, gridy, winsize, winstepsize):
+def funIntegerSearchMg(f, g, gridx, gridy, winsize, winstepsize, return_blocks=False):
     """[xGrid, yGrid, uGrid, vGrid, ccmax] = funIntegerSearchMg(f, g, gridx,
     gridy, winsize, winstepsize) (func/funIntegerSearchMg.m:3-343): a
     correlation of the whole ROI, then blocks split in halves level by level
@@ -307,4 +307,7 @@ def funIntegerSearchMg(f, g, gridx, gridy, winsize, winstepsize):
     vG = gridfit_springs(tx[sel], ty[sel], tv[sel], xList, yList)
     pG = gridfit_springs(tx[sel], ty[sel], tp[sel], xList, yList)
     xG, yG = np.meshgrid(xList, yList)
+    if return_blocks:
+        # the last level's blocks before the fit: tempx, tempy, tempu, tempv, tempPhi
+        return xG, yG, uG, vG, pG, np.stack([tx, ty, tu, tv, tp], 1)
     return xG, yG, uG, vG, pG

@@ -1332,7 +1332,9 @@ extern "C" void orc_nodal_strain(const double* coords, long N, const int32_t* el
       for (int g = 0; g < ng * ng; ++g) {
         const double dx = gxv[g] - coords[n], dy = gyv[g] - coords[N + n];
         const double d2 = dx * dx + dy * dy;
-        if (d2 < bd) { bd = d2; best = g; }
+        // distances within 1e-9 relative are ties (the first Gauss point
+        // wins): a hanging node at an edge midpoint is equidistant from two
+        if (d2 < bd * (1.0 - 1e-9)) { bd = d2; best = g; }
       }
       for (int k = 0; k < 4; ++k) sum[4 * n + k] += gs[4 * best + k];
       cnt[n] += 1;

@@ -88,7 +88,11 @@ __global__ void k_nodal_strain(const double* __restrict__ coords, int N, const i
       }
       for (int c = 0; c < 4; ++c) dp[c] = nd[4 + c] != 0 ? 1.0 : 0.0;
       const double x1 = px[0], x3 = px[2], y1 = py[0], y3 = py[2];
-      // the element's Gauss point nearest to the node (x-major order, first on ties)
+      // the element's Gauss point nearest to the node (x-major order, first on
+      // ties).  A hanging node at an edge midpoint is exactly as far from two
+      // Gauss points; distances within 1e-9 relative count as equal, so that
+      // rounding (and the contraction of the distance into FMAs) never decides
+      // which one it takes.
       int bi = 0, bj = 0;
       double bd = 1e300;
       for (int ti = 0; ti < ng; ++ti)
@@ -97,7 +101,7 @@ __global__ void k_nodal_strain(const double* __restrict__ coords, int N, const i
           const double gy = gpt[tj] * 0.5 * (y3 - y1) + 0.5 * (y3 + y1);
           const double dx = gx - xn, dy = gy - yn;
           const double d2 = dx * dx + dy * dy;
-          if (d2 < bd) { bd = d2; bi = ti; bj = tj; }
+          if (d2 < bd * (1.0 - 1e-9)) { bd = d2; bi = ti; bj = tj; }
         }
       double Nv[8], dk[8], de[8];
       shape(gpt[bi], gpt[bj], dp, Nv, dk, de);

@@ -1317,7 +1317,8 @@ int stdic_quadtree_mesh(stdic_ctx* c, const uint8_t* mask, int W, int H, const d
 // funIntegerSearchMg.m: multigrid integer search, node grid chosen inside.
 int stdic_integer_search_mg(stdic_ctx* c, const double* f, const double* g, int W, int H, const double gridx[2],
                             const double gridy[2], int winsize, const double winstepsize[2], double* x, double* y,
-                            double* u, double* v, double* cc, int64_t capacity, int32_t counts[2]) {
+                            double* u, double* v, double* cc, int64_t capacity, int32_t counts[2],
+                            double* blocks, int64_t block_capacity, int64_t* nblocks) {
   if (!c) return STDIC_E_ARG;
   if (!f || !g || W < 8 || H < 8 || !gridx || !gridy || winsize < 2 || !winstepsize || !(winstepsize[0] > 0) ||
       !(winstepsize[1] > 0) || !counts || ((x || y || u || v || cc) && capacity < 4))
@@ -1362,6 +1363,19 @@ int stdic_integer_search_mg(stdic_ctx* c, const double* f, const double* g, int 
   }
   counts[0] = out.nx;
   counts[1] = out.ny;
+  if (nblocks) *nblocks = out.nblocks;
+  if (blocks) {
+    if (block_capacity < out.nblocks)
+      return fail(c, STDIC_E_ARG, "funIntegerSearchMg: blocks holds fewer rows than the last level (see nblocks)");
+    const size_t bytes = sizeof(double) * out.blocks.size();
+    if (is_device_ptr(blocks)) {
+      cudaError_t e = cudaMemcpyAsync(blocks, out.blocks.data(), bytes, cudaMemcpyHostToDevice, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "funIntegerSearchMg block copy");
+    } else {
+      std::memcpy(blocks, out.blocks.data(), bytes);
+    }
+  }
   const int64_t ng = (int64_t)out.nx * out.ny;
   if ((x || y || u || v || cc) && capacity < ng)
     return fail(c, STDIC_E_ARG, "funIntegerSearchMg: the outputs hold fewer elements than the node grid (see counts)");

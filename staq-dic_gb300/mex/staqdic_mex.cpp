@@ -6,6 +6,8 @@
 //   [DfDx, DfDy] = staqdic_mex('gradient', ImgRef, ImgRefMask)      func/funImgGradient.m:53-78
 //   [x, y, u, v, ccmax, qfactors] = staqdic_mex('integer_search', f, g, S, gridx, gridy,
 //                                               winsize, winstepsize)   func/funIntegerSearch.m:82-203
+//   [xGrid, yGrid, uGrid, vGrid, ccmax] = staqdic_mex('integer_search_mg', f, g, gridx, gridy,
+//                                                     winsize, winstepsize)  func/funIntegerSearchMg.m:3-343
 //   [U, F, HtempPar, ConvItPerEle, markCoordHoleStrain, LocalICGNBadPtNum] =
 //       staqdic_mex('icgn_local', U0, coordinatesFEM, DfDx, DfDy, ImgRefMask, ImgRef, ImgDef,
 //                   winsize, winsize_List, tol, precision)     func_quadtree/LocalICGNQuadtree.m:1-177
@@ -209,6 +211,42 @@ void op_integer_search(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[
         op);
 }
 
+void op_integer_search_mg(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
+  const char* op = "integer_search_mg";
+  need(nrhs == 7 && nlhs <= 5, op,
+       "[xGrid,yGrid,uGrid,vGrid,ccmax] = staqdic_mex('integer_search_mg', f, g, gridx, gridy, winsize, winstepsize)");
+  const double* f = dbl(prhs[1], op, "f");
+  const double* g = dbl(prhs[2], op, "g");
+  const int W = (int)mxGetM(prhs[1]), H = (int)mxGetN(prhs[1]);
+  need(mxGetM(prhs[2]) == (size_t)W && mxGetN(prhs[2]) == (size_t)H, op, "f and g must have one size");
+  const double* px = dbl(prhs[3], op, "gridx");
+  const double* py = dbl(prhs[4], op, "gridy");
+  need(numel(prhs[3]) >= 2 && numel(prhs[4]) >= 2, op, "gridx and gridy hold [first last]");
+  const double gx[2] = {px[0], px[numel(prhs[3]) - 1]}, gy[2] = {py[0], py[numel(prhs[4]) - 1]};
+  const int ws = (int)scalar(prhs[5], op, "winsize");
+  const double* pst = dbl(prhs[6], op, "winstepsize");
+  need(numel(prhs[6]) >= 1, op, "winstepsize");
+  const double st[2] = {pst[0], numel(prhs[6]) > 1 ? pst[1] : pst[0]};
+  need(st[0] > 0 && st[1] > 0, op, "winstepsize must be positive");
+  // the node grid is chosen inside the search; its size is bounded by the region
+  const int64_t cap = (int64_t)(std::floor((gx[1] - gx[0]) / st[0]) + 1) * (int64_t)(std::floor((gy[1] - gy[0]) / st[1]) + 1);
+  need(cap >= 4, op, "the search region holds fewer than 2 x 2 grid steps");
+  double* buf[5];
+  for (int k = 0; k < 5; ++k) buf[k] = (double*)mxMalloc((size_t)cap * sizeof(double));
+  int32_t counts[2] = {0, 0};
+  const int rc = stdic_integer_search_mg(ctx(), f, g, W, H, gx, gy, ws, st, buf[0], buf[1], buf[2], buf[3], buf[4],
+                                         cap, counts, nullptr, 0, nullptr);
+  if (rc != STDIC_OK)
+    for (int k = 0; k < 5; ++k) mxFree(buf[k]);
+  check(rc, op);
+  const size_t nx = (size_t)counts[0], ny = (size_t)counts[1];
+  for (int k = 0; k < 5; ++k) {
+    plhs[k] = dmat(ny, nx);
+    std::memcpy(pr(plhs[k]), buf[k], nx * ny * sizeof(double));
+    mxFree(buf[k]);
+  }
+}
+
 // the frame of an IC-GN call from MATLAB's Df fields and images
 stdic_frame frame_of(const mxArray* dfdx, const mxArray* dfdy, const uint8_t* mask, const mxArray* f,
                      const mxArray* g, int precision, const char* op) {
@@ -362,6 +400,7 @@ extern "C" void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* 
   if (!std::strcmp(op, "ba_interp2")) return op_interp(nlhs, plhs, nrhs, prhs);
   if (!std::strcmp(op, "gradient")) return op_gradient(nlhs, plhs, nrhs, prhs);
   if (!std::strcmp(op, "integer_search")) return op_integer_search(nlhs, plhs, nrhs, prhs);
+  if (!std::strcmp(op, "integer_search_mg")) return op_integer_search_mg(nlhs, plhs, nrhs, prhs);
   if (!std::strcmp(op, "icgn_local")) return op_icgn_local(nlhs, plhs, nrhs, prhs);
   if (!std::strcmp(op, "subpb1")) return op_subpb1(nlhs, plhs, nrhs, prhs);
   if (!std::strcmp(op, "subpb2")) return op_subpb2(nlhs, plhs, nrhs, prhs);

@@ -79,7 +79,7 @@ def load(build_if_missing=True):
     L.stdic_ctx_set_wait_limit.argtypes = [_vp, _c.c_longlong]
     L.stdic_por_gpr.argtypes = [_vp, _vp, _c.c_int, _c.c_int64, _vp, _vp, _c.c_int, _c.c_int, _vp, _vp, _vp, _vp]
     L.stdic_integer_search_mg.argtypes = [_vp, _vp, _vp, _c.c_int, _c.c_int, _vp, _vp, _c.c_int, _vp, _vp, _vp,
-                                          _vp, _vp, _vp, _c.c_int64, _vp]
+                                          _vp, _vp, _vp, _c.c_int64, _vp, _vp, _c.c_int64, _vp]
     L.stdic_quadtree_mesh.argtypes = [_vp, _vp, _c.c_int, _c.c_int, _vp, _vp, _c.c_int, _c.c_int, _c.c_double,
                                       _c.c_double, _vp, _vp, _vp, _vp, _vp, _vp]
     L.stdic_interp_bicubic.argtypes = [_vp, _vp, _c.c_int64, _c.c_int64, _c.c_int64, _vp, _vp,

@@ -197,12 +197,13 @@ def funIntegerSearch(f, g, tempSizeOfSearchRegion, gridx, gridy, winsize, winste
     return x, y, u, v, cc
 
 
-def funIntegerSearchMg(f, g, gridx, gridy, winsize, winstepsize, *varargin, ctx=None):
+def funIntegerSearchMg(f, g, gridx, gridy, winsize, winstepsize, *varargin, ctx=None, blocks=False):
     """[xGrid,yGrid,uGrid,vGrid,cc] = funIntegerSearchMg(f,g,gridx,gridy,winsize,winstepsize)
     (stdic_integer_search_mg): the multigrid search for large displacements.
-    Outputs are ny x nx (row = y); cc is a dict with 'max' (cc.max).  The
-    reference's cc.qfactors are not produced (its caller on this path,
-    IntegerSearch.m, does not read them)."""
+    Outputs are ny x nx (row = y); cc is a dict with 'max' (cc.max) and, with
+    blocks=True, 'blocks': the last level's blocks before gridfit (nblocks x 5:
+    centre x, centre y, u, v, cc.max).  The reference's cc.qfactors are not
+    produced (its caller on this path, IntegerSearch.m, does not read them)."""
     c = _ctx(ctx)
     W, H = _shape2(f)
     st = np.asarray(_pair(winstepsize), dtype=np.float64)
@@ -214,13 +215,22 @@ def funIntegerSearchMg(f, g, gridx, gridy, winsize, winstepsize, *varargin, ctx=
     pf, pg = b.ptr(f, np.float64), b.ptr(g, np.float64)
     outs = [np.empty(cap) for _ in range(5)]
     counts = np.zeros(2, dtype=np.int32)
+    nbl = np.zeros(1, dtype=np.int64)
+    # the library refuses searches of more than 65535 last-level blocks
+    bcap = 65535 if blocks else 0
+    bl = np.empty(5 * bcap) if blocks else None
     D = lambda a: a.ctypes.data_as(_lib._d)
     c.check(c.L.stdic_integer_search_mg(c.h, pf, pg, W, H, D(gx), D(gy), int(_pair(winsize)[0]), D(st),
-                                        *[o.ctypes.data for o in outs], cap, counts.ctypes.data),
+                                        *[o.ctypes.data for o in outs], cap, counts.ctypes.data,
+                                        bl.ctypes.data if blocks else None, bcap, nbl.ctypes.data),
             "funIntegerSearchMg")
     nx, ny = int(counts[0]), int(counts[1])
     x, y, u, v, cm = (o[:nx * ny].reshape((ny, nx), order="F") for o in outs)
-    return x, y, u, v, {"max": cm}
+    cc = {"max": cm}
+    if blocks:
+        nb = int(nbl[0])
+        cc["blocks"] = np.stack([bl[k * nb:(k + 1) * nb] for k in range(5)], 1)
+    return x, y, u, v, cc
 
 
 # ---------------------------------------------------------------------------

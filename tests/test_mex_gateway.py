@@ -7,6 +7,7 @@ of the C ABI:
   * 'ba_interp2' (double and single): bit-identical to the reference's
     compiled ba_interp2.cpp (the golden vectors), output shape of X;
   * 'gradient', 'integer_search' (x, y, u, v, cc.max, cc.qfactors),
+    'integer_search_mg' (xGrid, yGrid, uGrid, vGrid, cc.max),
     'icgn_local' (U, F, HtempPar, codes, markCoordHoleStrain as 1-based
     indices, the bad count), 'subpb1', 'subpb2': equal to the direct calls
     (the same kernels on the same inputs; Subpb2's atomics leave 1e-9);
@@ -145,6 +146,22 @@ def test_gradient_and_integer_search_ops(mex, ctx):
     for a, b in ((x, xo), (y, yo), (u, uo), (v, vo), (ccm, cc["max"]), (qf, cc["qfactors"])):
         assert a.shape == b.shape
         assert np.array_equal(a, b, equal_nan=True)
+
+
+@pytest.mark.gpu
+def test_integer_search_mg_op(mex, ctx):
+    """'integer_search_mg' against the direct call (gridfit's data assembly
+    adds with atomics, so the fitted fields agree to rounding)."""
+    import staqdic
+    from staqdic import workloads
+    w = workloads.uniform256(seed=0)
+    f, g = w["f"].astype(np.float64), w["g"].astype(np.float64)
+    outs = mex("integer_search_mg", f, g, np.array([1.0, 256.0]), np.array([1.0, 256.0]), np.array([32.0]),
+               np.array([16.0]), nout=5)
+    ref = staqdic.funIntegerSearchMg(f, g, (1, 256), (1, 256), 32, 16, ctx=ctx)
+    for a, b in zip(outs, list(ref[:4]) + [ref[4]["max"]]):
+        assert a.shape == b.shape
+        assert np.allclose(a, b, rtol=0, atol=1e-9, equal_nan=True)
 
 
 @pytest.mark.gpu

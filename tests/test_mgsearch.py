@@ -1,8 +1,9 @@
 """stdic_integer_search_mg (funIntegerSearchMg.m) against the oracle's
 restatement (oracle/mg.py) on the same images.
 
-Bar: the node grid (xGrid, yGrid) identical; uGrid, vGrid within 1e-6 px and
-cc.max within 1e-6.  Every block's integer peak enters uGrid through gridfit,
+Bar: the last level's blocks (the reference's tempx, tempy, tempu, tempv)
+bit-exact and their cc.max within 1e-9; the node grid (xGrid, yGrid)
+identical; uGrid, vGrid within 1e-6 px and cc.max within 1e-6.  Every block's integer peak enters uGrid through gridfit,
 so a block whose peak moved by one sample would move the fitted field by far
 more than 1e-6 px; what remains is the difference between the device's
 conjugate-gradient solve of gridfit's normal equations (relative residual
@@ -31,8 +32,15 @@ def mg():
 
 def _compare(sd, mg, ctx, f, g, ws=32, st=16):
     W, H = f.shape
-    xo, yo, uo, vo, po = mg.funIntegerSearchMg(f, g, (1, W), (1, H), ws, st)
-    x, y, u, v, cc = sd.funIntegerSearchMg(f, g, (1, W), (1, H), ws, st, ctx=ctx)
+    xo, yo, uo, vo, po, bo = mg.funIntegerSearchMg(f, g, (1, W), (1, H), ws, st, return_blocks=True)
+    x, y, u, v, cc = sd.funIntegerSearchMg(f, g, (1, W), (1, H), ws, st, ctx=ctx, blocks=True)
+    # the last level's blocks: centres and displacements bit-exact (integer
+    # peaks plus findpeak offsets rounded to 1/1000), cc.max to 1e-9
+    b = cc["blocks"]
+    assert b.shape == bo.shape
+    assert np.array_equal(b[:, :2], bo[:, :2])
+    assert np.array_equal(b[:, 2:4], bo[:, 2:4], equal_nan=True), np.nonzero(np.any(b[:, 2:4] != bo[:, 2:4], 1))
+    assert np.max(np.abs(b[:, 4] - bo[:, 4])) < 1e-9
     assert x.shape == xo.shape and np.array_equal(x, xo) and np.array_equal(y, yo)
     assert np.array_equal(np.isnan(u), np.isnan(uo))
     ok = ~np.isnan(uo)

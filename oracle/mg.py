@@ -69,14 +69,19 @@ def normxcorr2_full(T, A):
     return out
 
 
+PEAK_TIE = 1e-10
+
+
 def findpeak(f, subpixel=True):
     """[xpeak, ypeak, max_f] = findpeak(f, subpixel) (func/findpeak.m:27-68):
     the first column-major maximum (x = column, y = row, 1-based), refined by a
     quadratic fit over its 3 x 3 neighbourhood unless it lies on the edge or
-    the fit moves it by more than one sample."""
+    the fit moves it by more than one sample.  Values within PEAK_TIE of the
+    maximum count as equal (the first of them is taken): a degenerate map has
+    several lags equal in exact arithmetic, which rounding alone would order."""
     f = np.asarray(f, dtype=np.float64)
     flat = f.ravel(order="F")
-    imax = int(np.argmax(flat))
+    imax = int(np.nonzero(flat >= np.max(flat) - PEAK_TIE)[0][0])
     max_f = flat[imax]
     ypeak, xpeak = imax % f.shape[0] + 1, imax // f.shape[0] + 1
     if not subpixel or xpeak == 1 or xpeak == f.shape[1] or ypeak == 1 or ypeak == f.shape[0]:

@@ -131,6 +131,13 @@ static inline double matlab_eps(double x) {
   return p < -1074 ? std::ldexp(1.0, -1074) : std::ldexp(1.0, p);
 }
 
+// Correlation values within this of the map's maximum count as equal in the
+// integer searches' peak choice (the first such lag, column-major, wins).  A
+// degenerate map -- a template with a single nonzero pixel inside a masked
+// region -- has several lags equal to 1 in exact arithmetic, and rounding
+// alone would pick among them.
+static const double kPeakTie = 1e-10;
+
 // bwselect(BW, c, r, n) on an m x n tile (column-major, BW[i + j*m]), seed at
 // 1-based row r (dim 1) and column c (dim 2).  Returns the connected component
 // of BW holding the seed; an out-of-range or background seed selects nothing.
@@ -945,17 +952,20 @@ static bool ncc_peak(const double* f, const double* g, long W, long ii, long jj,
   const double tolc = std::sqrt(matlab_eps(dmax));
   const double clip = std::sqrt(matlab_eps(1.0));
   std::vector<double> C((size_t)nr * nc);
-  int imax = -1;
   double cmax = -INFINITY;
   for (int k = 0; k < nr * nc; ++k) {
     double cv = den[k] > tolc ? num[k] / den[k] : 0.0;
     if ((std::fabs(cv) - 1) > clip) cv = 0;
     C[k] = cv;
-    if (cv > cmax) { cmax = cv; imax = k; }  // first maximum, column-major
+    if (cv > cmax) cmax = cv;
   }
+  // the first column-major lag within kPeakTie of the maximum: findpeak's
+  // first maximum, with lags that tie up to rounding taken as equal
+  int imax = 0;
+  while (imax < nr * nc - 1 && !(C[imax] >= cmax - kPeakTie)) ++imax;
   const int yp = imax % nr + 1, xp = imax / nr + 1;  // 1-based row / col
   *pr = yp; *pc = xp;
-  double ypeak = yp, xpeak = xp, maxf = cmax;
+  double ypeak = yp, xpeak = xp, maxf = C[imax];
   if (!(xp == 1 || xp == nc || yp == 1 || yp == nr)) {
     // u = f(ypeak-1:ypeak+1, xpeak-1:xpeak+1)(:), x = column offset, y = row offset
     double uu[9], xs[9], ys[9];

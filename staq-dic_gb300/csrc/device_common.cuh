@@ -42,6 +42,40 @@ STDIC_DEV void cta_exclusive_scan(const int* in, int* out, int n) {
   if (threadIdx.x == blockDim.x - 1) out[n] = acc;
 }
 
+// Correlation values within this of a map's maximum count as equal in the
+// integer searches' peak choice: the first such lag (column-major) is the
+// peak, which is findpeak's first maximum whenever the maximum is unique.  A
+// degenerate map -- a template with a single nonzero pixel in a masked region
+// -- holds several lags equal to 1 in exact arithmetic, and without the rule
+// rounding alone would choose among them.
+constexpr double kPeakTie = 1e-10;
+
+// Index of the first of n values C[] (visible to the whole CTA) that lies
+// within kPeakTie of their maximum; every thread receives it.  All threads of
+// the CTA must call it (blockDim.x <= 1024).
+STDIC_DEV int cta_first_near_max(const double* C, int n) {
+  __shared__ double s_v[32];
+  __shared__ int s_i[32];
+  const int nw = (blockDim.x + 31) >> 5;
+  double m = -INFINITY;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) m = fmax(m, C[k]);
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) s_v[threadIdx.x >> 5] = m;
+  __syncthreads();
+  m = -INFINITY;
+  for (int w = 0; w < nw; ++w) m = fmax(m, s_v[w]);
+  int first = 0x7fffffff;
+  for (int k = threadIdx.x; k < n; k += blockDim.x)
+    if (C[k] >= m - kPeakTie) { first = k; break; }
+  for (int o = 16; o > 0; o >>= 1) first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
+  if ((threadIdx.x & 31) == 0) s_i[threadIdx.x >> 5] = first;
+  __syncthreads();
+  first = 0x7fffffff;
+  for (int w = 0; w < nw; ++w) first = min(first, s_i[w]);
+  __syncthreads();
+  return first;
+}
+
 // findpeak.m:40-68 on the 3 x 3 neighbourhood of a correlation maximum,
 // v9[(dr+1) + 3 (dc+1)] at row offset dr and column offset dc: the least-
 // squares quadratic [1 x y xy x^2 y^2] (x = column, y = row offset) in the

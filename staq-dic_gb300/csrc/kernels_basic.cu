@@ -254,7 +254,6 @@ __global__ void __launch_bounds__(256) intsearch_kernel(const double* __restrict
                                                         double* v, double* cc, int32_t* peak) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ double red[32 * 2];
-  __shared__ int ired[32];
   __shared__ int best_idx;
   const int t = blockIdx.x;
   const int ix = t % nx, iy = t / nx;
@@ -341,32 +340,15 @@ __global__ void __launch_bounds__(256) intsearch_kernel(const double* __restrict
   const double clip = sqrt(eps_of(1.0));
   __syncthreads();
   // C into num[], then first (column-major) argmax
-  double bv = -INFINITY;
-  int bi = 0x7fffffff;
   for (int k = threadIdx.x; k < nl; k += blockDim.x) {
     double cv = den[k] > tolc ? num[k] / den[k] : 0.0;
     if ((fabs(cv) - 1) > clip) cv = 0;
     num[k] = cv;
-    if (cv > bv) { bv = cv; bi = k; }
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    const double ov = __shfl_down_sync(0xffffffffu, bv, off);
-    const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-    if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-  }
-  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = bv; ired[threadIdx.x >> 5] = bi; }
   __syncthreads();
-  if (threadIdx.x < 32) {
-    const int nw = (blockDim.x + 31) / 32;
-    double v2 = threadIdx.x < nw ? red[threadIdx.x] : -INFINITY;
-    int i2 = threadIdx.x < nw ? ired[threadIdx.x] : 0x7fffffff;
-    for (int off = 16; off > 0; off >>= 1) {
-      const double ov = __shfl_down_sync(0xffffffffu, v2, off);
-      const int oi = __shfl_down_sync(0xffffffffu, i2, off);
-      if (ov > v2 || (ov == v2 && oi < i2)) { v2 = ov; i2 = oi; }
-    }
-    if (threadIdx.x == 0) best_idx = i2;
-  }
+  // findpeak's first maximum, with lags tied up to rounding taken as equal
+  const int first = cta_first_near_max(num, nl);
+  if (threadIdx.x == 0) best_idx = first;
   __syncthreads();
   if (threadIdx.x != 0) return;
   const double* C = num;

@@ -293,14 +293,12 @@ __global__ void __launch_bounds__(256) mg_denmax_kernel(MgImg im, const MgBlock*
   if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(dmax + bi, (unsigned long long)__double_as_longlong(best));
 }
 
-// level 1: value of every lag and the first column-major maximum per CTA
-__global__ void __launch_bounds__(256) mg_l1_argmax_kernel(MgImg im, const MgBlock* __restrict__ blk,
-                                                           const MgStat* __restrict__ st, const double2* __restrict__ q,
-                                                           int Fx, const unsigned long long* __restrict__ dmax,
-                                                           double scale, double* __restrict__ pv,
-                                                           long long* __restrict__ pi) {
+// level 1, pass 1: the largest value of each CTA's lags
+__global__ void __launch_bounds__(256) mg_l1_max_kernel(MgImg im, const MgBlock* __restrict__ blk,
+                                                        const MgStat* __restrict__ st, const double2* __restrict__ q,
+                                                        int Fx, const unsigned long long* __restrict__ dmax,
+                                                        double scale, double* __restrict__ pv) {
   __shared__ double sv[32];
-  __shared__ long long si[32];
   int tx0, ty0, m, n, ax0, ay0, Mw, Nw;
   block_rects(blk[0], im.W, im.H, true, &tx0, &ty0, &m, &n, &ax0, &ay0, &Mw, &Nw);
   const long long R = Mw + m - 1, C = Nw + n - 1;
@@ -308,24 +306,57 @@ __global__ void __launch_bounds__(256) mg_l1_argmax_kernel(MgImg im, const MgBlo
   const double tol = sqrt(eps_of_d(__longlong_as_double((long long)dmax[0])));
   const double clip = sqrt(eps_of_d(1.0));
   double bv = -INFINITY;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < R * C; k += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(k % R), c = (int)(k / R);
+    const double num = q[(size_t)c * Fx + r].x * scale;
+    bv = fmax(bv, ncc_value(num, lag_den(im, ax0, ay0, Mw, Nw, m, n, r - m + 1, c - n + 1, denT, mn), tol, clip));
+  }
+  for (int o = 16; o > 0; o >>= 1) bv = fmax(bv, __shfl_down_sync(0xffffffffu, bv, o));
+  if ((threadIdx.x & 31) == 0) sv[threadIdx.x >> 5] = bv;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) bv = fmax(bv, sv[w]);
+    pv[blockIdx.x] = bv;
+  }
+}
+
+// level 1, pass 2: the first lag (column-major) within kPeakTie of the
+// map's maximum, per CTA
+__global__ void __launch_bounds__(256) mg_l1_first_kernel(MgImg im, const MgBlock* __restrict__ blk,
+                                                          const MgStat* __restrict__ st, const double2* __restrict__ q,
+                                                          int Fx, const unsigned long long* __restrict__ dmax,
+                                                          double scale, const double* __restrict__ pv, int np,
+                                                          long long* __restrict__ pi) {
+  __shared__ long long si[32];
+  __shared__ double sm;
+  if (threadIdx.x == 0) {
+    double m0 = -INFINITY;
+    for (int k = 0; k < np; ++k) m0 = fmax(m0, pv[k]);
+    sm = m0;
+  }
+  __syncthreads();
+  const double gmax = sm;
+  int tx0, ty0, m, n, ax0, ay0, Mw, Nw;
+  block_rects(blk[0], im.W, im.H, true, &tx0, &ty0, &m, &n, &ax0, &ay0, &Mw, &Nw);
+  const long long R = Mw + m - 1, C = Nw + n - 1;
+  const double mn = (double)m * n, denT = st[0].denT;
+  const double tol = sqrt(eps_of_d(__longlong_as_double((long long)dmax[0])));
+  const double clip = sqrt(eps_of_d(1.0));
   long long bi = 0x7fffffffffffffffLL;
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < R * C; k += (long long)gridDim.x * blockDim.x) {
     const int r = (int)(k % R), c = (int)(k / R);
     const double num = q[(size_t)c * Fx + r].x * scale;
     const double v = ncc_value(num, lag_den(im, ax0, ay0, Mw, Nw, m, n, r - m + 1, c - n + 1, denT, mn), tol, clip);
-    if (v > bv) { bv = v; bi = k; }
+    if (v >= gmax - kPeakTie) { bi = k; break; }
   }
   for (int o = 16; o > 0; o >>= 1) {
-    const double ov = __shfl_down_sync(0xffffffffu, bv, o);
     const long long oi = __shfl_down_sync(0xffffffffu, bi, o);
-    if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+    bi = oi < bi ? oi : bi;
   }
-  if ((threadIdx.x & 31) == 0) { sv[threadIdx.x >> 5] = bv; si[threadIdx.x >> 5] = bi; }
+  if ((threadIdx.x & 31) == 0) si[threadIdx.x >> 5] = bi;
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
-      if (sv[w] > bv || (sv[w] == bv && si[w] < bi)) { bv = sv[w]; bi = si[w]; }
-    pv[blockIdx.x] = bv;
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) bi = si[w] < bi ? si[w] : bi;
     pi[blockIdx.x] = bi;
   }
 }
@@ -358,10 +389,8 @@ __global__ void mg_l1_peak_kernel(MgImg im, const MgBlock* __restrict__ blk, con
                                   double scale, const double* __restrict__ pv, const long long* __restrict__ pi,
                                   int np, MgRes* __restrict__ res) {
   if (threadIdx.x != 0) return;
-  double bv = -INFINITY;
   long long bi = 0x7fffffffffffffffLL;
-  for (int k = 0; k < np; ++k)
-    if (pv[k] > bv || (pv[k] == bv && pi[k] < bi)) { bv = pv[k]; bi = pi[k]; }
+  for (int k = 0; k < np; ++k) bi = pi[k] < bi ? pi[k] : bi;
   int tx0, ty0, m, n, ax0, ay0, Mw, Nw;
   block_rects(blk[0], im.W, im.H, true, &tx0, &ty0, &m, &n, &ax0, &ay0, &Mw, &Nw);
   const int R = Mw + m - 1, C = Nw + n - 1;
@@ -468,8 +497,6 @@ __global__ void __launch_bounds__(192) mg_finish_kernel(MgImg im, const MgBlock*
                                                         const unsigned long long* __restrict__ dmax,
                                                         MgRes* __restrict__ res) {
   __shared__ double C[kLags];
-  __shared__ double bvs[8];
-  __shared__ int bis[8];
   const int bi = blockIdx.x;
   const MgBlock b = blocks[bi];
   if (!st[bi].ok) {
@@ -482,27 +509,15 @@ __global__ void __launch_bounds__(192) mg_finish_kernel(MgImg im, const MgBlock*
   const double tol = sqrt(eps_of_d(__longlong_as_double((long long)dmax[bi])));
   const double clip = sqrt(eps_of_d(1.0));
   const int l = threadIdx.x;
-  double bv = -INFINITY;
-  int bidx = 0x7fffffff;
   if (l < kLags) {
     double num = 0;
     for (int c = 0; c < nct; ++c) num += part[((size_t)bi * nct + c) * kLags + l];
     const int lr = l % kLagR, lc = l / kLagR;
-    const double v = ncc_value(num, lag_den(im, ax0, ay0, Mw, Nw, m, n, lr - 1, lc - 1, denT, mn), tol, clip);
-    C[l] = v;
-    bv = v;
-    bidx = l;
+    C[l] = ncc_value(num, lag_den(im, ax0, ay0, Mw, Nw, m, n, lr - 1, lc - 1, denT, mn), tol, clip);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    const double ov = __shfl_down_sync(0xffffffffu, bv, o);
-    const int oi = __shfl_down_sync(0xffffffffu, bidx, o);
-    if (ov > bv || (ov == bv && oi < bidx)) { bv = ov; bidx = oi; }
-  }
-  if ((threadIdx.x & 31) == 0) { bvs[threadIdx.x >> 5] = bv; bis[threadIdx.x >> 5] = bidx; }
   __syncthreads();
+  const int bidx = cta_first_near_max(C, kLags);
   if (threadIdx.x != 0) return;
-  for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
-    if (bvs[w] > bv || (bvs[w] == bv && bis[w] < bidx)) { bv = bvs[w]; bidx = bis[w]; }
   auto val = [&](int r, int c) { return C[r + kLagR * c]; };
   double yp, xp, mf;
   findpeak_at(val, kLagR, kLagC, bidx, &yp, &xp, &mf);
@@ -1046,7 +1061,8 @@ int integer_search_mg(const double* f, const double* g, int W, int H, const doub
     const long long lags = R * Cc;
     const int gxb = (int)std::min<long long>(1024, std::max<long long>(1, (lags + 255) / 256));
     mg_denmax_kernel<<<dim3(gxb, 1), 256, 0, s>>>(im, b1, st1, 1, dm1); ++nl;
-    mg_l1_argmax_kernel<<<npart1, 256, 0, s>>>(im, b1, st1, zt, Fx, dm1, scale, pv, pi); ++nl;
+    mg_l1_max_kernel<<<npart1, 256, 0, s>>>(im, b1, st1, zt, Fx, dm1, scale, pv); ++nl;
+    mg_l1_first_kernel<<<npart1, 256, 0, s>>>(im, b1, st1, zt, Fx, dm1, scale, pv, npart1, pi); ++nl;
     mg_l1_peak_kernel<<<1, 32, 0, s>>>(im, b1, st1, zt, Fx, dm1, scale, pv, pi, npart1, r1); ++nl;
   }
   MG_TRY(cudaGetLastError());

@@ -3,9 +3,8 @@ restatement (oracle/mg.py) on the same images.
 
 Bar: the last level's blocks (the reference's tempx, tempy, tempu, tempv)
 bit-exact and their cc.max within 1e-9; the node grid (xGrid, yGrid)
-identical; uGrid, vGrid within 1e-6 px and cc.max within 1e-6.  Every block's integer peak enters uGrid through gridfit,
-so a block whose peak moved by one sample would move the fitted field by far
-more than 1e-6 px; what remains is the difference between the device's
+identical; uGrid, vGrid within 1e-6 px and cc.max within 1e-6.  What remains
+after the bit-exact blocks is the difference between the device's
 conjugate-gradient solve of gridfit's normal equations (relative residual
 1e-12) and the oracle's direct solve, and rounding of the correlation sums.
 Cases: a 13 x -9 px translation at 256^2 (beyond the +-6 px whole-field

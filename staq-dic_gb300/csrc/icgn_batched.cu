@@ -618,6 +618,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
   float2* gq = nullptr;  // 6-DOF iterations: (gx, gy) of each tile pixel times the f selection
   uint8_t *mtile = nullptr, *bwf = nullptr, *bwg = nullptr, *tmp = nullptr, *bwm8 = nullptr;
   bool have_m8 = false;  // bwm8 holds the 8-connected selection of the mask tile
+  bool have_mtile = false;  // mtile holds the mask tile
   bool has_masked = false;
   bool decided = false;  // outputs of this subset already written by the set-up stage
   const double npx0 = (double)(wx + 1) * (double)(wy + 1);
@@ -694,15 +695,21 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     bwg = bwf + cap;
     tmp = bwg + cap;
     bwm8 = tmp + cap;
-    int z = 0;
-    PixIter it(pstart, mx);
-    for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
-      const uint8_t mk = __ldg(fr.mask + (y1 + it.j - 1) * fr.W + (x1 + it.i - 1)) != 0;
-      mtile[p] = mk;
-      if (!mk) z = 1;
+    // the mask tile: the set-up stage needs it to find masked subsets; the
+    // iteration stage only for a masked subset (its f selection) and, lazily,
+    // for the rare unmasked subset whose interpolated g has an exact zero
+    if (stage != 2 || has_masked) {
+      int z = 0;
+      PixIter it(pstart, mx);
+      for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
+        const uint8_t mk = __ldg(fr.mask + (y1 + it.j - 1) * fr.W + (x1 + it.i - 1)) != 0;
+        mtile[p] = mk;
+        if (!mk) z = 1;
+      }
+      have_mtile = true;
+      if (stage != 2) has_masked = tm.any(z, iscr) != 0;
+      if (has_masked) bwselect_team(tm, mtile, bwf, mx, my, sr, sc, 4, iscr);
     }
-    if (stage != 2) has_masked = tm.any(z, iscr) != 0;
-    if (has_masked) bwselect_team(tm, mtile, bwf, mx, my, sr, sc, 4, iscr);
     tm.sync();
   }
 
@@ -882,7 +889,12 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
   }
   if constexpr (!TWO) {
     // the subset's inverse Hessian and f-side sums, once, into the team's control block
-    for (int k = tm.tl; k < 36; k += tm.TT) split_f64(B.Hinv6[(size_t)item * 36 + k], ctl->hh[k], ctl->hl[k]);
+    const float2* hp = reinterpret_cast<const float2*>(B.Hinv6) + (size_t)item * 36;
+    for (int k = tm.tl; k < 36; k += tm.TT) {
+      const float2 h = hp[k];
+      ctl->hh[k] = h.x;
+      ctl->hl[k] = h.y;
+    }
     if (tm.tl < 6) { ctl->jf[tm.tl] = st6[item].Jf[tm.tl]; ctl->j1[tm.tl] = st6[item].J1[tm.tl]; }
     tm.sync();
   }
@@ -1043,6 +1055,13 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         // the 8-connected selection of the mask tile does not change between
         // iterations: filled once per subset, then copied
         if (!have_m8) {
+          if (!have_mtile) {
+            PixIter it(pstart, mx);
+            for (int p = tm.tl; p < npx; p += tm.TT, it.next())
+              mtile[p] = __ldg(fr.mask + (y1 + it.j - 1) * fr.W + (x1 + it.i - 1)) != 0;
+            have_mtile = true;
+            tm.sync();
+          }
           bwselect_team(tm, mtile, bwm8, mx, my, sr, sc, 8, iscr);
           have_m8 = true;
         }
@@ -1396,9 +1415,18 @@ __global__ void __launch_bounds__(128) factor6_kernel(const SubsetState6* __rest
       l[i * (i + 1) / 2 + j] = s2 * inv;
     }
   }
-  double* out = Hinv6 + (size_t)t * 36;
+  // the inverse is handed to the iteration stage as FP32 pairs (hi, lo) whose
+  // sum carries its FP64 value to about 2^-48: the split costs FP64
+  // instructions, which GB300 issues slowly, so it is done once here rather
+  // than by every team that takes the subset
+  float2* outp = reinterpret_cast<float2*>(Hinv6) + (size_t)t * 36;
+  double out[36];
   if (!ok) {
     lu_inverse6(H6 + (size_t)t * 21, out);
+    for (int k = 0; k < 36; ++k) {
+      const float hi = (float)out[k];
+      outp[k] = make_float2(hi, (float)(out[k] - (double)hi));
+    }
     return;
   }
   // M = L^-1 (lower, packed), then H^-1 = M^T M
@@ -1425,6 +1453,11 @@ __global__ void __launch_bounds__(128) factor6_kernel(const SubsetState6* __rest
       out[r * 6 + c2] = s2;
       out[c2 * 6 + r] = s2;
     }
+  }
+#pragma unroll
+  for (int k = 0; k < 36; ++k) {
+    const float hi = (float)out[k];
+    outp[k] = make_float2(hi, (float)(out[k] - (double)hi));
   }
 }
 

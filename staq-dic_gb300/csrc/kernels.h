@@ -83,7 +83,7 @@ struct BatchedArgs {
   int stage;
   void* st6;              // SubsetState6 per item
   double* H6;             // 21 per item: packed lower Hessian (row-major)
-  double* Hinv6;          // 36 per item: FP64 inverse Hessian (row-major)
+  double* Hinv6;          // 36 per item: the FP64 inverse Hessian (row-major) as FP32 pairs (hi, lo)
 };
 
 // Per-subset state handed from the 6-DOF set-up stage to the iterations.

@@ -65,6 +65,9 @@ bool is_device_ptr(const void* p) {
 
 size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// c->scal slot a kernel sets when a bounded wait for a TMA tile copy gave up
+constexpr int kTmaErrSlot = 40;
+
 // Plans device placement for one call: device pointers pass through, host
 // buffers and scratch get regions of the context workspace.
 struct Plan {
@@ -144,8 +147,16 @@ struct Plan {
       }
     }
     if (any_host) {
-      cudaError_t e = cudaStreamSynchronize(c->stream);
+      int terr = 0;
+      cudaError_t e = cudaMemcpyAsync(&terr, c->scal + kTmaErrSlot, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "stream synchronise");
+      if (terr) {
+        cudaMemsetAsync(c->scal + kTmaErrSlot, 0, sizeof(int), c->stream);
+        return fail(c, STDIC_E_TIMEOUT,
+                    "a bounded wait for a TMA tile copy gave up (the subsets involved were gathered from global "
+                    "memory instead)");
+      }
     }
     return STDIC_OK;
   }
@@ -194,6 +205,7 @@ int stdic_ctx_create(stdic_ctx** out, int device) {
   // caller's framework usually produces and consumes device buffers
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamDefault);
   if (e == cudaSuccess) e = cudaMalloc(&c->scal, (64 + 512) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c->scal, 0, (64 + 512) * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c->scald, 8 * sizeof(double));
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
@@ -517,6 +529,20 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
   if (cands.empty()) return fail(c, STDIC_E_UNSUPPORTED, "no launch shape fits this subset size");
   b.queue_head = c->scal + 4;  // [4] team phase, [5] single-warp phase
   b.n_big = c->scal + 6;
+  // tensor maps of the deformed frame(s) for the TMA footprint copies
+  b.gbox_n = 0;
+  b.tma_err = c->scal + kTmaErrSlot;
+  {
+    const int nf = b.frames > 0 ? b.frames : 1;
+    const bool stacked_ok = nf == 1 || b.g_stride == (long long)b.a.W * b.a.H;
+    if (b.g32 && stacked_ok) {
+      int n = 0;
+      while (n < stdic::kGBoxes && stdic::encode_image_map_f32(b.g32, b.a.W, (long long)b.a.H * nf, stdic::gbox_side(n),
+                                                               &b.gmap[n]))
+        ++n;
+      b.gbox_n = n == stdic::kGBoxes ? n : 0;
+    }
+  }
   auto launch = [&](const BatchedCand& cd) -> int {
     b.warps_per_subset = cd.tw;
     b.smem_px = cd.smem_px;

@@ -451,6 +451,7 @@ struct TeamCtl {
   float jf[6], j1[6];
   int item;
   int pad[3];
+  unsigned long long mbar;  // completion barrier of the team's footprint copies (TMA)
 };
 
 // Double-float helpers: a pair (hi, lo) of FP32 values represents hi + lo.
@@ -499,7 +500,7 @@ STDIC_DEV void add_jt6(float (&kg)[6], float2 g2, float dx, float dy, float t) {
 // iterations, tempg and five bitmaps; 2-DOF: tempg, tempf and five bitmaps.
 __host__ __device__ __forceinline__ int tile_px_bytes(bool two) { return two ? 13 : 17; }
 __host__ __device__ __forceinline__ size_t tiles_bytes(int px, bool two) {
-  return ((size_t)px * tile_px_bytes(two) + 15) / 16 * 16;
+  return ((size_t)px * tile_px_bytes(two) + 127) / 128 * 128;
 }
 // Bytes of one warp's global scratch slice (the per-pixel arrays for npx_max
 // pixels), a multiple of 16 so that every slice keeps the alignment of the
@@ -508,10 +509,13 @@ __host__ __device__ __forceinline__ size_t slice_bytes(int npx_max, bool two) {
   return ((size_t)npx_max * tile_px_bytes(two) + 15) / 16 * 16;
 }
 __host__ __device__ __forceinline__ size_t gtile_bytes(int gt) {
-  return ((size_t)(gt > 0 ? gt : 0) * 4 + 15) / 16 * 16;
+  return ((size_t)(gt > 0 ? gt : 0) * 4 + 127) / 128 * 128;
 }
+// a team's slot, a multiple of 128 bytes so that every team's staging area
+// (right after its 128-byte-rounded tiles) starts on a 128-byte boundary
 __host__ __device__ __forceinline__ size_t team_bytes(int px, bool two, int tw, int gt) {
-  return tiles_bytes(px, two) + gtile_bytes(gt) + sizeof(TeamCtl) + sizeof(float) * 32 * tw + 16 * tw + 64;
+  const size_t b = tiles_bytes(px, two) + gtile_bytes(gt) + sizeof(TeamCtl) + sizeof(float) * 32 * tw + 16 * tw + 64;
+  return (b + 127) / 128 * 128;
 }
 
 // Asynchronous 4-byte global -> shared copy (no register staging) and the
@@ -560,12 +564,44 @@ size_t batched_scratch_bytes(int npx_max, bool two, long long warps) {
 }
 
 int batched_small_px(int sm_px, bool two, int tw, int gtile) {
-  const size_t sub = (team_bytes(sm_px, two, tw, gtile) / tw) & ~(size_t)15;
+  const size_t sub = (team_bytes(sm_px, two, tw, gtile) / tw) & ~(size_t)127;
   const int gs = gtile / tw;
   const long long fixed = (long long)(gtile_bytes(gs) + sizeof(TeamCtl) + sizeof(float) * 32 + 16 + 64 + 15);
   long long px = ((long long)sub - fixed) / tile_px_bytes(two);
   while (px > 0 && team_bytes((int)px, two, 1, gs) > sub) --px;
   return (int)(px > 0 ? px : 0);
+}
+
+// TMA copy of a box x box float tile of the deformed frame at image position
+// (x, y) (x a multiple of 4: TMA's 16-byte rule) into the team's staging
+// area, completing on the team's mbarrier.  The fence orders the generic
+// accesses that the team's synchronisation before this call has completed
+// with the copy's writes (the area may have held other data).
+STDIC_DEV void tma_box_issue(const CUtensorMap* map, float* dst, int x, int y, unsigned long long* mbar,
+                             unsigned bytes) {
+  const unsigned sbar = (unsigned)__cvta_generic_to_shared(mbar);
+  const unsigned sdst = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          sdst),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(sbar)
+      : "memory");
+}
+
+// Bounded wait for the completion of the mbarrier phase of the given parity.
+STDIC_DEV bool tma_box_wait(unsigned long long* mbar, unsigned parity, int polls) {
+  const unsigned sbar = (unsigned)__cvta_generic_to_shared(mbar);
+  for (int it = 0; it < polls; ++it) {
+    unsigned done;
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                 : "=r"(done)
+                 : "r"(sbar), "r"(parity)
+                 : "memory");
+    if (done) return true;
+  }
+  return false;
 }
 
 // One subset on one team: set-up, iterations and outputs.  base/ctl/fscr/iscr
@@ -574,7 +610,7 @@ int batched_small_px(int sm_px, bool two, int tw, int gtile) {
 template <int TW, bool TWO, int STAGE>
 STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, unsigned char* base,
                           TeamCtl* ctl, float* fscr, int* iscr, unsigned char* gbase, int smpx,
-                          float* gt, int gcap) {
+                          float* gt, int gcap, unsigned& gphase, bool& tma_ok) {
   const IcgnArgs& a = B.a;
   const int lane = threadIdx.x & 31;
   constexpr int stage = STAGE;
@@ -904,6 +940,9 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
   bool err = false;
   bool oob = run ? corners_oob_warp(P, (int)x0, (int)y0, (int)x1, (int)y1, mx, my, a.W, a.H, lane) : false;
   float ibf = 1.f / bottomf;
+  // the g box staged by TMA for this subset (tbox 0: none): image position of
+  // its first element and its side; reused while the footprint stays inside
+  int tbox = 0, bgx0 = 0, bgy0 = 0;
   while (run && step <= kMaxIter && normNew > tolf && normAbs > tolf) {
     ++step;
     if constexpr (!TWO) {
@@ -1001,13 +1040,49 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
           const long long cx0 = ax0 < 0 ? 0 : ax0, cx1 = ax1 > fr.W - 1 ? fr.W - 1 : ax1;
           const long long cy0 = ay0 < 0 ? 0 : ay0, cy1 = ay1 > fr.H - 1 ? fr.H - 1 : ay1;
           const long long w_ = cx1 - cx0 + 1, h_ = cy1 - cy0 + 1;
-          if (w_ >= 4 && h_ >= 4 && w_ <= gcap && h_ <= gcap && w_ * h_ <= gcap) {
+          if (B.gbox_n > 0 && tma_ok) {
+            // one TMA box per subset, with a 2-pixel margin, copied again
+            // only when the footprint leaves it
+            if (!(tbox > 0 && cx0 >= bgx0 && cx1 < bgx0 + tbox && cy0 >= bgy0 && cy1 < bgy0 + tbox)) {
+              constexpr long long M = 2;
+              const long long bx = ((cx0 - M) >> 2) << 2;  // floor to a multiple of 4
+              const long long by = cy0 - M;
+              const long long need = max(cx1 + M - bx + 1, cy1 + M - by + 1);
+              int k = 0;
+              while (k < B.gbox_n && gbox_side(k) < need) ++k;
+              tbox = 0;
+              if (k < B.gbox_n && (long long)gbox_side(k) * gbox_side(k) <= gcap) {
+                const int box = gbox_side(k);
+                tm.sync();  // every thread is done with the previous box
+                if (tm.tl == 0)
+                  tma_box_issue(&B.gmap[k], gt, (int)bx, frame * fr.H + (int)by, &ctl->mbar,
+                                (unsigned)(box * box * 4));
+                const bool done = tma_box_wait(&ctl->mbar, gphase, 1 << 22);
+                if (!tm.any(!done, iscr)) {
+                  gphase ^= 1u;
+                  tbox = box; bgx0 = (int)bx; bgy0 = (int)by;
+                } else {
+                  // last resort: the copy has not landed after 2^22 polls.  The
+                  // error is recorded, the team polls once more for a bounded
+                  // interval so that no copy is left writing its shared memory,
+                  // and it gathers from global memory from here on
+                  if (tm.tl == 0 && B.tma_err) atomicExch(B.tma_err, 1);
+                  tma_box_wait(&ctl->mbar, gphase, 1 << 22);
+                  tma_ok = false;
+                }
+              }
+            }
+            if (tbox > 0) {
+              gx0 = bgx0; gy0 = bgy0; gtw = gth = tbox;
+              staged = true;
+            }
+          } else if (w_ >= 4 && h_ >= 4 && w_ <= gcap && h_ <= gcap && w_ * h_ <= gcap) {
             gx0 = (int)cx0; gy0 = (int)cy0; gtw = (int)w_; gth = (int)h_;
             staged = true;
           }
         }
       }
-      if (staged) {
+      if (staged && tbox == 0) {
         PixIter ti(tm.tl, tm.TT, gtw);
         const int ng_ = gtw * gth;
         for (int k = tm.tl; k < ng_; k += tm.TT, ti.next())
@@ -1263,6 +1338,18 @@ STDIC_DEV void team_loop(const BatchedArgs& B, const Team<TW>& tm, int* head, in
   float* fscr = (float*)(ctl + 1);
   int* iscr = (int*)(fscr + 32 * TW);
   const int nf = B.frames > 0 ? B.frames : 1;
+  // the team's footprint-copy barrier (its slot moves between the team and
+  // the single-warp phases of the split form, so it lives per call)
+  unsigned gphase = 0;
+  bool tma_ok = B.gbox_n > 0;
+  const unsigned sbar = (unsigned)__cvta_generic_to_shared(&ctl->mbar);
+  if (tma_ok) {
+    if (tm.tl == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tm.sync();
+  }
   for (;;) {
     if (tm.tl == 0) {
       const int q = lo + atomicAdd(head, 1);
@@ -1273,7 +1360,12 @@ STDIC_DEV void team_loop(const BatchedArgs& B, const Team<TW>& tm, int* head, in
     const int item = ctl->item;
     tm.sync();
     if (item < 0) break;
-    run_subset<TW, TWO, STAGE>(B, tm, item, base, ctl, fscr, iscr, gbase, smpx, gt, gcap);
+    run_subset<TW, TWO, STAGE>(B, tm, item, base, ctl, fscr, iscr, gbase, smpx, gt, gcap, gphase, tma_ok);
+  }
+  if (B.gbox_n > 0) {
+    tm.sync();
+    if (tm.tl == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(sbar) : "memory");
+    tm.sync();
   }
 }
 
@@ -1297,8 +1389,11 @@ STDIC_DEV void team_loop(const BatchedArgs& B, const Team<TW>& tm, int* head, in
 // reduction and runs the same update on them, so all warps carry bit-identical
 // P without a shared-memory broadcast.
 template <int TW, bool TWO, int STAGE>
-__global__ void __launch_bounds__(256, STAGE == 1 ? 3 : 2) icgn_batched_kernel(BatchedArgs B) {
-  extern __shared__ __align__(16) unsigned char dsm[];
+__global__ void __launch_bounds__(256, STAGE == 1 ? 3 : 2) icgn_batched_kernel(const __grid_constant__ BatchedArgs B) {
+  extern __shared__ __align__(128) unsigned char dsm_raw[];
+  // team slots from a 128-byte boundary (TMA copies land there); the launch
+  // adds 128 bytes of dynamic shared memory for this
+  unsigned char* const dsm = dsm_raw + ((128u - ((unsigned)__cvta_generic_to_shared(dsm_raw) & 127u)) & 127u);
   const int nf = B.frames > 0 ? B.frames : 1;
   const int Ntot = B.a.N * nf;
   const int warp = threadIdx.x >> 5;
@@ -1325,7 +1420,7 @@ __global__ void __launch_bounds__(256, STAGE == 1 ? 3 : 2) icgn_batched_kernel(B
         Team<1> t1;
         t1.id = warp;
         t1.tl = threadIdx.x & 31;
-        const size_t sub = (tb / TW) & ~(size_t)15;
+        const size_t sub = (tb / TW) & ~(size_t)127;
         team_loop<1, TWO, STAGE>(B, t1, B.queue_head + 1, 0, nrest, tbase + sub * (warp % TW),
                                  B.smem_px_small, B.gtile_small, B.scratch + gstride * (gwarp0 + warp),
                                  B.order2 + 2 * (size_t)Ntot - nrest);
@@ -1340,7 +1435,7 @@ __global__ void __launch_bounds__(256, STAGE == 1 ? 3 : 2) icgn_batched_kernel(B
       Team<1> t1;
       t1.id = warp;
       t1.tl = threadIdx.x & 31;
-      const size_t sub = (tb / TW) & ~(size_t)15;
+      const size_t sub = (tb / TW) & ~(size_t)127;
       team_loop<1, TWO, STAGE>(B, t1, B.queue_head + 1, split_q, Ntot,
                                tbase + sub * (warp % TW), B.smem_px_small, B.gtile_small,
                                B.scratch + gstride * (gwarp0 + warp));
@@ -1471,7 +1566,7 @@ cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hin
 template <int TW, bool TWO, int STAGE>
 static cudaError_t launch_tw(const BatchedArgs& b, int blocks, int threads, cudaStream_t s) {
   const int teams = threads / (TW * 32);
-  const size_t smem = batched_team_bytes(b.smem_px, TWO, TW, b.gtile) * teams;
+  const size_t smem = batched_team_bytes(b.smem_px, TWO, TW, b.gtile) * teams + 128;
   if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
   cudaError_t e = cudaFuncSetAttribute(icgn_batched_kernel<TW, TWO, STAGE>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1502,7 +1597,7 @@ cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, c
 // (any other stage) and the fused 2-DOF form.
 int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px, int gtile, int stage) {
   const int teams = threads / (tw * 32);
-  const size_t smem = batched_team_bytes(smem_px, two, tw, gtile) * teams;
+  const size_t smem = batched_team_bytes(smem_px, two, tw, gtile) * teams + 128;
   if (smem > 227 * 1024) return 0;
   int nb = 0;
   cudaError_t e = cudaSuccess;

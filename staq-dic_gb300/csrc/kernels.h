@@ -6,6 +6,7 @@
 #include <functional>
 #include <vector>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace stdic {
@@ -52,6 +53,20 @@ inline int grown_tile_pixels(int ws) {
   return (wg + 1) * (wg + 1);
 }
 
+// Square box sizes (floats a side) of the TMA copies that stage the warped g
+// footprint of a subset in shared memory; a subset takes the smallest box that
+// holds its footprint with a 2-pixel margin (a multiple of 8: TMA's 16-byte
+// rule for the inner dimension).
+constexpr int kGBoxes = 9;
+__host__ __device__ constexpr int gbox_side(int k) {  // 16, 24, 32, 40, 48, 64, 80, 96, 128
+  return k < 5 ? 16 + 8 * k : (k == 5 ? 64 : (k == 6 ? 80 : (k == 7 ? 96 : 128)));
+}
+
+// 2-D tiled tensor map of a rows x W float image (W contiguous) with a box x
+// box tile; false when TMA cannot describe it (base or pitch not 16-byte
+// aligned, or the driver entry point is missing).
+bool encode_image_map_f32(const void* base, long long W, long long rows, int box, CUtensorMap* m);
+
 // Batched FP32 queue entry, precomputed per call on the device.
 struct BatchedArgs {
   IcgnArgs a;
@@ -84,6 +99,12 @@ struct BatchedArgs {
   void* st6;              // SubsetState6 per item
   double* H6;             // 21 per item: packed lower Hessian (row-major)
   double* Hinv6;          // 36 per item: the FP64 inverse Hessian (row-major) as FP32 pairs (hi, lo)
+  // TMA staging of the warped g footprint: gbox_n tensor maps of g32 (W x
+  // H*frames floats), gmap[k] with gbox_side(k)-square boxes; gbox_n = 0 stages
+  // per element (cp.async) or gathers from global memory instead
+  int gbox_n;
+  int* tma_err;           // set to 1 when a footprint copy's bounded wait gives up
+  CUtensorMap gmap[kGBoxes];
 };
 
 // Per-subset state handed from the 6-DOF set-up stage to the iterations.

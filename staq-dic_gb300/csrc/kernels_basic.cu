@@ -207,6 +207,19 @@ bool image_tensor_map(const void* img, int W, int H, int dtype, CUtensorMap* m) 
 }
 }  // namespace
 
+bool encode_image_map_f32(const void* base, long long W, long long rows, int box, CUtensorMap* m) {
+  if (((uintptr_t)base & 15) != 0 || (W * 4) % 16 != 0 || box < 4 || box > 256 || (box * 4) % 16 != 0) return false;
+  auto enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)W * 4};
+  const cuuint32_t bx[2] = {(cuuint32_t)box, (cuuint32_t)box};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, bx, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 cudaError_t launch_gradient(const void* img, const uint8_t* mask, int W, int H, void* dfdx,
                             void* dfdy, int dtype, cudaStream_t s, int* err) {
   const int Wo = W - 6, Ho = H - 6;

@@ -647,6 +647,90 @@ def measure_adjoint(ctx, torch, size=4096):
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
         out[mode] = {"ms": float(np.mean(ms)), "subsets_per_s": N / (np.mean(ms) * 1e-3)}
+    # the FP64 oracle on all host cores over a seeded sample of subsets: its
+    # throughput, and the FP32 gradients' error against it on that sample
+    from oracle import build as ob
+    ob.build_oracle()
+    from oracle import oracle as orc
+    orc.set_threads(os.cpu_count() or 1)
+    idx = np.sort(rng.choice(N, min(N, 4000), replace=False))
+    Uh, Fh = U.cpu().numpy().reshape(-1, 2)[idx].ravel(), F.cpu().numpy().reshape(-1, 4)[idx].ravel()
+    f64, g64 = w["f"].astype(np.float64), w["g"].astype(np.float64)
+    t0 = time.perf_counter()
+    co, dUo, dFo, _ = orc.icgn_adjoint(f64, g64, None, c[idx], 32, Uh, Fh)
+    dt = time.perf_counter() - t0
+    _, cn, dU, dF, _ = staqdic.icgn_adjoint(U, F, ct, f, g, 32, precision="batched", want_dg=False, size=(W, H),
+                                            ctx=ctx)
+    dU = dU.cpu().numpy().reshape(-1, 2)[idx]
+    dF = dF.cpu().numpy().reshape(-1, 4)[idx]
+    ok = np.isfinite(co)
+    gref = np.concatenate([dUo.reshape(-1, 2), dFo.reshape(-1, 4)], 1)[ok]
+    gout = np.concatenate([dU, dF], 1)[ok]
+    rel = np.linalg.norm(gout - gref, axis=1) / np.linalg.norm(gref, axis=1)
+    out["cpu_oracle"] = {"subsets_per_s": idx.size / dt, "cores": os.cpu_count() or 1,
+                         "sample": "%d seeded subsets, FP64 with dg" % idx.size}
+    out["fp32_grad_rel_err_max"] = float(rel.max())
+    return out
+
+
+def measure_c1(ctx, torch, steps=20):
+    """C1, the reference's CPU-runnable case: the 256^2 affine speckle pair, a
+    uniform 14 x 14 grid of 32-px subsets (196 nodes).  The integer search
+    (S = 6), the FP64 plain and FP32 batched LocalICGNQuadtree, one Subpb2
+    solve, each through the public API with host arrays (copies included);
+    the oracle on all host cores beside them."""
+    import staqdic
+    from oracle import build as ob
+    ob.build_oracle()
+    from oracle import oracle as orc
+    orc.set_threads(os.cpu_count() or 1)
+    w = make_workload("uniform256")
+    c, el = w["coordinatesFEM"], w["elementsFEM"]
+    N = c.shape[0]
+    f64, g64 = w["f"].astype(np.float64), w["g"].astype(np.float64)
+    W, H = f64.shape
+    wl = np.asarray(w["winsize_list"], np.int32)
+
+    def timed(fn, k):
+        fn()
+        ts = []
+        for _ in range(k):
+            t0 = time.perf_counter()
+            r = fn()
+            ts.append(time.perf_counter() - t0)
+        return 1e3 * float(np.median(ts)), r
+
+    out = {"workload": "uniform256: 256x256 affine speckle pair, %d subsets of 32 px" % N}
+    ms, _ = timed(lambda: staqdic.funIntegerSearch(f64, g64, 6, (1, W), (1, H), 32, 16, ctx=ctx, qfactors=False), steps)
+    cms, _ = timed(lambda: orc.funIntegerSearch(f64, g64, 6, (1, W), (1, H), 32, 16), 3)
+    out["integer_search"] = {"ms_gpu": ms, "ms_cpu_oracle": cms}
+    Df = staqdic.funImgGradient(f64, ImgRefMask=w["maskf"], ctx=ctx)
+    Dfo = orc.funImgGradient(f64, w["maskf"])
+    DP = {"winsize": int(wl.max()), "winsize_per_node": wl}
+    res = {}
+    for prec in ("plain", "batched"):
+        ff, gg, D = (f64, g64, Df) if prec == "plain" else (w["f"], w["g"], staqdic.funImgGradient(
+            w["f"], ImgRefMask=w["maskf"], ctx=ctx, dtype=np.float32))
+        ms, r = timed(lambda: staqdic.LocalICGNQuadtree(w["U0"], c, D, ff, gg, DP, "GaussNewton", TOL, precision=prec,
+                                                        ctx=ctx), steps)
+        res[prec] = (ms, r)
+    cms, ro = timed(lambda: orc.LocalICGNQuadtree(w["U0"], c, Dfo, f64, g64, wl, TOL), 3)
+    Uo, convo = ro[0], ro[3]
+    for prec, (ms, r) in res.items():
+        U, conv = r[0], r[4]
+        n = int(converged_rule(U, conv, Uo).sum())
+        out[prec] = {"ms": ms, "subsets_per_s": n / (ms * 1e-3), "converged": n,
+                     "max_abs_du_px_equal_codes": float(np.nanmax(np.abs(U - Uo).reshape(-1, 2).max(1)[conv == convo]))}
+    out["cpu_oracle"] = {"ms": cms, "subsets_per_s": int(converged_rule(Uo, convo).sum()) / (cms * 1e-3),
+                         "cores": os.cpu_count() or 1}
+    mesh = {"coordinatesFEM": c, "elementsFEM": el, "dirichlet": w["dirichlet"]}
+    beta, mu = 1e-3 * 16 ** 2 * 1e-3, 1e-3
+    U1 = np.nan_to_num(res["plain"][1][0])
+    F1 = np.zeros(4 * N)
+    ms, _ = timed(lambda: staqdic.Subpb2Quadtree(mesh, 2, beta, mu, U1, F1, np.zeros(4 * N), np.zeros(2 * N), 0.0, 16,
+                                                 ctx=ctx), steps)
+    cms, _ = timed(lambda: orc.Subpb2Quadtree(c, el, w["dirichlet"], None, 2, beta, mu, U1, F1, 0.0, 16), 3)
+    out["subpb2"] = {"ms_gpu": ms, "ms_cpu_oracle_direct_solve": cms}
     return out
 
 
@@ -704,7 +788,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 1024^2 pass, the ADMM iterations, the adjoint and the multi-frame launch")
-    ap.add_argument("--only", choices=["c2", "admm", "adjoint", "c5", "mg"],
+    ap.add_argument("--only", choices=["c2", "admm", "adjoint", "c5", "mg", "c1"],
                     help="run one secondary measurement alone and print it (for profiling)")
     ap.add_argument("--profile", choices=["batched", "plain"],
                     help="only the headline workload's passes of one form (warm-up + steps), for ncu captures")
@@ -745,6 +829,8 @@ def main():
             res = measure_adjoint(ctx, torch)
         elif args.only == "mg":
             res = measure_mg(ctx, torch)
+        elif args.only == "c1":
+            res = measure_c1(ctx, torch)
         else:
             res = measure_c5(ctx, torch, flush)
         print(json.dumps({"only": args.only, "result": res}), flush=True)
@@ -913,6 +999,7 @@ def main():
         out["adjoint_c4"] = guarded(measure_adjoint, ctx, torch)
         out["c5"] = guarded(measure_c5, ctx, torch, flush)
         out["mg_search"] = guarded(measure_mg, ctx, torch)
+        out["c1"] = guarded(measure_c1, ctx, torch)
     print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()

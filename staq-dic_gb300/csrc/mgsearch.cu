@@ -121,15 +121,42 @@ __global__ void __launch_bounds__(256) ii_rows_kernel(const double* __restrict__
   }
 }
 
-// Column prefix sums of the row sums; row 0 is zero.
-__global__ void ii_cols_kernel(int W, int H, double* I1, double* I2, int* In) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+// Column prefix sums of the row sums (row 0 is zero): a 32 x 32 CTA takes 32
+// columns, each of its 32 thread rows a chunk of rows; the chunk totals are
+// scanned in shared memory and added back.
+__global__ void __launch_bounds__(1024) ii_cols_kernel(int W, int H, double* I1, double* I2, int* In) {
+  __shared__ double t1[32][33], t2[32][33];
+  __shared__ int tn[32][33];
+  const int x = blockIdx.x * 32 + threadIdx.x, ch = threadIdx.y;
   const int W1 = W + 1;
+  const int per = (H + 31) / 32;
+  const int y0 = 1 + ch * per, y1 = min(H, y0 + per - 1);
+  double a1 = 0, a2 = 0;
+  int an = 0;
+  if (x <= W) {
+    if (ch == 0) { I1[x] = 0; I2[x] = 0; In[x] = 0; }
+    for (int y = y0; y <= y1; ++y) {
+      const size_t k = (size_t)y * W1 + x;
+      a1 += I1[k]; a2 += I2[k]; an += In[k];
+    }
+  }
+  t1[ch][threadIdx.x] = a1; t2[ch][threadIdx.x] = a2; tn[ch][threadIdx.x] = an;
+  __syncthreads();
+  if (ch == 0) {
+    double c1 = 0, c2 = 0;
+    int cn = 0;
+    for (int k = 0; k < 32; ++k) {
+      const double u1 = t1[k][threadIdx.x], u2 = t2[k][threadIdx.x];
+      const int un = tn[k][threadIdx.x];
+      t1[k][threadIdx.x] = c1; t2[k][threadIdx.x] = c2; tn[k][threadIdx.x] = cn;
+      c1 += u1; c2 += u2; cn += un;
+    }
+  }
+  __syncthreads();
   if (x > W) return;
-  I1[x] = 0; I2[x] = 0; In[x] = 0;
-  double c1 = 0, c2 = 0;
-  int cn = 0;
-  for (int y = 1; y <= H; ++y) {
+  double c1 = t1[ch][threadIdx.x], c2 = t2[ch][threadIdx.x];
+  int cn = tn[ch][threadIdx.x];
+  for (int y = y0; y <= y1; ++y) {
     const size_t k = (size_t)y * W1 + x;
     c1 += I1[k]; c2 += I2[k]; cn += In[k];
     I1[k] = c1; I2[k] = c2; In[k] = cn;
@@ -197,49 +224,79 @@ STDIC_DEV bool block_rects(const MgBlock& b, int W, int H, bool level1, int* tx0
 // meanT and denT = sqrt(mn-1) std(T); ok = 0 where the reference's try block
 // fails (bad crop, normxcorr2 error: non-finite data, constant template)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) mg_stats_kernel(MgImg im, const MgBlock* __restrict__ blocks, int level1,
-                                                       MgStat* __restrict__ st) {
-  __shared__ double red[32];
-  const MgBlock b = blocks[blockIdx.x];
+// Pass 1 (pass = 0) and pass 2 (pass = 1) of the template statistics: nct
+// CTAs per block add the template's values (pass 1) or squared deviations from
+// its mean (pass 2) over a strided share of its pixels; part[block][cta]
+// receives the CTA's sum, bad[block][cta] whether it saw a non-finite value.
+__global__ void __launch_bounds__(256) mg_tsum_kernel(MgImg im, const MgBlock* __restrict__ blocks, int level1,
+                                                      int nct, int pass, const MgStat* __restrict__ st,
+                                                      double* __restrict__ part, int* __restrict__ bad) {
+  __shared__ double red[8];
+  const int bi = blockIdx.x / nct, cta = blockIdx.x % nct;
   int tx0, ty0, m, n, ax0, ay0, Mw, Nw;
-  const bool rects = block_rects(b, im.W, im.H, level1 != 0, &tx0, &ty0, &m, &n, &ax0, &ay0, &Mw, &Nw);
-  if (!rects) {
-    if (threadIdx.x == 0) st[blockIdx.x] = MgStat{0.0, 0.0, 0, 0};
-    return;
+  const bool rects = block_rects(blocks[bi], im.W, im.H, level1 != 0, &tx0, &ty0, &m, &n, &ax0, &ay0, &Mw, &Nw);
+  double acc = 0;
+  int nf = 0;
+  if (rects && (pass == 0 || st[bi].ok)) {
+    const double mean = pass ? st[bi].meanT : 0.0;
+    const int np = m * n;
+    for (int q = cta * blockDim.x + threadIdx.x; q < np; q += nct * blockDim.x) {
+      const int i = q % m, j = q / m;
+      const double v = im.f[(size_t)(ty0 + j) * im.W + tx0 + i];
+      if (pass == 0) {
+        if (!isfinite(v)) nf = 1;
+        acc += v;
+      } else {
+        const double d = v - mean;
+        acc += d * d;
+      }
+    }
   }
-  const int W1 = im.W + 1;
-  const bool finiteA = rect_sum(im.In, W1, ax0, ax0 + Mw - 1, ay0, ay0 + Nw - 1) == 0;
-  const long long np = (long long)m * n;
-  auto bsum = [&](double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-    __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  nf = __syncthreads_or(nf);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
     double t = 0;
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
-    return t;
-  };
-  double s = 0;
-  int bad = 0;
-  for (long long q = threadIdx.x; q < np; q += blockDim.x) {
-    const int i = (int)(q % m), j = (int)(q / m);
-    const double v = im.f[(size_t)(ty0 + j) * im.W + tx0 + i];
-    if (!isfinite(v)) bad = 1;
-    s += v;
+    part[blockIdx.x] = t;
+    if (pass == 0) bad[blockIdx.x] = nf;
   }
-  bad = __syncthreads_or(bad);
-  const double mn = (double)np;
-  const double meanT = bsum(s) / mn;
-  double q2 = 0;
-  for (long long q = threadIdx.x; q < np; q += blockDim.x) {
-    const int i = (int)(q % m), j = (int)(q / m);
-    const double d = im.f[(size_t)(ty0 + j) * im.W + tx0 + i] - meanT;
-    q2 += d * d;
-  }
-  const double stdT = sqrt(bsum(q2) / (mn - 1));
-  if (threadIdx.x == 0) {
-    const bool ok = finiteA && !bad && (stdT != 0);
-    st[blockIdx.x] = MgStat{meanT, sqrt(mn - 1) * stdT, ok ? 1 : 0, 0};
+}
+
+// Per block, after pass 1 (pass = 0): the crops' validity, meanT and the
+// non-finite checks of C and D; after pass 2: denT = sqrt(mn-1) std(T) and
+// ok = 0 where the reference's try block fails (bad crop, normxcorr2 error:
+// non-finite data, constant template).  The partial sums are added in CTA
+// order, so the result does not depend on scheduling.
+__global__ void mg_tstat_kernel(MgImg im, const MgBlock* __restrict__ blocks, int nb, int level1, int nct, int pass,
+                                const double* __restrict__ part, const int* __restrict__ bad,
+                                MgStat* __restrict__ st) {
+  const int bi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bi >= nb) return;
+  int tx0, ty0, m, n, ax0, ay0, Mw, Nw;
+  const bool rects = block_rects(blocks[bi], im.W, im.H, level1 != 0, &tx0, &ty0, &m, &n, &ax0, &ay0, &Mw, &Nw);
+  const double mn = (double)m * (double)n;
+  if (pass == 0) {
+    if (!rects) {
+      st[bi] = MgStat{0.0, 0.0, 0, 0};
+      return;
+    }
+    double sum = 0;
+    int nf = 0;
+    for (int c = 0; c < nct; ++c) {
+      sum += part[(size_t)bi * nct + c];
+      nf |= bad[(size_t)bi * nct + c];
+    }
+    const bool finiteA = rect_sum(im.In, im.W + 1, ax0, ax0 + Mw - 1, ay0, ay0 + Nw - 1) == 0;
+    st[bi] = MgStat{sum / mn, 0.0, (finiteA && !nf) ? 1 : 0, 0};
+  } else {
+    if (!st[bi].ok) return;
+    double q = 0;
+    for (int c = 0; c < nct; ++c) q += part[(size_t)bi * nct + c];
+    const double stdT = sqrt(q / (mn - 1));
+    st[bi].denT = sqrt(mn - 1) * stdT;
+    st[bi].ok = stdT != 0 ? 1 : 0;
   }
 }
 
@@ -249,9 +306,9 @@ __global__ void __launch_bounds__(1024) mg_stats_kernel(MgImg im, const MgBlock*
 // z[y][x] = A(x, y) + i Tz(m-1-x, n-1-y), zero padded to Fx x Fy
 __global__ void mg_fill_kernel(MgImg im, const MgBlock* __restrict__ blk, const MgStat* __restrict__ st,
                                double2* __restrict__ z, int Fx, int Fy) {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= (long long)Fx * Fy) return;
-  const int x = (int)(k % Fx), y = (int)(k / Fx);
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= Fx) return;
+  const size_t k = (size_t)y * Fx + x;
   int tx0, ty0, m, n, ax0, ay0, Mw, Nw;
   block_rects(blk[0], im.W, im.H, true, &tx0, &ty0, &m, &n, &ax0, &ay0, &Mw, &Nw);
   double a = 0, t = 0;
@@ -263,9 +320,9 @@ __global__ void mg_fill_kernel(MgImg im, const MgBlock* __restrict__ blk, const 
 // P = FFT(A) FFT(Tflip) from Z = FFT(A + i Tflip), in the transposed layout
 // Zt[kx][ky]: FFT(A) = (Z(k) + conj Z(-k)) / 2, FFT(Tflip) = (Z(k) - conj Z(-k)) / 2i
 __global__ void mg_product_kernel(const double2* __restrict__ Zt, double2* __restrict__ Pt, int Fx, int Fy) {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= (long long)Fx * Fy) return;
-  const int ky = (int)(k % Fy), kx = (int)(k / Fy);
+  const int ky = blockIdx.x * blockDim.x + threadIdx.x, kx = blockIdx.y;
+  if (ky >= Fy) return;
+  const size_t k = (size_t)kx * Fy + ky;
   const int mx = kx == 0 ? 0 : Fx - kx, my = ky == 0 ? 0 : Fy - ky;
   const double2 z1 = Zt[k], z2 = Zt[(size_t)mx * Fy + my];
   const double ar = 0.5 * (z1.x + z2.x), ai = 0.5 * (z1.y - z2.y);  // (z1 + conj z2) / 2
@@ -282,11 +339,29 @@ __global__ void __launch_bounds__(256) mg_denmax_kernel(MgImg im, const MgBlock*
   if (!st[bi].ok) return;
   int tx0, ty0, m, n, ax0, ay0, Mw, Nw;
   block_rects(blocks[bi], im.W, im.H, level1 != 0, &tx0, &ty0, &m, &n, &ax0, &ay0, &Mw, &Nw);
-  const long long R = Mw + m - 1, C = Nw + n - 1;
+  const int R = Mw + m - 1, C = Nw + n - 1;
   const double mn = (double)m * n, denT = st[bi].denT;
+  if (!level1) {
+    // The tolerance only decides lags whose denominator is at most
+    // sqrt(eps(max |den|)), and every denominator of the map is at most
+    // denT sqrt(sum of A^2 over the window D).  When every lag of the 13 x 14
+    // crop lies above the tolerance that bound implies (doubled, against
+    // rounding), the values findpeak reads do not depend on the map's maximum
+    // and the scan is skipped (dmax stays 0, the smallest tolerance).
+    __shared__ int s_need;
+    const double ub = 2.0 * denT * sqrt(fmax(rect_sum(im.I2, im.W + 1, ax0, ax0 + Mw - 1, ay0, ay0 + Nw - 1), 0.0));
+    const double tmax = sqrt(eps_of_d(ub));
+    int low = 0;
+    for (int l = threadIdx.x; l < kLags; l += blockDim.x)
+      if (!(lag_den(im, ax0, ay0, Mw, Nw, m, n, l % kLagR - 1, l / kLagR - 1, denT, mn) > tmax)) low = 1;
+    low = __syncthreads_or(low);
+    if (threadIdx.x == 0) s_need = low;
+    __syncthreads();
+    if (!s_need) return;
+  }
   double best = 0;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < R * C; k += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(k % R), c = (int)(k / R);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < R * C; k += gridDim.x * blockDim.x) {
+    const int r = k % R, c = k / R;
     best = fmax(best, lag_den(im, ax0, ay0, Mw, Nw, m, n, r - m + 1, c - n + 1, denT, mn));
   }
   for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_down_sync(0xffffffffu, best, o));
@@ -306,8 +381,8 @@ __global__ void __launch_bounds__(256) mg_l1_max_kernel(MgImg im, const MgBlock*
   const double tol = sqrt(eps_of_d(__longlong_as_double((long long)dmax[0])));
   const double clip = sqrt(eps_of_d(1.0));
   double bv = -INFINITY;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < R * C; k += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(k % R), c = (int)(k / R);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < (int)(R * C); k += gridDim.x * blockDim.x) {
+    const int r = k % (int)R, c = k / (int)R;
     const double num = q[(size_t)c * Fx + r].x * scale;
     bv = fmax(bv, ncc_value(num, lag_den(im, ax0, ay0, Mw, Nw, m, n, r - m + 1, c - n + 1, denT, mn), tol, clip));
   }
@@ -343,8 +418,8 @@ __global__ void __launch_bounds__(256) mg_l1_first_kernel(MgImg im, const MgBloc
   const double tol = sqrt(eps_of_d(__longlong_as_double((long long)dmax[0])));
   const double clip = sqrt(eps_of_d(1.0));
   long long bi = 0x7fffffffffffffffLL;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < R * C; k += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(k % R), c = (int)(k / R);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < (int)(R * C); k += gridDim.x * blockDim.x) {
+    const int r = k % (int)R, c = k / (int)R;
     const double num = q[(size_t)c * Fx + r].x * scale;
     const double v = ncc_value(num, lag_den(im, ax0, ay0, Mw, Nw, m, n, r - m + 1, c - n + 1, denT, mn), tol, clip);
     if (v >= gmax - kPeakTie) { bi = k; break; }
@@ -978,7 +1053,7 @@ int integer_search_mg(const double* f, const double* g, int W, int H, const doub
   int* In = fw.take<int>(nI);
   MgImg im{f, g, W, H, I1, I2, In};
   ii_rows_kernel<<<H, 256, 0, s>>>(g, W, I1, I2, In); ++nl;
-  ii_cols_kernel<<<(W + 1 + 255) / 256, 256, 0, s>>>(W, H, I1, I2, In); ++nl;
+  ii_cols_kernel<<<(W + 1 + 31) / 32, dim3(32, 32), 0, s>>>(W, H, I1, I2, In); ++nl;
   MG_TRY(cudaGetLastError());
 
   // ROI and border gaps (:5-9)
@@ -1015,6 +1090,7 @@ int integer_search_mg(const double* f, const double* g, int W, int H, const doub
     cz.take<unsigned long long>(1);
     cz.take<double>(npart1);
     cz.take<long long>(npart1);
+    cz.take<int>(npart1);
     need1 = cz.off;
   }
   void* w1 = grow(need1);
@@ -1033,10 +1109,15 @@ int integer_search_mg(const double* f, const double* g, int W, int H, const doub
   unsigned long long* dm1 = c1.take<unsigned long long>(1);
   double* pv = c1.take<double>(npart1);
   long long* pi = c1.take<long long>(npart1);
+  int* pbad = c1.take<int>(npart1);
   MgBlock hb{gx[0], gx[1], gy[0], gy[1], gx[0], gx[1], gy[0], gy[1], 0.0, 0.0};
   MG_TRY(cudaMemcpyAsync(b1, &hb, sizeof(MgBlock), cudaMemcpyHostToDevice, s));
   MG_TRY(cudaMemsetAsync(dm1, 0, sizeof(unsigned long long), s));
-  mg_stats_kernel<<<1, 1024, 0, s>>>(im, b1, 1, st1); ++nl;
+  // template statistics of the whole region: 1024 CTAs, two passes
+  mg_tsum_kernel<<<npart1, 256, 0, s>>>(im, b1, 1, npart1, 0, st1, pv, pbad); ++nl;
+  mg_tstat_kernel<<<1, 32, 0, s>>>(im, b1, 1, 1, npart1, 0, pv, pbad, st1); ++nl;
+  mg_tsum_kernel<<<npart1, 256, 0, s>>>(im, b1, 1, npart1, 1, st1, pv, pbad); ++nl;
+  mg_tstat_kernel<<<1, 32, 0, s>>>(im, b1, 1, 1, npart1, 1, pv, pbad, st1); ++nl;
   MgStat hst;
   MG_TRY(cudaMemcpyAsync(&hst, st1, sizeof(MgStat), cudaMemcpyDeviceToHost, s));
   MG_TRY(cudaStreamSynchronize(s));
@@ -1044,15 +1125,13 @@ int integer_search_mg(const double* f, const double* g, int W, int H, const doub
     *err = "normxcorr2 of the whole region fails (constant or non-finite template, or non-finite image)";
     return -1;
   }
-  const long long nz = (long long)Fx * Fy;
-  const int zb = (int)((nz + 255) / 256);
-  mg_fill_kernel<<<zb, 256, 0, s>>>(im, b1, st1, z, Fx, Fy); ++nl;
+  mg_fill_kernel<<<dim3((Fx + 255) / 256, Fy), 256, 0, s>>>(im, b1, st1, z, Fx, Fy); ++nl;
   MG_TRY(launch_fft_twiddles(twx, Fx, s)); ++nl;
   MG_TRY(launch_fft_twiddles(twy, Fy, s)); ++nl;
   MG_TRY(launch_fft_rows(z, Fy, Fx, twx, false, s)); ++nl;
   MG_TRY(launch_transpose_c(z, zt, Fy, Fx, s)); ++nl;
   MG_TRY(launch_fft_rows(zt, Fx, Fy, twy, false, s)); ++nl;
-  mg_product_kernel<<<zb, 256, 0, s>>>(zt, z, Fx, Fy); ++nl;
+  mg_product_kernel<<<dim3((Fy + 255) / 256, Fx), 256, 0, s>>>(zt, z, Fx, Fy); ++nl;
   MG_TRY(launch_fft_rows(z, Fx, Fy, twy, true, s)); ++nl;
   MG_TRY(launch_transpose_c(z, zt, Fx, Fy, s)); ++nl;
   MG_TRY(launch_fft_rows(zt, Fy, Fx, twx, true, s)); ++nl;
@@ -1118,7 +1197,11 @@ int integer_search_mg(const double* f, const double* g, int W, int H, const doub
     ncts.push_back(nct);
   }
   size_t part_max = 0;
-  for (size_t k = 0; k < modes.size(); ++k) part_max = std::max(part_max, (size_t)nbs[k] * ncts[k] * kLags);
+  size_t tsum_max = 1;
+  for (size_t k = 0; k < modes.size(); ++k) {
+    part_max = std::max(part_max, (size_t)nbs[k] * ncts[k] * kLags);
+    tsum_max = std::max(tsum_max, (size_t)nbs[k] * ncts[k]);
+  }
   // the levels' scratch (a second grow: level 1's transforms are no longer needed)
   size_t need2 = 0;
   {
@@ -1130,6 +1213,8 @@ int integer_search_mg(const double* f, const double* g, int W, int H, const doub
     cz.take<unsigned long long>(nb);
     cz.take<double>(part_max);
     cz.take<double>(5 * (size_t)nb);
+    cz.take<double>(tsum_max);
+    cz.take<int>(tsum_max);
     need2 = cz.off;
   }
   void* w2 = grow(need2);
@@ -1145,13 +1230,20 @@ int integer_search_mg(const double* f, const double* g, int W, int H, const doub
   unsigned long long* dmax = c2.take<unsigned long long>(nb);
   double* part = c2.take<double>(part_max);
   double* coll = c2.take<double>(5 * (size_t)nb);
+  double* tpart = c2.take<double>(tsum_max);
+  int* tbad = c2.take<int>(tsum_max);
   MG_TRY(cudaMemcpyAsync(cur, &hb, sizeof(MgBlock), cudaMemcpyHostToDevice, s));
   long long ncur = 1;
   for (size_t k = 0; k < modes.size(); ++k) {
     const long long nn = nbs[k];
     const int nct = ncts[k];
     mg_split_kernel<<<(int)((ncur + 255) / 256), 256, 0, s>>>(cur, nxt, (int)ncur, modes[k], (double)winsize); ++nl;
-    mg_stats_kernel<<<(unsigned)nn, 256, 0, s>>>(im, nxt, 0, st); ++nl;
+    const unsigned nt = (unsigned)(nn * nct);
+    const int sb = (int)((nn + 127) / 128);
+    mg_tsum_kernel<<<nt, 256, 0, s>>>(im, nxt, 0, nct, 0, st, tpart, tbad); ++nl;
+    mg_tstat_kernel<<<sb, 128, 0, s>>>(im, nxt, (int)nn, 0, nct, 0, tpart, tbad, st); ++nl;
+    mg_tsum_kernel<<<nt, 256, 0, s>>>(im, nxt, 0, nct, 1, st, tpart, tbad); ++nl;
+    mg_tstat_kernel<<<sb, 128, 0, s>>>(im, nxt, (int)nn, 0, nct, 1, tpart, tbad, st); ++nl;
     MG_TRY(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long) * nn, s));
     {
       // lags of a block's full map: about (2 wx + 11)(2 wy + 11); 8 lags per thread

@@ -768,6 +768,48 @@ def measure_mg(ctx, torch, steps=5):
     return out
 
 
+def measure_series(ctx, torch):
+    """The accumulative frame loop (staqdic.series.run_series) over a loading
+    sequence of ten 1024^2 frames of the plate with a hole (Kirsch field at
+    0.2 % .. 2 % far-field strain, 19.9k quadtree nodes), batched FP32: the
+    initial guess of each frame from the previous result (frames 1-4) or
+    funPOR_GPR (frames 5-9), LocalICGNQuadtree, the NaN fill, all through the
+    public API with host arrays.  The oracle's FP64 loop (oracle/series.py)
+    is timed once on the same frames as the CPU reference point."""
+    import staqdic
+    from staqdic import series
+    w = make_workload("ramp1024")
+    mesh = {"coordinatesFEM": w["coordinatesFEM"], "elementsFEM": w["elementsFEM"]}
+    Df = staqdic.funImgGradient(w["f"], ImgRefMask=w["maskf"], ctx=ctx, dtype=np.float32)
+    call = lambda: series.run_series(mesh, Df, w["f"], w["g_list"], w["U0_first"], w["winsize_list"],
+                                     precision="batched", ctx=ctx)
+    call()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    r = call()
+    ms = 1e3 * (time.perf_counter() - t)
+    P, N = len(w["g_list"]), int(w["coordinatesFEM"].shape[0])
+    nconv = sum(int(((c >= 1) & (c <= 100) & ~np.isnan(u[0::2])).sum()) for c, u in zip(r["conv"], r["U"]))
+    err = [float(np.nanmedian(np.abs(u - ut).reshape(-1, 2).max(1))) for u, ut in zip(r["U"], w["Utrue_list"])]
+    err0 = [float(np.nanmedian(np.abs(u - ut).reshape(-1, 2).max(1))) for u, ut in zip(r["U0"], w["Utrue_list"])]
+    from oracle import oracle as orc
+    from oracle import series as osr
+    t = time.perf_counter()
+    o = osr.run_series(mesh, w["f"], w["maskf"], w["g_list"], w["U0_first"], w["winsize_list"])
+    cpu_ms = 1e3 * (time.perf_counter() - t)
+    both = [((a >= 1) & (a <= 100) & (b >= 1) & (b <= 100) & ~np.isnan(x[0::2]) & ~np.isnan(y[0::2]))
+            for a, b, x, y in zip(r["conv"], o["conv"], r["U"], o["U"])]
+    dU = [np.abs(x - y).reshape(-1, 2).max(1)[m] for x, y, m in zip(r["U"], o["U"], both)]
+    return {"workload": "ramp1024: %d frames of 1024x1024, Kirsch field 0.2%%..%.0f%% strain, quadtree %d nodes"
+                        % (P, 0.2 * P, N),
+            "ms_per_sequence": ms, "ms_per_frame": ms / P, "converged_subsets": nconv,
+            "value": nconv / (ms * 1e-3), "unit": "converged subsets/s (host arrays, copies included)",
+            "median_err_vs_truth_px": err, "median_guess_err_vs_truth_px": err0,
+            "within_0_01px_of_oracle_frac": float(np.mean(np.concatenate(dU) <= 0.01)),
+            "cpu_oracle_ms": cpu_ms, "cpu_oracle_threads": orc.num_threads(),
+            "cpu_oracle": "oracle/series.py (the FP64 LocalICGNQuadtree restatement), one run"}
+
+
 def guarded(fn, *args):
     """One secondary measurement: its failure is reported in its own object and
     leaves the headline line intact."""
@@ -788,7 +830,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 1024^2 pass, the ADMM iterations, the adjoint and the multi-frame launch")
-    ap.add_argument("--only", choices=["c2", "admm", "adjoint", "c5", "mg", "c1"],
+    ap.add_argument("--only", choices=["c2", "admm", "adjoint", "c5", "mg", "c1", "series"],
                     help="run one secondary measurement alone and print it (for profiling)")
     ap.add_argument("--profile", choices=["batched", "plain"],
                     help="only the headline workload's passes of one form (warm-up + steps), for ncu captures")
@@ -831,6 +873,8 @@ def main():
             res = measure_mg(ctx, torch)
         elif args.only == "c1":
             res = measure_c1(ctx, torch)
+        elif args.only == "series":
+            res = measure_series(ctx, torch)
         else:
             res = measure_c5(ctx, torch, flush)
         print(json.dumps({"only": args.only, "result": res}), flush=True)
@@ -1000,6 +1044,7 @@ def main():
         out["c5"] = guarded(measure_c5, ctx, torch, flush)
         out["mg_search"] = guarded(measure_mg, ctx, torch)
         out["c1"] = guarded(measure_c1, ctx, torch)
+        out["series"] = guarded(measure_series, ctx, torch)
     print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -133,6 +133,52 @@ def bumps4096(seed=3, size=4096):
                  np.full(coords.shape[0], ws, np.int32), st, ufun, dict(winsize=ws))
 
 
+def ramp1024(seed=5, size=1024, frames=10, deps=0.002):
+    """A loading sequence: frame k (k = 1..frames) of the 1024^2 plate with a
+    hole under a Kirsch field at far-field strain k deps, all against one
+    reference image and one quadtree mesh.  Frame-to-frame increments stay
+    below about 1.5 px, the small steps the reference's sequence
+    initialisation (previous result, then a POD/GPR prediction) assumes."""
+    rng = np.random.default_rng(seed)
+    W = H = size
+    a = 150.0 * size / 1024
+    sp = synth.Speckles(W, H, _speckle_count(W, H), rng)
+    centre = ((W + 1) / 2, (H + 1) / 2)
+    xs, ys = synth.pixel_grid(W, H)
+    f = synth._render(sp, W, H, xs, ys, sp.cx, sp.cy) + rng.normal(0, 0.01, (W, H))
+    maskf = (np.hypot(xs - centre[0], ys - centre[1]) >= a).astype(np.uint8)
+    fN = np.asfortranarray((synth.normalize(f) * maskf).astype(np.float32))
+    s = size / 1024
+
+    def size_fn(x, y):
+        d = abs(math.hypot(x - centre[0], y - centre[1]) - a)
+        return 4.0 if d < 75 * s else (8.0 if d < 0.35 * W else (16.0 if d < 0.46 * W else 32.0))
+
+    def hole_fn(x, y):
+        return math.hypot(x - centre[0], y - centre[1]) < a
+
+    coords, elems, dirichlet, sizes = synth.quadtree_mesh(W, H, 64, 32, size_fn, 4.0, hole_fn)
+    hn = synth.node_sizes(coords, elems, sizes)
+    ws_list = np.clip(2 * hn, 8, 64).astype(np.int32)
+    inside = np.hypot(coords[:, 0] - centre[0], coords[:, 1] - centre[1]) < a
+    gs, Us, ufuns = [], [], []
+    for k in range(1, frames + 1):
+        ufun = synth.kirsch_field(a, deps * k, 0.3, centre)
+        _, g, X, Y = synth.render_pair(W, H, sp, ufun, noise=0.0, want_f=False)
+        g = g + rng.normal(0, 0.01, (W, H))
+        maskg = (np.hypot(X - centre[0], Y - centre[1]) >= a)
+        gs.append(np.asfortranarray((synth.normalize(g) * maskg).astype(np.float32)))
+        ux, uy = ufun(coords[:, 0], coords[:, 1])
+        U = np.stack([ux, uy], 1)
+        U[inside] = 0.0
+        Us.append(U.ravel())
+        ufuns.append(ufun)
+    d = _pack("ramp1024", fN, gs[0], maskf, None, coords, elems, dirichlet, Us[0], ws_list, 32, ufuns[0],
+              dict(hole_radius=a, centre=centre))
+    d.update(g_list=gs, Utrue_list=Us, U0_first=np.round(Us[0]), ufun_list=ufuns)
+    return d
+
+
 def series1024(seed=4, size=1024, pairs=16):
     """16 frame pairs sharing one reference image and one quadtree mesh."""
     rng = np.random.default_rng(seed)
@@ -173,4 +219,4 @@ def series1024(seed=4, size=1024, pairs=16):
 
 
 WORKLOADS = {"uniform256": uniform256, "hole1024": hole1024, "hole2048": hole2048,
-             "bumps4096": bumps4096, "series1024": series1024}
+             "bumps4096": bumps4096, "series1024": series1024, "ramp1024": ramp1024}

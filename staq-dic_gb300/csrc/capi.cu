@@ -30,6 +30,11 @@ struct stdic_ctx {
   double* scald = nullptr;  // device double scalars: [0] residual
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t es0 = nullptr, es1 = nullptr;  // around the last IC-GN solver kernel
+  // side stream for host copies that overlap kernels of the same call (the
+  // deformed frame's upload during the set-up stage, the Hessians' download
+  // during the iterations), with the events that order it against `stream`
+  cudaStream_t side = nullptr;
+  cudaEvent_t evs0 = nullptr, evs1 = nullptr, evh0 = nullptr, evh1 = nullptr;
   bool solver_timed = false;
   std::string err;
   long long launches = 0;
@@ -63,6 +68,18 @@ bool is_device_ptr(const void* p) {
   return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
+// host memory the CUDA driver has pinned (cudaHostAlloc, cudaHostRegister):
+// copies from and to it are asynchronous, so they can overlap kernels
+bool is_pinned_host_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
 size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // c->scal slot a kernel sets when a bounded wait for a TMA tile copy gave up
@@ -70,6 +87,18 @@ constexpr int kTmaErrSlot = 40;
 
 // Plans device placement for one call: device pointers pass through, host
 // buffers and scratch get regions of the context workspace.
+//
+// Host inputs are copied on the call's stream before its kernels, except
+// "late" ones (in_late), which the side stream copies while the first kernels
+// run; the call's stream waits for them (wait_late) before the first kernel
+// that reads them.  Host outputs are copied after the kernels, except those
+// handed to copy_early, which the side stream copies as soon as the kernels
+// that write them are done, while later kernels run.  Every side-stream copy
+// starts after the work the call's stream held when it was issued (so it never
+// touches workspace that an earlier call still uses) and is joined back into
+// the call's stream before finish() copies the rest, and in any case when the
+// plan goes out of scope, so the next call on the stream is ordered after it.
+// Under stream capture nothing goes to the side stream.
 struct Plan {
   struct Item {
     const void* host;
@@ -79,30 +108,93 @@ struct Plan {
     bool dev;
     int dir;  // 0 in, 1 out, 2 scratch
     void** slot;
+    bool late;   // input copied on the side stream (in_late)
+    bool early;  // output already copied on the side stream (copy_early)
   };
   std::vector<Item> items;
   size_t total = 0;
   bool any_host = false;
+  stdic_ctx* ctx = nullptr;
+  bool late_pending = false, early_pending = false;
+
+  Plan() = default;
+  Plan(const Plan&) = delete;
+  Plan& operator=(const Plan&) = delete;
+  ~Plan() { join(); }
 
   template <class T>
   void in(const T* p, size_t count, T** slot) {
-    Item it{p, nullptr, sizeof(T) * count, 0, is_device_ptr(p), 0, (void**)slot};
+    Item it{p, nullptr, sizeof(T) * count, 0, is_device_ptr(p), 0, (void**)slot, false, false};
     if (!p) { *slot = nullptr; return; }
     if (!it.dev) { it.off = total; total += al(it.bytes); any_host = true; }
     items.push_back(it);
   }
+  // pageable host memory is copied in order on the call's stream instead
+  template <class T>
+  void in_late(const T* p, size_t count, T** slot) {
+    in(p, count, slot);
+    if (p) items.back().late = !items.back().dev && is_pinned_host_ptr(p);
+  }
   template <class T>
   void out(T* p, size_t count, T** slot) {
-    Item it{nullptr, p, sizeof(T) * count, 0, is_device_ptr(p), 1, (void**)slot};
+    Item it{nullptr, p, sizeof(T) * count, 0, is_device_ptr(p), 1, (void**)slot, false, false};
     if (!p) { *slot = nullptr; return; }
     if (!it.dev) { it.off = total; total += al(it.bytes); any_host = true; }
     items.push_back(it);
   }
   template <class T>
   void scratch(size_t count, T** slot) {
-    Item it{nullptr, nullptr, sizeof(T) * count, total, false, 2, (void**)slot};
+    Item it{nullptr, nullptr, sizeof(T) * count, total, false, 2, (void**)slot, false, false};
     total += al(it.bytes);
     items.push_back(it);
+  }
+  bool copied_early(const void* const* slot) const {
+    for (auto& it : items)
+      if ((const void* const*)it.slot == slot) return it.early;
+    return false;
+  }
+  // true when the output bound to slot is a host buffer that finish() would copy
+  bool host_output(const void* const* slot) const {
+    for (auto& it : items)
+      if ((const void* const*)it.slot == slot) return it.dir == 1 && !it.dev;
+    return false;
+  }
+  // The call's stream waits for the late inputs (idempotent).
+  void wait_late() {
+    if (late_pending && ctx) cudaStreamWaitEvent(ctx->stream, ctx->evs1, 0);
+    late_pending = false;
+  }
+  // Copies the host output bound to slot now, on the side stream, after the
+  // work the call's stream holds so far; finish() skips it.  Returns false
+  // (nothing issued) when the output is not pinned host memory (a copy into
+  // pageable memory would block the host until the kernels before it are
+  // done) or under capture.
+  bool copy_early(const void* const* slot) {
+    if (!ctx || ctx->capturing || early_pending) return false;
+    for (auto& it : items) {
+      if ((const void* const*)it.slot != slot || it.dir != 1 || it.dev) continue;
+      if (!is_pinned_host_ptr(it.host_out)) return false;
+      if (cudaEventRecord(ctx->evh0, ctx->stream) != cudaSuccess ||
+          cudaStreamWaitEvent(ctx->side, ctx->evh0, 0) != cudaSuccess ||
+          cudaMemcpyAsync(it.host_out, *it.slot, it.bytes, cudaMemcpyDeviceToHost, ctx->side) != cudaSuccess ||
+          cudaEventRecord(ctx->evh1, ctx->side) != cudaSuccess) {
+        // nothing is left pending on the side stream that the call's stream
+        // could miss: wait for it whole, and copy the output in finish()
+        cudaGetLastError();
+        cudaStreamSynchronize(ctx->side);
+        return false;
+      }
+      it.early = true;
+      early_pending = true;
+      return true;
+    }
+    return false;
+  }
+  // Joins every side-stream copy into the call's stream.
+  void join() {
+    wait_late();
+    if (early_pending && ctx) cudaStreamWaitEvent(ctx->stream, ctx->evh1, 0);
+    early_pending = false;
   }
   // out-or-scratch: user buffer when given, else workspace
   template <class T>
@@ -127,28 +219,68 @@ struct Plan {
       }
       c->ws_size = want;
     }
+    ctx = c;
+    bool side_started = false;
     for (auto& it : items) {
       if (it.dir == 0 && it.dev) *it.slot = const_cast<void*>(it.host);
       else if (it.dir == 1 && it.dev) *it.slot = it.host_out;
       else *it.slot = (char*)c->ws + it.off;
       if (it.dir == 0 && !it.dev) {
-        cudaError_t e = cudaMemcpyAsync(*it.slot, it.host, it.bytes, cudaMemcpyHostToDevice, c->stream);
-        if (e != cudaSuccess) return cuda_fail(c, e, "host-to-device copy");
+        cudaStream_t s = c->stream;
+        if (it.late && !c->capturing) {
+          if (!side_started) {
+            cudaError_t e = cudaEventRecord(c->evs0, c->stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->evs0, 0);
+            if (e != cudaSuccess) return cuda_fail(c, e, "side stream");
+            side_started = true;
+            late_pending = true;
+          }
+          s = c->side;
+        }
+        cudaError_t e = cudaMemcpyAsync(*it.slot, it.host, it.bytes, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) {
+          if (side_started) {
+            // no event marks the end of the side copies: wait for them here
+            cudaStreamSynchronize(c->side);
+            late_pending = false;
+          }
+          return cuda_fail(c, e, "host-to-device copy");
+        }
+      }
+    }
+    if (side_started) {
+      cudaError_t e = cudaEventRecord(c->evs1, c->side);
+      if (e != cudaSuccess) {
+        cudaStreamSynchronize(c->side);
+        late_pending = false;
+        return cuda_fail(c, e, "side stream");
       }
     }
     return STDIC_OK;
   }
 
-  int finish(stdic_ctx* c) {
+  // Copies the host outputs and synchronises the stream when any buffer of
+  // the call is on the host.  A device int dev_int (a count the call
+  // produced) may ride along to a host int *dst_int in the same
+  // synchronisation; *delivered says whether it did.
+  int finish(stdic_ctx* c, const int* dev_int = nullptr, int* dst_int = nullptr, bool* delivered = nullptr) {
+    join();
+    if (delivered) *delivered = false;
     for (auto& it : items) {
-      if (it.dir == 1 && !it.dev) {
+      if (it.dir == 1 && !it.dev && !it.early) {
         cudaError_t e = cudaMemcpyAsync(it.host_out, *it.slot, it.bytes, cudaMemcpyDeviceToHost, c->stream);
         if (e != cudaSuccess) return cuda_fail(c, e, "device-to-host copy");
       }
     }
     if (any_host) {
       int terr = 0;
-      cudaError_t e = cudaMemcpyAsync(&terr, c->scal + kTmaErrSlot, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+      cudaError_t e = cudaSuccess;
+      if (dev_int && dst_int && delivered && !is_device_ptr(dst_int)) {
+        e = cudaMemcpyAsync(dst_int, dev_int, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "scalar read-back");
+        *delivered = true;
+      }
+      e = cudaMemcpyAsync(&terr, c->scal + kTmaErrSlot, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
       if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "stream synchronise");
       if (terr) {
@@ -211,6 +343,9 @@ int stdic_ctx_create(stdic_ctx** out, int device) {
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
   if (e == cudaSuccess) e = cudaEventCreate(&c->es0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->es1);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  for (cudaEvent_t* ev : {&c->evs0, &c->evs1, &c->evh0, &c->evh1})
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     cudaGetLastError();
     delete c;
@@ -233,6 +368,9 @@ int stdic_ctx_destroy(stdic_ctx* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->es0) cudaEventDestroy(c->es0);
   if (c->es1) cudaEventDestroy(c->es1);
+  for (cudaEvent_t ev : {c->evs0, c->evs1, c->evh0, c->evh1})
+    if (ev) cudaEventDestroy(ev);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return STDIC_OK;
@@ -402,12 +540,15 @@ struct FrameDev {
   const float *f32, *g32, *dfdx32, *dfdy32;
 };
 
+// late_g: a host deformed frame is uploaded on the side stream (Plan::in_late)
+// while the first kernels run; the caller waits for it before reading g.
 int stage_frame(stdic_ctx* c, Plan& pl, const stdic_frame* fr, FrameDev* d, bool want_f32,
-                int frames) {
+                int frames, bool late_g = false) {
   const size_t es = fr->dtype == STDIC_F64 ? 8 : 4;
   const size_t np = (size_t)fr->W * fr->H, ng = (size_t)(fr->W - 6) * (fr->H - 6);
   pl.in((const unsigned char*)fr->f, es * np, (unsigned char**)&d->f);
-  pl.in((const unsigned char*)fr->g, es * np * frames, (unsigned char**)&d->g);
+  if (late_g) pl.in_late((const unsigned char*)fr->g, es * np * frames, (unsigned char**)&d->g);
+  else pl.in((const unsigned char*)fr->g, es * np * frames, (unsigned char**)&d->g);
   pl.in((const unsigned char*)fr->dfdx, es * ng, (unsigned char**)&d->dfdx);
   pl.in((const unsigned char*)fr->dfdy, es * ng, (unsigned char**)&d->dfdy);
   pl.in(fr->mask, np, (uint8_t**)&d->mask);
@@ -523,8 +664,12 @@ struct QueueKeys {
   int ws_all;
 };
 
+// pl (optional): the call's plan; the iteration stage waits for its late
+// inputs, and early_slot names an output (the Hessians) that the set-up stage
+// completes and that the side stream copies to the host during the iterations
+// of the final launch.
 int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector<BatchedCand>& cands,
-                const QueueKeys& qk) {
+                const QueueKeys& qk, Plan* pl = nullptr, const void* const* early_slot = nullptr) {
   const bool two = b.two_dof != 0;
   if (cands.empty()) return fail(c, STDIC_E_UNSUPPORTED, "no launch shape fits this subset size");
   b.queue_head = c->scal + 4;  // [4] team phase, [5] single-warp phase
@@ -543,7 +688,7 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
       b.gbox_n = n == stdic::kGBoxes ? n : 0;
     }
   }
-  auto launch = [&](const BatchedCand& cd) -> int {
+  auto launch = [&](const BatchedCand& cd, bool final) -> int {
     b.warps_per_subset = cd.tw;
     b.smem_px = cd.smem_px;
     b.split = cd.split > 0 ? 1 : 0;
@@ -573,6 +718,9 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
       cudaError_t e = cudaMemsetAsync(b.queue_head, 0, 2 * sizeof(int), c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "queue reset");
       b.stage = stages[k];
+      // the deformed frame is read from the iteration stage on (the fused
+      // 2-DOF pass reads it throughout)
+      if (pl && b.stage != 1) pl->wait_late();
       rc = check_launch(c, stdic::launch_icgn_batched(b, b.stage == 1 ? cd.blocks1 : cd.blocks, cd.threads, c->stream),
                         "IC-GN batched");
       if (rc) return rc;
@@ -580,6 +728,7 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
         rc = check_launch(c, stdic::launch_factor6((const stdic::SubsetState6*)b.st6, b.H6, b.Hinv6, Ntot, c->stream),
                           "Hessian factorisation");
         if (rc) return rc;
+        if (final && pl && early_slot) pl->copy_early(early_slot);
 
       }
     }
@@ -592,7 +741,7 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
     // no timing inside a capture: the first shape (or the fixed one) for this
     // launch only, not cached, so the next uncaptured call still tunes
     const int pick = tune_pick();
-    return launch(cands[pick >= 0 ? std::min(pick, (int)cands.size() - 1) : 0]);
+    return launch(cands[pick >= 0 ? std::min(pick, (int)cands.size() - 1) : 0], true);
   }
   if (it == c->tune.end()) {
     int best = 0;
@@ -603,7 +752,7 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
       float bt = 1e30f;
       for (auto& cd : cands) {
         cudaEventRecord(c->ev0, c->stream);
-        const int rc = launch(cd);
+        const int rc = launch(cd, false);
         cudaEventRecord(c->ev1, c->stream);
         if (rc) return rc;
         cudaEventSynchronize(c->ev1);
@@ -618,9 +767,9 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
     it = c->tune.emplace(key, best).first;
   }
   const BatchedCand* chosen = &cands[std::min<size_t>((size_t)it->second, cands.size() - 1)];
-  if (c->capturing) return launch(*chosen);
+  if (c->capturing) return launch(*chosen, true);
   cudaEventRecord(c->es0, c->stream);
-  const int rc = launch(*chosen);
+  const int rc = launch(*chosen, true);
   cudaEventRecord(c->es1, c->stream);
   c->solver_timed = rc == STDIC_OK;
   return rc;
@@ -647,7 +796,9 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
   const bool batched = precision == STDIC_BATCHED_F32;
   Plan pl;
   FrameDev d;
-  stage_frame(c, pl, fr, &d, batched, frames);
+  // batched FP32 frames: g is first read by the iteration stage, so a host
+  // g is uploaded while the queue, set-up and factorisation kernels run
+  stage_frame(c, pl, fr, &d, batched, frames, batched && fr->dtype == STDIC_F32);
   stdic::IcgnArgs a{};
   pl.in(U0, 2 * NT, (double**)&a.U0);
   pl.in(coords, 2 * (size_t)N, (double**)&a.coords);
@@ -680,8 +831,10 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
   a.W = fr->W; a.H = fr->H; a.N = N;
   a.ws_all = winsize; a.ws_max = winsize; a.tol = tol;
   a.npx_max = npx_max;
+  bool early_h = false;  // HtempPar copied to the host during the iterations
   if (N > 0) {
     if (!batched) {
+      pl.wait_late();
       cudaEventRecord(c->es0, c->stream);
       int nk = 0;
       rc = check_launch(c, stdic::launch_icgn6_plain(a, order, c->scal + 64, c->scal + 12, c->stream, &nk),
@@ -699,7 +852,15 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
         b.g_stride = (long long)fr->W * fr->H;
         b.scratch = bscr;
         b.st6 = st6; b.H6 = H6; b.Hinv6 = Hinv6; b.order2 = order2;
-        rc = run_batched(c, b, (int)NT, cands, QueueKeys{a.ws_list, nullptr, winsize});
+        // host HtempPar with host result codes: the set-up stage writes every
+        // row the iterations keep, so the rows are copied to the host during
+        // the iterations; the iteration stage only zeroes the rows of the
+        // subsets it ends with a run-time error (code -1), which the host
+        // then zeroes in its copy from the codes
+        early_h = pl.host_output((const void* const*)&a.Hpk) && pl.host_output((const void* const*)&a.conv);
+        rc = run_batched(c, b, (int)NT, cands, QueueKeys{a.ws_list, nullptr, winsize}, &pl,
+                         early_h ? (const void* const*)&a.Hpk : nullptr);
+        early_h = early_h && pl.copied_early((const void* const*)&a.Hpk);
       }
     }
     if (rc) return rc;
@@ -710,9 +871,15 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
   } else if (filter) {
     cudaMemsetAsync(c->scal + 1, 0, sizeof(int), c->stream);
   }
-  rc = pl.finish(c);
+  bool delivered = false;
+  rc = pl.finish(c, filter ? c->scal + 1 : nullptr, filter ? badnum : nullptr, &delivered);
   if (rc) return rc;
-  return filter ? deliver_int(c, c->scal + 1, badnum) : STDIC_OK;
+  if (early_h) {
+    for (size_t k = 0; k < NT; ++k)
+      if (conv[k] == -1)
+        for (int q = 0; q < 21; ++q) Hpk[(size_t)q * NT + k] = 0.0;
+  }
+  return filter && !delivered ? deliver_int(c, c->scal + 1, badnum) : STDIC_OK;
 }
 
 int stdic_icgn_local(stdic_ctx* c, const stdic_frame* fr, const double* U0, const double* coords, int N,

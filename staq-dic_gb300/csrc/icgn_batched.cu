@@ -1095,8 +1095,13 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
                       : cubic32(fr.g, fr.W, fr.H, iu, su, iv, sv);
       };
       int p = tm.tl;
-      // two pixels per trip so that both pixels' taps are in flight together
-      for (; p + tm.TT < npx; p += 2 * tm.TT) {
+      // two pixels per trip so that both pixels' taps are in flight together.
+      // The trip count is the same on every lane (trips whose both pixels
+      // exist on the team's last thread); the rest, fewer than 2 TT pixels,
+      // is taken below as two single-pixel steps, so that a tile of
+      // 2 k TT + TT + 1 pixels (17^2 = 289 on one warp) does not run its
+      // last pair on one lane while the others wait to run their single one.
+      for (; p - tm.tl + 2 * tm.TT <= npx; p += 2 * tm.TT) {
         const int ia = it.i, ja = it.j;
         it.next();
         const int ib = it.i, jb = it.j;
@@ -1112,6 +1117,13 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
         const float dx = dx0 + (float)it.i, dy = dy0 + (float)it.j;
         const float t = sample(fu + p0 * dx + p2 * dy, fv0 + p1 * dx + p3 * dy);
         one(p, dx, dy, it.i, it.j, t);
+        p += tm.TT;
+        it.next();
+        if (p < npx) {
+          const float dxb = dx0 + (float)it.i, dyb = dy0 + (float)it.j;
+          const float tb = sample(fu + p0 * dxb + p2 * dyb, fv0 + p1 * dxb + p3 * dyb);
+          one(p, dxb, dyb, it.i, it.j, tb);
+        }
       }
       red[0] = (float)zg;
       red[1] = sg; red[2] = qg; red[3] = ng;

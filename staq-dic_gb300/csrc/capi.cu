@@ -40,6 +40,9 @@ struct stdic_ctx {
   long long launches = 0;
   // autotuner cache: (N bucket, npx_max, two_dof, frames) -> index of the launch shape
   std::map<std::tuple<int, int, int, int>, int> tune;
+  // resident CTAs per SM of a batched launch shape (tw, two_dof, threads,
+  // tile pixels, staged floats, stage), queried from the driver once
+  std::map<std::tuple<int, int, int, int, int, int>, int> occ;
   int tuning = 1;
   bool capturing = false;  // the stream is being captured into a CUDA graph
   long long wait_limit = 0;  // polls of a PCG grid-barrier wait (0: the default)
@@ -613,9 +616,17 @@ std::vector<BatchedCand> batched_candidates(stdic_ctx* c, bool two, int npx_max,
     int smem_px = (int)((per_warp * tw - 512 - 32 * 4 * tw) / bpp);
     smem_px = std::max(64, std::min(smem_px, npx_max));
     const int gtile = gt_warp * tw;
-    const int per_sm = stdic::batched_blocks_per_sm(tw, two, threads, smem_px, gtile, 2);
+    auto occupancy = [&](int stage) {
+      const auto key = std::make_tuple(tw, (int)two, threads, smem_px, gtile, stage);
+      auto hit = c->occ.find(key);
+      if (hit != c->occ.end()) return hit->second;
+      const int n = stdic::batched_blocks_per_sm(tw, two, threads, smem_px, gtile, stage);
+      c->occ.emplace(key, n);
+      return n;
+    };
+    const int per_sm = occupancy(2);
     if (per_sm <= 0) continue;
-    const int per_sm1 = two ? per_sm : std::max(per_sm, stdic::batched_blocks_per_sm(tw, two, threads, smem_px, gtile, 1));
+    const int per_sm1 = two ? per_sm : std::max(per_sm, occupancy(1));
     const int units_per_block = split ? threads / 32 : teams_per_block;
     const int max_blocks = (Ntot + units_per_block - 1) / units_per_block;
     const int blocks = std::max(1, std::min(c->nsm * per_sm, max_blocks));

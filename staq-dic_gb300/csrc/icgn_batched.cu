@@ -462,23 +462,35 @@ STDIC_DEV void split_f64(double v, float& hi, float& lo) {
 }
 
 // sum_q (hh_q + hl_q) * x_q in double-float arithmetic, rounded once to FP32:
-// each product is split exactly by an FMA and the running sum is kept as an
-// error-free (TwoSum) pair, so the result matches an FP64 dot product of the
-// same operands rounded to FP32, without using the FP64 pipe.
+// each product is split exactly by an FMA into p_q + e_q, and the p_q are
+// added pairwise (a tree of depth log2 K) by error-free TwoSums whose errors
+// join the e_q, so the result matches an FP64 dot product of the same operands
+// rounded to FP32, without using the FP64 pipe.  The tree keeps the chain of
+// dependent operations short: this sits on the serial path of every iteration.
+STDIC_DEV void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
 template <int K>
 STDIC_DEV float dot_df(const float* hh, const float* hl, const float* x) {
-  float S = 0.f, E = 0.f;
+  float p[K], e[K];
 #pragma unroll
   for (int q = 0; q < K; ++q) {
-    const float p = __fmul_rn(hh[q], x[q]);
-    const float e = fmaf(hl[q], x[q], fmaf(hh[q], x[q], -p));
-    const float t = __fadd_rn(S, p);
-    const float bp = __fsub_rn(t, S);
-    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(t, bp)), __fsub_rn(p, bp));
-    E = __fadd_rn(E, __fadd_rn(err, e));
-    S = t;
+    p[q] = __fmul_rn(hh[q], x[q]);
+    e[q] = fmaf(hl[q], x[q], fmaf(hh[q], x[q], -p[q]));
   }
-  return __fadd_rn(S, E);
+#pragma unroll
+  for (int w = 1; w < K; w *= 2) {
+#pragma unroll
+    for (int q = 0; q + w < K; q += 2 * w) {
+      float t, err;
+      two_sum(p[q], p[q + w], t, err);
+      p[q] = t;
+      e[q] = __fadd_rn(__fadd_rn(e[q], e[q + w]), err);
+    }
+  }
+  return __fadd_rn(p[0], e[0]);
 }
 
 // kg += J t for the 6-DOF steepest-descent images J = [dx gx, dx gy, dy gx,
@@ -659,7 +671,16 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
   bool decided = false;  // outputs of this subset already written by the set-up stage
   const double npx0 = (double)(wx + 1) * (double)(wy + 1);
 
+  // 6-DOF iterations: the subset's inverse Hessian pairs and f-side sums are
+  // loaded here, with its state, and written to the control block after the
+  // tile set-up, so that their latency overlaps the state's
+  float2 hpre = make_float2(0.f, 0.f), hpre2 = make_float2(0.f, 0.f);
+  float jpre = 0.f;
   if (stage == 2) {
+    const float2* hp = reinterpret_cast<const float2*>(B.Hinv6) + (size_t)item * 36;
+    if (tm.tl < 36) hpre = hp[tm.tl];
+    if (tm.tl + tm.TT < 36) hpre2 = hp[tm.tl + tm.TT];
+    if (tm.tl < 12) jpre = tm.tl < 6 ? st6[item].Jf[tm.tl] : st6[item].J1[tm.tl - 6];
     const SubsetState6 s6 = st6[item];
     if (s6.code != 0) {
       decided = true;
@@ -677,6 +698,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     if (crop_valid) {
       const int mx0 = wx + 1, np0 = (wx + 1) * (wy + 1);
       PixIter it(tm.tl, tm.TT, mx0);
+      #pragma unroll 4
       for (int p = tm.tl; p < np0; p += tm.TT, it.next()) {
         const float t = fr.F(x1 + it.i, y1 + it.j) * fr.M(x1 + it.i, y1 + it.j);
         if (t != t) nanf = 1;
@@ -737,6 +759,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     if (stage != 2 || has_masked) {
       int z = 0;
       PixIter it(pstart, mx);
+      #pragma unroll 4
       for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
         const uint8_t mk = __ldg(fr.mask + (y1 + it.j - 1) * fr.W + (x1 + it.i - 1)) != 0;
         mtile[p] = mk;
@@ -755,6 +778,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     // only: each thread caches the masked gradients of its own pixels
     if (stage == 2 && !decided && code == 0 && !nan_out) {
       PixIter it(pstart, mx);
+      #pragma unroll 4
       for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
         const float s = bw ? (float)bw[p] : 1.f;
         gq[p] = make_float2(fr.GX(x1 + it.i, y1 + it.j) * s, fr.GY(x1 + it.i, y1 + it.j) * s);
@@ -796,6 +820,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     for (int k = 0; k < 21; ++k) hs[k] = 0.f;
     float sf = 0.f, nf = 0.f, sa = 0.f;
     PixIter it(pstart, mx);
+    #pragma unroll 2
     for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
       const int i = it.i, j = it.j;
       const float s = bw ? (float)bw[p] : 1.f;
@@ -924,14 +949,12 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     return;
   }
   if constexpr (!TWO) {
-    // the subset's inverse Hessian and f-side sums, once, into the team's control block
-    const float2* hp = reinterpret_cast<const float2*>(B.Hinv6) + (size_t)item * 36;
-    for (int k = tm.tl; k < 36; k += tm.TT) {
-      const float2 h = hp[k];
-      ctl->hh[k] = h.x;
-      ctl->hl[k] = h.y;
-    }
-    if (tm.tl < 6) { ctl->jf[tm.tl] = st6[item].Jf[tm.tl]; ctl->j1[tm.tl] = st6[item].J1[tm.tl]; }
+    // the subset's inverse Hessian and f-side sums (loaded with its state),
+    // once, into the team's control block
+    if (tm.tl < 36) { ctl->hh[tm.tl] = hpre.x; ctl->hl[tm.tl] = hpre.y; }
+    if (tm.tl + tm.TT < 36) { ctl->hh[tm.tl + tm.TT] = hpre2.x; ctl->hl[tm.tl + tm.TT] = hpre2.y; }
+    if (tm.tl < 6) ctl->jf[tm.tl] = jpre;
+    else if (tm.tl < 12) ctl->j1[tm.tl - 6] = jpre;
     tm.sync();
   }
   const bool run = (code == 0 && !nan_out);

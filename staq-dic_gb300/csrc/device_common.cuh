@@ -371,6 +371,59 @@ STDIC_DEV void small_solve(const double* Ain, const double* b, int n, double* x)
   }
 }
 
+// small_solve's Cholesky branch for n = 6 split in two, for a matrix that
+// stays fixed while right-hand sides change: chol6_factor forms L (row-major,
+// the same operations in the same order as small_solve) and returns false
+// where small_solve would take its LU branch; chol6_solve then gives, for
+// each b, the x small_solve gives.  With n fixed the arrays live in registers.
+STDIC_DEV bool chol6_factor(const double* A, double* L) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+    if (!(A[i * 6 + i] > 0)) return false;
+  double l[36];
+#pragma unroll
+  for (int k = 0; k < 36; ++k) l[k] = 0;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    double d = A[j * 6 + j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) d -= l[j * 6 + k] * l[j * 6 + k];
+    if (!(d > 0)) return false;
+    const double ljj = sqrt(d);
+    l[j * 6 + j] = ljj;
+#pragma unroll
+    for (int i = j + 1; i < 6; ++i) {
+      double s = A[i * 6 + j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) s -= l[i * 6 + k] * l[j * 6 + k];
+      l[i * 6 + j] = s / ljj;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 36; ++k) L[k] = l[k];
+  return true;
+}
+
+STDIC_DEV void chol6_solve(const double* L, const double* b, double* x) {
+  double y[6], z[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double s = b[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) s -= L[i * 6 + k] * y[k];
+    y[i] = s / L[i * 6 + i];
+  }
+#pragma unroll
+  for (int i = 5; i >= 0; --i) {
+    double s = y[i];
+#pragma unroll
+    for (int k = i + 1; k < 6; ++k) s -= L[k * 6 + i] * z[k];
+    z[i] = s / L[i * 6 + i];
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) x[i] = z[i];
+}
+
 // x = A \ b for a symmetric 2x2 A = [a11 a12; a12 a22] in registers, with the
 // branch structure of small_solve (Cholesky when it succeeds, else LU with
 // partial pivoting).

@@ -71,6 +71,27 @@ STDIC_DEV void masked_stats(const double* t, int npx, double* scratch, double* m
 // Any warped tile pixel outside [3, W-2] x [3, H-2] (funICGNQuadtree.m:154)
 STDIC_DEV bool any_oob(const Frame64& fr, const double P[6], long long x0, long long y0,
                        long long x1, long long y1, int mx, int my) {
+  // The warp is affine, so every pixel lies in the hull of the four corner
+  // pixels; rounding moves a position by about 1e-12 px at these image
+  // sizes.  Threads 0-3 evaluate one corner each, with the same operations as
+  // the per-pixel test: a corner outside is a pixel outside (the answer), and
+  // corners inside by more than 1e-6 px put every pixel inside.  Only a
+  // corner within 1e-6 px of the border takes the test of every pixel.
+  {
+    int out = 0, near = 0;
+    if (threadIdx.x < 4) {
+      const int i = (threadIdx.x & 1) ? mx - 1 : 0, j = (threadIdx.x & 2) ? my - 1 : 0;
+      double u22, v22;
+      warp_exact(P, (double)(x1 + i - x0), (double)(y1 + j - y0), (double)x0, (double)y0, &u22, &v22);
+      const double xl = 3, xh = (double)fr.W - 2, yl = 3, yh = (double)fr.H - 2;
+      if (u22 < xl || u22 > xh || v22 < yl || v22 > yh) out = 1;
+      else if (!(u22 >= xl + 1e-6 && u22 <= xh - 1e-6 && v22 >= yl + 1e-6 && v22 <= yh - 1e-6)) near = 1;
+    }
+    // (__syncthreads_or returns whether any thread's value is nonzero, not
+    // their bitwise or: one barrier per question)
+    if (__syncthreads_or(out)) return true;
+    if (!__syncthreads_or(near)) return false;
+  }
   int bad = 0;
   const int npx = mx * my;
   for (int p = threadIdx.x; p < npx; p += blockDim.x) {
@@ -85,6 +106,8 @@ STDIC_DEV bool any_oob(const Frame64& fr, const double P[6], long long x0, long 
 struct Shared {
   double P[6];
   double Hm[36];
+  double L[36];  // 6-DOF: Cholesky factor of Hm (when hm_spd)
+  int hm_spd;
   double red[32 * 21];
   int ired[32];
   int flag;
@@ -94,18 +117,52 @@ struct Shared {
 
 }  // namespace
 
+// 6-DOF: per-pixel terms of the iterations that stay fixed over a subset,
+// kept in shared memory when the class's tiles leave room for them.  The
+// values are those the iterations would otherwise recompute, with the same
+// operations, so the results do not change.
+struct PlainCache {
+  int rf;  // (tempf - meanf) / bottomf per pixel (one FP64 division per pixel less per iteration)
+  int jg;  // masked gradients gx s, gy s per pixel, and the tile's dx, dy offsets per column and row
+};
+
+// Largest tile side of a class (its tiles are square, side^2 <= npx_cap).
+__host__ __device__ inline int plain_side_cap(int npx_cap) {
+  int m = 1;
+  while ((m + 1) * (m + 1) <= npx_cap) ++m;
+  return m;
+}
+
+// Dynamic shared memory of the 6-DOF kernel: tempg, [rf], [gx s, gy s],
+// [dx, dy offsets] (doubles), then four npx_cap-byte bitmaps.
+__host__ __device__ inline size_t plain6_smem_bytes(int npx_cap, PlainCache c) {
+  const size_t d = (size_t)npx_cap * (1 + (c.rf ? 1 : 0) + (c.jg ? 2 : 0)) +
+                   (c.jg ? 2 * (size_t)plain_side_cap(npx_cap) : 0);
+  return d * sizeof(double) + 4 * (size_t)npx_cap;
+}
+
 // ---------------------------------------------------------------------------
-// 6-DOF first pass.  Dynamic shared memory: npx_cap doubles (tempg) + 4
-// npx_cap bytes (mask tile, bw_f, bw_g, scratch bitmap).
+// 6-DOF first pass.  Dynamic shared memory: npx_cap doubles (tempg), the
+// cached terms of PlainCache, then 4 npx_cap bytes (mask tile, bw_f, bw_g,
+// scratch bitmap).
 // ---------------------------------------------------------------------------
 // One node on the whole CTA; npx_cap is the tile capacity of the CTA's
 // dynamic shared memory (the grown tile of the largest subset of its class).
 __device__ void plain6_node(const IcgnArgs& a, const int node, unsigned char* dsm, Shared& sh,
-                            const int npx_cap) {
+                            const int npx_cap, const PlainCache cc) {
   Frame64 fr{(const double*)a.f, (const double*)a.g, a.mask, (const double*)a.dfdx,
              (const double*)a.dfdy, a.W, a.H};
   double* tg = (double*)dsm;
-  uint8_t* mtile = (uint8_t*)(tg + npx_cap);
+  double* dp = tg + npx_cap;
+  double* rf = nullptr;
+  double *gxs = nullptr, *gys = nullptr, *dxl = nullptr, *dyl = nullptr;
+  if (cc.rf) { rf = dp; dp += npx_cap; }
+  if (cc.jg) {
+    const int mc = plain_side_cap(npx_cap);
+    gxs = dp; gys = dp + npx_cap; dxl = gys + npx_cap; dyl = dxl + mc;
+    dp = dyl + mc;
+  }
+  uint8_t* mtile = (uint8_t*)dp;
   uint8_t* bwf = mtile + npx_cap;
   uint8_t* bwg = bwf + npx_cap;
   uint8_t* tmp = bwg + npx_cap;
@@ -183,6 +240,11 @@ __device__ void plain6_node(const IcgnArgs& a, const int node, unsigned char* ds
     for (int p = threadIdx.x; p < npx; p += blockDim.x) bwf[p] = 1;
     __syncthreads();
   }
+  if (cc.jg)
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+      dxl[k] = (double)(x1 + k - x0);
+      dyl[k] = (double)(y1 + k - y0);
+    }
   // tempf (masked) is staged in tg for the statistics, then regenerated on the fly
   {
     double h[21];
@@ -192,6 +254,7 @@ __device__ void plain6_node(const IcgnArgs& a, const int node, unsigned char* ds
       const int i = p % m, j = p / m;
       const double s = (double)bwf[p];
       const double gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
+      if (cc.jg) { gxs[p] = gx; gys[p] = gy; }
       tg[p] = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
       const double dx = (double)(x1 + i - x0), dy = (double)(y1 + j - y0);
       const double J[6] = {dx * gx, dx * gy, dy * gx, dy * gy, gx, gy};
@@ -206,6 +269,9 @@ __device__ void plain6_node(const IcgnArgs& a, const int node, unsigned char* ds
       int q = 0;
       for (int aa = 0; aa < 6; ++aa)
         for (int bb = aa; bb < 6; ++bb) { sh.Hm[aa * 6 + bb] = h[q]; sh.Hm[bb * 6 + aa] = h[q]; ++q; }
+      // H is fixed over the iterations: its Cholesky factor is formed once
+      // (mldivide's factorisation of the same matrix on every iteration)
+      sh.hm_spd = chol6_factor(sh.Hm, sh.L) ? 1 : 0;
     }
   }
   double meanf, bottomf;
@@ -213,7 +279,11 @@ __device__ void plain6_node(const IcgnArgs& a, const int node, unsigned char* ds
   double sabs;
   {
     double v[1] = {0};
-    for (int p = threadIdx.x; p < npx; p += blockDim.x) v[0] += fabs(tg[p]);
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+      v[0] += fabs(tg[p]);
+      // each thread keeps the f side of its own pixels' residuals
+      if (cc.rf) rf[p] = (tg[p] - meanf) / bottomf;
+    }
     block_sum<1>(v, sh.red);
     sabs = v[0];
   }
@@ -241,7 +311,9 @@ __device__ void plain6_node(const IcgnArgs& a, const int node, unsigned char* ds
     for (int p = threadIdx.x; p < npx; p += blockDim.x) {
       const int i = p % m, j = p / m;
       double u22, v22;
-      warp_exact(P, (double)(x1 + i - x0), (double)(y1 + j - y0), (double)x0, (double)y0, &u22, &v22);
+      const double dxp = cc.jg ? dxl[i] : (double)(x1 + i - x0);
+      const double dyp = cc.jg ? dyl[j] : (double)(y1 + j - y0);
+      warp_exact(P, dxp, dyp, (double)x0, (double)y0, &u22, &v22);
       const double t = ba_cubic_exact(fr.g, fr.W, fr.H, v22, u22);
       tg[p] = t;
       if (t != t) nang = 1;
@@ -268,11 +340,21 @@ __device__ void plain6_node(const IcgnArgs& a, const int node, unsigned char* ds
     double b2[6] = {0, 0, 0, 0, 0, 0};
     for (int p = threadIdx.x; p < npx; p += blockDim.x) {
       const int i = p % m, j = p / m;
-      const double s = (double)bwf[p];
-      const double gx = fr.GX(x1 + i, y1 + j) * s, gy = fr.GY(x1 + i, y1 + j) * s;
-      const double fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
-      const double dx = (double)(x1 + i - x0), dy = (double)(y1 + j - y0);
-      const double r = (fv - meanf) / bottomf - (tg[p] - meang) / bottomg;
+      double gx, gy, dx, dy, rfp;
+      if (cc.jg) {
+        gx = gxs[p]; gy = gys[p]; dx = dxl[i]; dy = dyl[j];
+      } else {
+        const double s = (double)bwf[p];
+        gx = fr.GX(x1 + i, y1 + j) * s; gy = fr.GY(x1 + i, y1 + j) * s;
+        dx = (double)(x1 + i - x0); dy = (double)(y1 + j - y0);
+      }
+      if (cc.rf) {
+        rfp = rf[p];
+      } else {
+        const double fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * (double)bwf[p];
+        rfp = (fv - meanf) / bottomf;
+      }
+      const double r = rfp - (tg[p] - meang) / bottomg;
       b2[0] += dx * gx * r;
       b2[1] += dx * gy * r;
       b2[2] += dy * gx * r;
@@ -295,7 +377,8 @@ __device__ void plain6_node(const IcgnArgs& a, const int node, unsigned char* ds
       if (nN < tol || nA < tol) done = 1;
       else {
         double D[6];
-        small_solve(sh.Hm, b, 6, D);
+        if (sh.hm_spd) chol6_solve(sh.L, b, D);
+        else small_solve(sh.Hm, b, 6, D);
         for (int k = 0; k < 6; ++k) D[k] = -D[k];
         double Pn[6];
         for (int k = 0; k < 6; ++k) Pn[k] = P[k];
@@ -531,6 +614,7 @@ struct PlainClass {
   const int32_t* order;  // node order (sorted by size); nullptr: nodes 0..N-1
   const int* range;      // [lo, hi) of this class in order; nullptr: [0, N)
   int npx_cap;           // tile capacity of the CTA's shared memory
+  PlainCache cache;      // 6-DOF: per-pixel terms kept in shared memory
 };
 
 template <int T, bool TWO>
@@ -541,7 +625,7 @@ __global__ void __launch_bounds__(T) icgn_plain_class_kernel(IcgnArgs a, PlainCl
   for (int q = lo + blockIdx.x; q < hi; q += gridDim.x) {
     const int node = cl.order ? cl.order[q] : q;
     if constexpr (TWO) plain2_node(a, node, dsm, sh, cl.npx_cap);
-    else plain6_node(a, node, dsm, sh, cl.npx_cap);
+    else plain6_node(a, node, dsm, sh, cl.npx_cap, cl.cache);
     __syncthreads();  // thread 0's output writes read sh before the next node reuses it
   }
 }
@@ -566,8 +650,21 @@ __global__ void plain_class_ranges_kernel(const int* __restrict__ hist, int* ran
 }
 
 template <int T, bool TWO>
-cudaError_t launch_class(const IcgnArgs& a, const PlainClass& cl, int nodes_hint, cudaStream_t s) {
-  const size_t smem = (size_t)cl.npx_cap * (TWO ? 2 * sizeof(double) + 4 : sizeof(double) + 4);
+cudaError_t launch_class(const IcgnArgs& a, PlainClass cl, int nodes_hint, cudaStream_t s) {
+  size_t smem;
+  if (TWO) {
+    cl.cache = PlainCache{0, 0};
+    smem = (size_t)cl.npx_cap * (2 * sizeof(double) + 4);
+  } else {
+    // the 6-DOF kernel keeps as many of its fixed per-pixel terms in shared
+    // memory as 200 KB of it allows (every class but the largest tiles'
+    // keeps both; the occupancy of these classes is set by registers)
+    constexpr size_t kLimit = 200 * 1024;
+    cl.cache = PlainCache{1, 1};
+    if (plain6_smem_bytes(cl.npx_cap, cl.cache) > kLimit) cl.cache.jg = 0;
+    if (plain6_smem_bytes(cl.npx_cap, cl.cache) > kLimit) cl.cache.rf = 0;
+    smem = plain6_smem_bytes(cl.npx_cap, cl.cache);
+  }
   cudaError_t e = cudaFuncSetAttribute(icgn_plain_class_kernel<T, TWO>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

@@ -24,7 +24,7 @@ struct stdic_ctx {
   size_t ws_size = 0;
   int* scal = nullptr;  // device scalars: [1] badnum, [2] iters, [3] status, [4..5] queue heads, [6] queue split,
                         // [7] adjoint queue head, [8..9] iteration-list counts,
-                        // [10] gradient tile-copy time-out flag, [12..19] plain IC-GN size-class ranges,
+                        // [10] gradient tile-copy time-out flag, [12..23] plain IC-GN size-class ranges and work counters,
                         // [24..33] bad-point code statistics (5 x int64),
                         // [64..575] work-queue histogram and bin cursors
   double* scald = nullptr;  // device double scalars: [0] residual

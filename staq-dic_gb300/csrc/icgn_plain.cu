@@ -614,6 +614,7 @@ struct PlainClass {
   const int32_t* order;  // node order (sorted by size); nullptr: nodes 0..N-1
   const int* range;      // [lo, hi) of this class in order; nullptr: [0, N)
   int npx_cap;           // tile capacity of the CTA's shared memory
+  int* head;             // work counter of the class (zero at launch)
   PlainCache cache;      // 6-DOF: per-pixel terms kept in shared memory
 };
 
@@ -622,7 +623,15 @@ __global__ void __launch_bounds__(T) icgn_plain_class_kernel(IcgnArgs a, PlainCl
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ Shared sh;
   const int lo = cl.range ? cl.range[0] : 0, hi = cl.range ? cl.range[1] : a.N;
-  for (int q = lo + blockIdx.x; q < hi; q += gridDim.x) {
+  // CTAs pull nodes from the class's counter: iteration counts vary by two
+  // orders of magnitude, and a fixed stride left some SMs working twice as
+  // long as the mean
+  __shared__ int s_q;
+  for (;;) {
+    if (threadIdx.x == 0) s_q = lo + atomicAdd(cl.head, 1);
+    __syncthreads();
+    const int q = s_q;
+    if (q >= hi) break;
     const int node = cl.order ? cl.order[q] : q;
     if constexpr (TWO) plain2_node(a, node, dsm, sh, cl.npx_cap);
     else plain6_node(a, node, dsm, sh, cl.npx_cap, cl.cache);
@@ -634,7 +643,7 @@ __global__ void __launch_bounds__(T) icgn_plain_class_kernel(IcgnArgs a, PlainCl
 // takes everything larger.
 constexpr int kClasses = 4;
 constexpr int kClassEdge[kClasses] = {8, 16, 32, 255};
-constexpr int kClassThreads[kClasses] = {64, 128, 256, 256};
+constexpr int kClassThreads[kClasses] = {32, 64, 128, 256};
 
 // Queue positions of each class from the histogram of subset edges of an
 // ascending queue (bin b = edge b).
@@ -643,6 +652,7 @@ __global__ void plain_class_ranges_kernel(const int* __restrict__ hist, int* ran
   const int e[kClasses] = {edges.x, edges.y, edges.z, edges.w};
   int pos = 0, b = 0;
   for (int k = 0; k < kClasses; ++k) {
+    ranges[2 * kClasses + k] = 0;  // the class's work counter
     ranges[2 * k] = pos;
     for (; b <= e[k]; ++b) pos += hist[b];
     ranges[2 * k + 1] = pos;
@@ -696,10 +706,13 @@ cudaError_t launch_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* 
   if (!per_node) {
     // one subset size: one class
     const int ws = a.ws_all;
-    PlainClass cl{nullptr, nullptr, a.npx_max};
+    PlainClass cl{nullptr, nullptr, a.npx_max, ranges + 2 * kClasses};
+    cudaError_t e = cudaMemsetAsync(cl.head, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
     *kernels = 1;
-    if (ws <= 8) return launch_class<64, TWO>(a, cl, a.N, s);
-    if (ws <= 16) return launch_class<128, TWO>(a, cl, a.N, s);
+    if (ws <= 8) return launch_class<32, TWO>(a, cl, a.N, s);
+    if (ws <= 16) return launch_class<64, TWO>(a, cl, a.N, s);
+    if (ws <= 32) return launch_class<128, TWO>(a, cl, a.N, s);
     return launch_class<256, TWO>(a, cl, a.N, s);
   }
   cudaError_t e = launch_build_queue(TWO ? nullptr : a.ws_list, TWO ? a.wsl2 : nullptr, a.ws_all, a.N, order,
@@ -712,8 +725,10 @@ cudaError_t launch_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* 
   *kernels = 4;
   for (int k = 0; k < kClasses && e == cudaSuccess; ++k) {
     PlainClass cl{order, ranges + 2 * k, k + 1 < kClasses ? std::min(grown_tile_pixels(kClassEdge[k]), a.npx_max)
-                                                           : a.npx_max};
+                                                           : a.npx_max,
+                  ranges + 2 * kClasses + k};
     switch (kClassThreads[k]) {
+      case 32: e = launch_class<32, TWO>(a, cl, a.N, s); break;
       case 64: e = launch_class<64, TWO>(a, cl, a.N, s); break;
       case 128: e = launch_class<128, TWO>(a, cl, a.N, s); break;
       default: e = launch_class<256, TWO>(a, cl, a.N, s); break;

@@ -141,7 +141,7 @@ cudaError_t launch_intsearch(const double* f, const double* g, int W, int H, int
                              int32_t* peak, cudaStream_t s);
 // Plain FP64 IC-GN, one CTA per node, in subset-size classes (CTA size and
 // shared memory per class).  order: N device ints; qscratch: 512 device ints
-// (the queue histogram and cursors); ranges: 8 device ints (class ranges).
+// (the queue histogram and cursors); ranges: 12 device ints (class ranges, then one work counter per class).
 // *kernels receives the number of kernels launched.
 // cc.qfactors of the integer search: PCE and PPE of each grid point's full
 // normxcorr2 map, normalised over the points; qf is npt x 2 (column-major),

@@ -1513,7 +1513,7 @@ __device__ __noinline__ void lu_inverse6(const double* __restrict__ H, double* _
     for (int c2 = 0; c2 < 6; ++c2) out[r * 6 + c2] = A[r][6 + c2];
 }
 
-__global__ void __launch_bounds__(128) factor6_kernel(const SubsetState6* __restrict__ st,
+__global__ void __launch_bounds__(64) factor6_kernel(const SubsetState6* __restrict__ st,
                                                       const double* __restrict__ H6,
                                                       double* __restrict__ Hinv6, int n) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1550,15 +1550,18 @@ __global__ void __launch_bounds__(128) factor6_kernel(const SubsetState6* __rest
   // instructions, which GB300 issues slowly, so it is done once here rather
   // than by every team that takes the subset
   float2* outp = reinterpret_cast<float2*>(Hinv6) + (size_t)t * 36;
-  double out[36];
   if (!ok) {
-    lu_inverse6(H6 + (size_t)t * 21, out);
+    // the rare LU path has its own array, so that the Cholesky path's
+    // result (out below) is never addressed and stays in registers
+    double lu[36];
+    lu_inverse6(H6 + (size_t)t * 21, lu);
     for (int k = 0; k < 36; ++k) {
-      const float hi = (float)out[k];
-      outp[k] = make_float2(hi, (float)(out[k] - (double)hi));
+      const float hi = (float)lu[k];
+      outp[k] = make_float2(hi, (float)(lu[k] - (double)hi));
     }
     return;
   }
+  double out[36];
   // M = L^-1 (lower, packed), then H^-1 = M^T M
   double m[21];
 #pragma unroll
@@ -1594,7 +1597,9 @@ __global__ void __launch_bounds__(128) factor6_kernel(const SubsetState6* __rest
 cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hinv6, int n,
                            cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  factor6_kernel<<<(n + 127) / 128, 128, 0, s>>>(st, H6, Hinv6, n);
+  // 64-thread blocks: four times as many blocks as SMs even for ~20k
+  // subsets, so that the FP64-bound work spreads evenly
+  factor6_kernel<<<(n + 63) / 64, 64, 0, s>>>(st, H6, Hinv6, n);
   return cudaGetLastError();
 }
 

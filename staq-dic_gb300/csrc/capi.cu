@@ -35,6 +35,8 @@ struct stdic_ctx {
   // during the iterations), with the events that order it against `stream`
   cudaStream_t side = nullptr;
   cudaEvent_t evs0 = nullptr, evs1 = nullptr, evh0 = nullptr, evh1 = nullptr;
+  // streams and events on which the plain IC-GN size classes run concurrently
+  stdic::PlainStreams plain{};
   bool solver_timed = false;
   std::string err;
   long long launches = 0;
@@ -347,8 +349,11 @@ int stdic_ctx_create(stdic_ctx** out, int device) {
   if (e == cudaSuccess) e = cudaEventCreate(&c->es0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->es1);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
-  for (cudaEvent_t* ev : {&c->evs0, &c->evs1, &c->evh0, &c->evh1})
+  for (cudaEvent_t* ev : {&c->evs0, &c->evs1, &c->evh0, &c->evh1, &c->plain.fork, &c->plain.join[0],
+                          &c->plain.join[1], &c->plain.join[2]})
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  for (cudaStream_t* st : {&c->plain.side[0], &c->plain.side[1], &c->plain.side[2]})
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     cudaGetLastError();
     delete c;
@@ -371,9 +376,12 @@ int stdic_ctx_destroy(stdic_ctx* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->es0) cudaEventDestroy(c->es0);
   if (c->es1) cudaEventDestroy(c->es1);
-  for (cudaEvent_t ev : {c->evs0, c->evs1, c->evh0, c->evh1})
+  for (cudaEvent_t ev : {c->evs0, c->evs1, c->evh0, c->evh1, c->plain.fork, c->plain.join[0], c->plain.join[1],
+                         c->plain.join[2]})
     if (ev) cudaEventDestroy(ev);
   if (c->side) cudaStreamDestroy(c->side);
+  for (cudaStream_t st : {c->plain.side[0], c->plain.side[1], c->plain.side[2]})
+    if (st) cudaStreamDestroy(st);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return STDIC_OK;
@@ -736,7 +744,8 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
                         "IC-GN batched");
       if (rc) return rc;
       if (!two && k == 0) {
-        rc = check_launch(c, stdic::launch_factor6((const stdic::SubsetState6*)b.st6, b.H6, b.Hinv6, Ntot, c->stream),
+        rc = check_launch(c, stdic::launch_factor6((const stdic::SubsetState6*)b.st6, b.H6, b.Hinv6, Ntot,
+                                                   b.order2, b.order2 ? b.n2 : nullptr, c->stream),
                           "Hessian factorisation");
         if (rc) return rc;
         if (final && pl && early_slot) pl->copy_early(early_slot);
@@ -848,7 +857,7 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
       pl.wait_late();
       cudaEventRecord(c->es0, c->stream);
       int nk = 0;
-      rc = check_launch(c, stdic::launch_icgn6_plain(a, order, c->scal + 64, c->scal + 12, c->stream, &nk),
+      rc = check_launch(c, stdic::launch_icgn6_plain(a, order, c->scal + 64, c->scal + 12, c->stream, &nk, &c->plain),
                         "IC-GN plain", 0);
       c->launches += nk;
       cudaEventRecord(c->es1, c->stream);
@@ -994,7 +1003,7 @@ static int subpb1_impl(stdic_ctx* c, const stdic_frame* fr, const double* UOld, 
     if (!batched) {
       cudaEventRecord(c->es0, c->stream);
       int nk = 0;
-      rc = check_launch(c, stdic::launch_icgn2_plain(a, order, c->scal + 64, c->scal + 12, c->stream, &nk),
+      rc = check_launch(c, stdic::launch_icgn2_plain(a, order, c->scal + 64, c->scal + 12, c->stream, &nk, &c->plain),
                         "Subpb1 plain", 0);
       c->launches += nk;
       cudaEventRecord(c->es1, c->stream);
@@ -1279,7 +1288,7 @@ int stdic_admm(stdic_ctx* c, const stdic_frame* fr, const double* coords, int N,
     if (batched) r = run_batched(c, b, N, cands, QueueKeys{nullptr, dwl, 0});
     else {
       int nk = 0;
-      r = check_launch(c, stdic::launch_icgn2_plain(a, order, c->scal + 64, c->scal + 12, c->stream, &nk),
+      r = check_launch(c, stdic::launch_icgn2_plain(a, order, c->scal + 64, c->scal + 12, c->stream, &nk, &c->plain),
                        "Subpb1 plain", 0);
       c->launches += nk;
     }

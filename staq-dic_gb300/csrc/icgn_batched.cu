@@ -1515,8 +1515,18 @@ __device__ __noinline__ void lu_inverse6(const double* __restrict__ H, double* _
 
 __global__ void __launch_bounds__(64) factor6_kernel(const SubsetState6* __restrict__ st,
                                                       const double* __restrict__ H6,
-                                                      double* __restrict__ Hinv6, int n) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+                                                      double* __restrict__ Hinv6, int n,
+                                                      const int32_t* __restrict__ list,
+                                                      const int* __restrict__ counts) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (list) {
+    // the subsets the iterations take, packed at the front of the grid (in
+    // node order the subsets decided in the set-up come in runs, which left
+    // the busiest SM at 1.5x the mean)
+    const int nw = counts[0], ns = counts[1];
+    if (t >= nw + ns) return;
+    t = t < nw ? list[t] : list[2 * (size_t)n - ns + (t - nw)];
+  }
   if (t >= n || st[t].code != 0) return;
   // packed lower Cholesky factor L (row-major), all indices compile-time
   double l[21];
@@ -1595,11 +1605,11 @@ __global__ void __launch_bounds__(64) factor6_kernel(const SubsetState6* __restr
 }
 
 cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hinv6, int n,
-                           cudaStream_t s) {
+                           const int32_t* list, const int* counts, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   // 64-thread blocks: four times as many blocks as SMs even for ~20k
   // subsets, so that the FP64-bound work spreads evenly
-  factor6_kernel<<<(n + 63) / 64, 64, 0, s>>>(st, H6, Hinv6, n);
+  factor6_kernel<<<(n + 63) / 64, 64, 0, s>>>(st, H6, Hinv6, n, list, counts);
   return cudaGetLastError();
 }
 

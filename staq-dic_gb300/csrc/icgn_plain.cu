@@ -699,7 +699,7 @@ cudaError_t launch_class(const IcgnArgs& a, PlainClass cl, int nodes_hint, cudaS
 
 template <bool TWO>
 cudaError_t launch_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,
-                         int* kernels) {
+                         int* kernels, const PlainStreams* ps) {
   *kernels = 0;
   if (a.N <= 0) return cudaSuccess;
   const bool per_node = TWO ? a.wsl2 != nullptr : a.ws_list != nullptr;
@@ -723,17 +723,44 @@ cudaError_t launch_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* 
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   *kernels = 4;
+  // The classes run concurrently when side streams are given: each class is
+  // a persistent grid that fills the SMs, so a later class's CTAs start as
+  // the earlier class drains, and the slow subsets at the end of one class
+  // (3 to 101 iterations each) overlap the next class's work instead of
+  // leaving SMs idle.  The 8-px class, whose long subsets make the longest
+  // tail, is launched first.
+  if (ps) {
+    e = cudaEventRecord(ps->fork, s);
+    if (e != cudaSuccess) return e;
+  }
+  int forked = 0;
   for (int k = 0; k < kClasses && e == cudaSuccess; ++k) {
     PlainClass cl{order, ranges + 2 * k, k + 1 < kClasses ? std::min(grown_tile_pixels(kClassEdge[k]), a.npx_max)
                                                            : a.npx_max,
                   ranges + 2 * kClasses + k};
+    cudaStream_t sk = s;
+    if (ps && k > 0) {
+      sk = ps->side[k - 1];
+      e = cudaStreamWaitEvent(sk, ps->fork, 0);
+      if (e != cudaSuccess) break;
+    }
     switch (kClassThreads[k]) {
-      case 32: e = launch_class<32, TWO>(a, cl, a.N, s); break;
-      case 64: e = launch_class<64, TWO>(a, cl, a.N, s); break;
-      case 128: e = launch_class<128, TWO>(a, cl, a.N, s); break;
-      default: e = launch_class<256, TWO>(a, cl, a.N, s); break;
+      case 32: e = launch_class<32, TWO>(a, cl, a.N, sk); break;
+      case 64: e = launch_class<64, TWO>(a, cl, a.N, sk); break;
+      case 128: e = launch_class<128, TWO>(a, cl, a.N, sk); break;
+      default: e = launch_class<256, TWO>(a, cl, a.N, sk); break;
+    }
+    if (ps && k > 0) {
+      const cudaError_t e2 = cudaEventRecord(ps->join[k - 1], sk);
+      if (e == cudaSuccess) e = e2;
+      if (e2 == cudaSuccess) ++forked;
     }
     ++*kernels;
+  }
+  // every side stream that was given work is joined back, errors or not
+  for (int k = 0; k < forked; ++k) {
+    const cudaError_t e2 = cudaStreamWaitEvent(s, ps->join[k], 0);
+    if (e == cudaSuccess) e = e2;
   }
   return e;
 }
@@ -741,13 +768,13 @@ cudaError_t launch_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* 
 }  // namespace
 
 cudaError_t launch_icgn6_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,
-                               int* kernels) {
-  return launch_plain<false>(a, order, qscratch, ranges, s, kernels);
+                               int* kernels, const PlainStreams* ps) {
+  return launch_plain<false>(a, order, qscratch, ranges, s, kernels, ps);
 }
 
 cudaError_t launch_icgn2_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,
-                               int* kernels) {
-  return launch_plain<true>(a, order, qscratch, ranges, s, kernels);
+                               int* kernels, const PlainStreams* ps) {
+  return launch_plain<true>(a, order, qscratch, ranges, s, kernels, ps);
 }
 
 }  // namespace stdic

@@ -119,8 +119,12 @@ struct SubsetState6 {
   float Jf[6], J1[6];
 };
 
+// list/counts (optional): the iteration stage's work lists of the set-up
+// stage (list[0..counts[0]) and list[2n - counts[1]..2n)); only those subsets
+// are factorised, packed at the front of the grid so that they spread evenly
+// over the SMs
 cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hinv6, int n,
-                           cudaStream_t s);
+                           const int32_t* list, const int* counts, cudaStream_t s);
 
 
 // Size of one team's shared slot / global slice of the batched kernel.
@@ -150,10 +154,18 @@ size_t intsearch_qfactor_scratch_bytes(int nx, int ny, int Sx, int Sy, int wsx, 
 cudaError_t launch_intsearch_qfactors(const double* f, const double* g, int W, int Sx, int Sy, double gx0,
                                       double gy0, int nx, int ny, int wsx, int wsy, int stepx, int stepy,
                                       double* scratch, double* qf, cudaStream_t s);
+// Streams and events on which the size classes run concurrently (nullptr:
+// one after another on s): class 0 on s, class k on side[k-1], forked from s
+// after the class ranges are known and joined back into s at the end.
+struct PlainStreams {
+  cudaStream_t side[3];
+  cudaEvent_t fork;
+  cudaEvent_t join[3];
+};
 cudaError_t launch_icgn6_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,
-                               int* kernels);
+                               int* kernels, const PlainStreams* ps = nullptr);
 cudaError_t launch_icgn2_plain(const IcgnArgs& a, int32_t* order, int* qscratch, int* ranges, cudaStream_t s,
-                               int* kernels);
+                               int* kernels, const PlainStreams* ps = nullptr);
 // tmp_dev: five device 64-bit integers of scratch (the code statistics)
 cudaError_t launch_badpoints(int32_t* conv, int N, double* U, double* F, int two_dof,
                              int* badnum_dev, unsigned long long* tmp_dev, cudaStream_t s);

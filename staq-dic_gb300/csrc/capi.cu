@@ -225,42 +225,40 @@ struct Plan {
       c->ws_size = want;
     }
     ctx = c;
-    bool side_started = false;
+    // Two passes: the in-order copies first, then the late ones.  A late copy
+    // starts only after every in-order copy (the side stream waits for an
+    // event recorded behind them), so that it overlaps the first kernels and
+    // does not share the host link with the inputs those kernels wait for.
+    bool any_late = false;
     for (auto& it : items) {
       if (it.dir == 0 && it.dev) *it.slot = const_cast<void*>(it.host);
       else if (it.dir == 1 && it.dev) *it.slot = it.host_out;
       else *it.slot = (char*)c->ws + it.off;
       if (it.dir == 0 && !it.dev) {
-        cudaStream_t s = c->stream;
         if (it.late && !c->capturing) {
-          if (!side_started) {
-            cudaError_t e = cudaEventRecord(c->evs0, c->stream);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->evs0, 0);
-            if (e != cudaSuccess) return cuda_fail(c, e, "side stream");
-            side_started = true;
-            late_pending = true;
-          }
-          s = c->side;
+          any_late = true;
+          continue;
         }
-        cudaError_t e = cudaMemcpyAsync(*it.slot, it.host, it.bytes, cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) {
-          if (side_started) {
-            // no event marks the end of the side copies: wait for them here
-            cudaStreamSynchronize(c->side);
-            late_pending = false;
-          }
-          return cuda_fail(c, e, "host-to-device copy");
-        }
+        cudaError_t e = cudaMemcpyAsync(*it.slot, it.host, it.bytes, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "host-to-device copy");
       }
     }
-    if (side_started) {
-      cudaError_t e = cudaEventRecord(c->evs1, c->side);
-      if (e != cudaSuccess) {
-        cudaStreamSynchronize(c->side);
-        late_pending = false;
-        return cuda_fail(c, e, "side stream");
-      }
+    if (!any_late) return STDIC_OK;
+    cudaError_t e = cudaEventRecord(c->evs0, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->evs0, 0);
+    if (e != cudaSuccess) return cuda_fail(c, e, "side stream");
+    for (auto& it : items) {
+      if (!(it.dir == 0 && !it.dev && it.late)) continue;
+      e = cudaMemcpyAsync(*it.slot, it.host, it.bytes, cudaMemcpyHostToDevice, c->side);
+      if (e != cudaSuccess) break;
     }
+    if (e == cudaSuccess) e = cudaEventRecord(c->evs1, c->side);
+    if (e != cudaSuccess) {
+      // no event marks the end of the side copies: wait for them here
+      cudaStreamSynchronize(c->side);
+      return cuda_fail(c, e, "host-to-device copy");
+    }
+    late_pending = true;
     return STDIC_OK;
   }
 

@@ -31,7 +31,12 @@
  * of the context's GPU.  Host buffers are staged through a context-owned device
  * workspace and the call returns after the results are copied back.  When every
  * pointer of a call is device memory the call is asynchronous on the context's
- * stream (per-node codes are ready after stream synchronisation).
+ * stream (per-node codes are ready after stream synchronisation).  Pinned host
+ * memory (cudaHostAlloc, cudaHostRegister) lets the batched LocalICGNQuadtree
+ * calls overlap copies with kernels: the deformed frame is uploaded on a
+ * context-owned second stream during the set-up kernels, and HtempPar is
+ * downloaded during the iterations; pageable memory gives the same results
+ * with the copies in order.
  *
  * Errors: 0 on success, a negative STDIC_E_* code otherwise (stdic_last_error
  * gives text).  Per-node failures never raise: they are reported through the

@@ -54,8 +54,10 @@ TOL = 1e-2
 DEFAULT_WORKLOAD = "hole2048"
 # sources of the batched solver kernels: a traffic figure is quoted only from
 # an ncu capture of exactly these sources
-KERNEL_SOURCES = ("staq-dic_gb300/csrc/icgn_batched.cu", "staq-dic_gb300/csrc/device_common.cuh",
-                  "staq-dic_gb300/csrc/kernels.h")
+KERNEL_SOURCES = ("staq-dic_gb300/csrc/icgn_batched.cuh", "staq-dic_gb300/csrc/icgn_batched.cu",
+                  "staq-dic_gb300/csrc/icgn_batched_tw1.cu", "staq-dic_gb300/csrc/icgn_batched_tw2.cu",
+                  "staq-dic_gb300/csrc/icgn_batched_tw4.cu", "staq-dic_gb300/csrc/icgn_batched_tw8.cu",
+                  "staq-dic_gb300/csrc/device_common.cuh", "staq-dic_gb300/csrc/kernels.h")
 
 
 def log(*a):

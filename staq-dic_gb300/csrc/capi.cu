@@ -614,7 +614,8 @@ std::vector<BatchedCand> batched_candidates(stdic_ctx* c, bool two, int npx_max,
                            {4, 256, 32, 5600, 1300}, {4, 256, 64, 5600, 1300},
                            {8, 256, 64, 5600, 650},  {4, 256, 32, 5600, 1600},
                            {2, 256, 32, 5600, 1300}, {1, 256, 0, 5600, 0},
-                           {2, 256, 64, 5600, 0},    {4, 256, 32, 5600, 0}};
+                           {2, 256, 64, 5600, 0},    {4, 256, 32, 5600, 0},
+                           {2, 256, 32, 5600, 0}};
   for (auto& sh : shapes) {
     const int tw = sh[0], threads = sh[1], split = sh[2], per_warp = sh[3], gt_warp = sh[4];
     const int teams_per_block = threads / (32 * tw);

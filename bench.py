@@ -1000,6 +1000,14 @@ def main():
                     "frac": alg_bytes / (kern_ms * 1e-3) / 1e9 / peaks.get("hbm_gbs"),
                     "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
                     "peak_source": src}
+    # the warped footprint of g each iteration gathers: 4 (ws+4)^2 bytes per
+    # subset per iteration (taps reach one pixel before and two after)
+    it_b = np.where((cc >= 1) & (cc <= 101), cc, 0).astype(np.float64)
+    gather_bytes = float((4.0 * (ws_list.astype(np.float64) + 4) ** 2 * it_b).sum())
+    gather_l2 = {"achieved": gather_bytes / (kern_ms * 1e-3) / 1e9, "unit": "GB/s",
+                 "bytes_per_launch": gather_bytes,
+                 "note": "algorithmic bytes of the warped g footprints the iterations gather (through L1 "
+                         "and L2) over the solver kernels' time"}
     plain_flops = float(flops_per_subset(conv_plain, ws_list).sum())
     pk = [s for s in plain_kern if s > 0]
     plain_rf = plain_roofline(plain_flops, float(np.mean(pk)) if pk else float(np.mean(plain_ms)), fp64_peak)
@@ -1017,6 +1025,7 @@ def main():
            "gpu_launches": int(launches),
            "roofline": roofline,
            "roofline_hbm": roofline_hbm,
+           "gather_l2": gather_l2,
            "plain_fp64": {"value": plain_value, "ms_per_step": float(np.mean(plain_ms)),
                           "converged": plain_conv, "roofline": plain_rf},
            "batched_over_plain": value / plain_value if plain_value > 0 else None,

@@ -57,6 +57,8 @@ DEFAULT_WORKLOAD = "hole2048"
 KERNEL_SOURCES = ("staq-dic_gb300/csrc/icgn_batched.cuh", "staq-dic_gb300/csrc/icgn_batched.cu",
                   "staq-dic_gb300/csrc/icgn_batched_tw1.cu", "staq-dic_gb300/csrc/icgn_batched_tw2.cu",
                   "staq-dic_gb300/csrc/icgn_batched_tw4.cu", "staq-dic_gb300/csrc/icgn_batched_tw8.cu",
+                  "staq-dic_gb300/csrc/icgn_batched_tw1s.cu", "staq-dic_gb300/csrc/icgn_batched_tw2s.cu",
+                  "staq-dic_gb300/csrc/icgn_batched_tw4s.cu", "staq-dic_gb300/csrc/icgn_batched_tw8s.cu",
                   "staq-dic_gb300/csrc/device_common.cuh", "staq-dic_gb300/csrc/kernels.h")
 
 

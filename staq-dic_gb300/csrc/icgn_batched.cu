@@ -162,11 +162,12 @@ cudaError_t launch_factor6(const SubsetState6* st, const double* H6, double* Hin
 }
 
 cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, cudaStream_t s) {
+  const bool stg = b.stage != 1 && (b.gtile > 0 || b.gtile_small > 0);
   switch (b.warps_per_subset) {
-    case 1: return launch_icgn_batched_tw1(b, blocks, threads, s);
-    case 2: return launch_icgn_batched_tw2(b, blocks, threads, s);
-    case 4: return launch_icgn_batched_tw4(b, blocks, threads, s);
-    case 8: return launch_icgn_batched_tw8(b, blocks, threads, s);
+    case 1: return stg ? launch_icgn_batched_tw1s(b, blocks, threads, s) : launch_icgn_batched_tw1u(b, blocks, threads, s);
+    case 2: return stg ? launch_icgn_batched_tw2s(b, blocks, threads, s) : launch_icgn_batched_tw2u(b, blocks, threads, s);
+    case 4: return stg ? launch_icgn_batched_tw4s(b, blocks, threads, s) : launch_icgn_batched_tw4u(b, blocks, threads, s);
+    case 8: return stg ? launch_icgn_batched_tw8s(b, blocks, threads, s) : launch_icgn_batched_tw8u(b, blocks, threads, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -178,11 +179,12 @@ int batched_blocks_per_sm(int tw, bool two, int threads, int smem_px, int gtile,
   const int teams = threads / (tw * 32);
   const size_t smem = batched_team_bytes(smem_px, two, tw, gtile) * teams + 128;
   if (smem > 227 * 1024) return 0;
+  const bool stg = (two || stage != 1) && gtile > 0;
   switch (tw) {
-    case 1: return batched_blocks_per_sm_tw1(two, threads, smem, stage);
-    case 2: return batched_blocks_per_sm_tw2(two, threads, smem, stage);
-    case 4: return batched_blocks_per_sm_tw4(two, threads, smem, stage);
-    case 8: return batched_blocks_per_sm_tw8(two, threads, smem, stage);
+    case 1: return stg ? batched_blocks_per_sm_tw1s(two, threads, smem, stage) : batched_blocks_per_sm_tw1u(two, threads, smem, stage);
+    case 2: return stg ? batched_blocks_per_sm_tw2s(two, threads, smem, stage) : batched_blocks_per_sm_tw2u(two, threads, smem, stage);
+    case 4: return stg ? batched_blocks_per_sm_tw4s(two, threads, smem, stage) : batched_blocks_per_sm_tw4u(two, threads, smem, stage);
+    case 8: return stg ? batched_blocks_per_sm_tw8s(two, threads, smem, stage) : batched_blocks_per_sm_tw8u(two, threads, smem, stage);
   }
   return 0;
 }

@@ -1,10 +1,10 @@
-// The batched IC-GN kernel for teams of 1 warp (set-up, iterations and the
-// fused 2-DOF form), in a translation unit of its own so that the team
-// widths compile in parallel.
+// The batched IC-GN kernel for teams of 1 warp without the staged g
+// footprint (the set-up, the iterations and the fused 2-DOF form), in a
+// translation unit of its own so that the instantiations compile in parallel.
 #include "icgn_batched.cuh"
 
 namespace stdic {
 
-STDIC_BATCHED_TEAM_WIDTH(1)
+STDIC_BATCHED_UNIT(1, false, u)
 
 }  // namespace stdic

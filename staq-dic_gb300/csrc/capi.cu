@@ -35,6 +35,7 @@ struct stdic_ctx {
   // during the iterations), with the events that order it against `stream`
   cudaStream_t side = nullptr;
   cudaEvent_t evs0 = nullptr, evs1 = nullptr, evh0 = nullptr, evh1 = nullptr;
+  cudaEvent_t evband[8] = {};  // end of each row band of a banded upload
   // streams and events on which the plain IC-GN size classes run concurrently
   stdic::PlainStreams plain{};
   bool solver_timed = false;
@@ -89,6 +90,9 @@ size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // c->scal slot a kernel sets when a bounded wait for a TMA tile copy gave up
 constexpr int kTmaErrSlot = 40;
+// Frames of fewer than kBandMinRows rows per band are uploaded whole.
+constexpr int kBandMinRows = 128;
+constexpr int kBandScratch = 2 * 256 * stdic::kQueueMaxBands + 2 * stdic::kQueueMaxBands + 1;
 
 // Plans device placement for one call: device pointers pass through, host
 // buffers and scratch get regions of the context workspace.
@@ -103,6 +107,13 @@ constexpr int kTmaErrSlot = 40;
 // touches workspace that an earlier call still uses) and is joined back into
 // the call's stream before finish() copies the rest, and in any case when the
 // plan goes out of scope, so the next call on the stream is ordered after it.
+// "Banded" inputs (in_banded, with set_bands) are uploaded on the side stream
+// in row bands, each band's end marked by an event, so that kernels that need
+// only the first rows of a frame can start (wait_band) while the rest crosses
+// the host link.  A band's copies are issued when the call first waits for
+// it, so that the host queues the kernels of the earlier bands in between
+// (queuing a copy costs the host about as long as the kernels it overlaps);
+// the late copies follow the last band.
 // Under stream capture nothing goes to the side stream.
 struct Plan {
   struct Item {
@@ -115,12 +126,19 @@ struct Plan {
     void** slot;
     bool late;   // input copied on the side stream (in_late)
     bool early;  // output already copied on the side stream (copy_early)
+    // banded input (in_banded): bytes per array row, rows, and the image row
+    // of array row 0 (row_bytes 0: not banded)
+    size_t row_bytes = 0;
+    int rows = 0, row0 = 0;
   };
+  int nbands = 0, band_H = 0;  // set_bands: the frame's rows in nbands bands
+  bool bands_pending = false;     // banded copies in use in this call (until join)
+  int bands_issued = 0;           // bands whose copies are issued
   std::vector<Item> items;
   size_t total = 0;
   bool any_host = false;
   stdic_ctx* ctx = nullptr;
-  bool late_pending = false, early_pending = false;
+  bool late_pending = false, early_pending = false, late_issued = false;
 
   Plan() = default;
   Plan(const Plan&) = delete;
@@ -133,6 +151,74 @@ struct Plan {
     if (!p) { *slot = nullptr; return; }
     if (!it.dev) { it.off = total; total += al(it.bytes); any_host = true; }
     items.push_back(it);
+  }
+  // Uploads the frame's rows in nb bands of about H / nb rows (set before
+  // commit; nb <= 8).
+  void set_bands(int nb, int H) {
+    nbands = std::max(0, std::min(nb, 8));
+    band_H = H;
+  }
+  // A host array of `rows` rows of `row_bytes` bytes whose row r holds image
+  // row r + row0, uploaded band by band (pinned memory only; pageable memory
+  // is copied in order on the call's stream).
+  template <class T>
+  void in_banded(const T* p, size_t count, T** slot, size_t row_bytes, int rows, int row0) {
+    in(p, count, slot);
+    if (p && !items.back().dev && is_pinned_host_ptr(p)) {
+      items.back().row_bytes = row_bytes;
+      items.back().rows = rows;
+      items.back().row0 = row0;
+    }
+  }
+  // The call's stream waits for the rows of bands 0..b (idempotent per band).
+  int wait_band(int b) {
+    if (!bands_pending || !ctx || b < 0 || b >= nbands) return STDIC_OK;
+    const int rc = issue_bands(b);
+    if (rc) return rc;
+    cudaError_t e = cudaStreamWaitEvent(ctx->stream, ctx->evband[b], 0);
+    return e == cudaSuccess ? STDIC_OK : cuda_fail(ctx, e, "band wait");
+  }
+  // Issues the copies of the bands up to b not yet issued, each followed by
+  // its band's event; after the last band, the late copies and evs1.
+  int issue_bands(int b) {
+    if (!bands_pending || !ctx) return STDIC_OK;
+    stdic_ctx* c = ctx;
+    cudaError_t e = cudaSuccess;
+    b = std::min(b, nbands - 1);
+    for (; bands_issued <= b && e == cudaSuccess; ++bands_issued) {
+      const int k = bands_issued;
+      const long long beg = (long long)k * band_H / nbands, end = (long long)(k + 1) * band_H / nbands;
+      for (auto& it : items) {
+        if (!(it.dir == 0 && !it.dev && it.row_bytes > 0 && !it.late)) continue;
+        const long long lo = std::max(0LL, std::min((long long)it.rows, beg - it.row0));
+        const long long hi = k == nbands - 1 ? it.rows : std::max(0LL, std::min((long long)it.rows, end - it.row0));
+        if (hi <= lo) continue;
+        e = cudaMemcpyAsync((char*)*it.slot + lo * it.row_bytes, (const char*)it.host + lo * it.row_bytes,
+                            (hi - lo) * it.row_bytes, cudaMemcpyHostToDevice, c->side);
+        if (e != cudaSuccess) break;
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(c->evband[k], c->side);
+    }
+    if (e == cudaSuccess && bands_issued == nbands && !late_issued) e = issue_late(c);
+    if (e != cudaSuccess) {
+      // no event marks the end of the side copies: wait for them here
+      cudaStreamSynchronize(c->side);
+      bands_pending = false;
+      late_pending = false;
+      return cuda_fail(c, e, "host-to-device copy");
+    }
+    return STDIC_OK;
+  }
+  // The late copies on the side stream, then evs1 behind them.
+  cudaError_t issue_late(stdic_ctx* c) {
+    cudaError_t e = cudaSuccess;
+    for (auto& it : items) {
+      if (!(it.dir == 0 && !it.dev && it.late)) continue;
+      e = cudaMemcpyAsync(*it.slot, it.host, it.bytes, cudaMemcpyHostToDevice, c->side);
+      if (e != cudaSuccess) return e;
+    }
+    late_issued = true;
+    return cudaEventRecord(c->evs1, c->side);
   }
   // pageable host memory is copied in order on the call's stream instead
   template <class T>
@@ -164,10 +250,14 @@ struct Plan {
       if ((const void* const*)it.slot == slot) return it.dir == 1 && !it.dev;
     return false;
   }
-  // The call's stream waits for the late inputs (idempotent).
-  void wait_late() {
+  // The call's stream waits for the late inputs (idempotent), issuing the
+  // bands not yet issued first.
+  int wait_late() {
+    const int rc = issue_bands(nbands - 1);
+    if (rc) return rc;
     if (late_pending && ctx) cudaStreamWaitEvent(ctx->stream, ctx->evs1, 0);
     late_pending = false;
+    return STDIC_OK;
   }
   // Copies the host output bound to slot now, on the side stream, after the
   // work the call's stream holds so far; finish() skips it.  Returns false
@@ -195,11 +285,14 @@ struct Plan {
     }
     return false;
   }
-  // Joins every side-stream copy into the call's stream.
-  void join() {
-    wait_late();
+  // Joins every side-stream copy into the call's stream (evs1 is recorded
+  // after the last of them, banded or late).
+  int join() {
+    const int rc = wait_late();
+    bands_pending = false;
     if (early_pending && ctx) cudaStreamWaitEvent(ctx->stream, ctx->evh1, 0);
     early_pending = false;
+    return rc;
   }
   // out-or-scratch: user buffer when given, else workspace
   template <class T>
@@ -229,7 +322,8 @@ struct Plan {
     // starts only after every in-order copy (the side stream waits for an
     // event recorded behind them), so that it overlaps the first kernels and
     // does not share the host link with the inputs those kernels wait for.
-    bool any_late = false;
+    bool any_late = false, any_banded = false;
+    const bool banding = nbands > 0 && band_H > 0 && !c->capturing;
     for (auto& it : items) {
       if (it.dir == 0 && it.dev) *it.slot = const_cast<void*>(it.host);
       else if (it.dir == 1 && it.dev) *it.slot = it.host_out;
@@ -239,26 +333,33 @@ struct Plan {
           any_late = true;
           continue;
         }
+        if (it.row_bytes > 0 && banding) {
+          any_banded = true;
+          continue;
+        }
         cudaError_t e = cudaMemcpyAsync(*it.slot, it.host, it.bytes, cudaMemcpyHostToDevice, c->stream);
         if (e != cudaSuccess) return cuda_fail(c, e, "host-to-device copy");
       }
     }
-    if (!any_late) return STDIC_OK;
+    if (!any_late && !any_banded) return STDIC_OK;
     cudaError_t e = cudaEventRecord(c->evs0, c->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->evs0, 0);
     if (e != cudaSuccess) return cuda_fail(c, e, "side stream");
-    for (auto& it : items) {
-      if (!(it.dir == 0 && !it.dev && it.late)) continue;
-      e = cudaMemcpyAsync(*it.slot, it.host, it.bytes, cudaMemcpyHostToDevice, c->side);
-      if (e != cudaSuccess) break;
+    late_pending = true;
+    late_issued = false;
+    if (any_banded) {
+      // band copies (and the late ones after them) are issued by wait_band
+      bands_pending = true;
+      bands_issued = 0;
+      return STDIC_OK;
     }
-    if (e == cudaSuccess) e = cudaEventRecord(c->evs1, c->side);
+    e = issue_late(c);
     if (e != cudaSuccess) {
       // no event marks the end of the side copies: wait for them here
       cudaStreamSynchronize(c->side);
+      late_pending = false;
       return cuda_fail(c, e, "host-to-device copy");
     }
-    late_pending = true;
     return STDIC_OK;
   }
 
@@ -267,7 +368,8 @@ struct Plan {
   // produced) may ride along to a host int *dst_int in the same
   // synchronisation; *delivered says whether it did.
   int finish(stdic_ctx* c, const int* dev_int = nullptr, int* dst_int = nullptr, bool* delivered = nullptr) {
-    join();
+    const int jrc = join();
+    if (jrc) return jrc;
     if (delivered) *delivered = false;
     for (auto& it : items) {
       if (it.dir == 1 && !it.dev && !it.early) {
@@ -350,6 +452,8 @@ int stdic_ctx_create(stdic_ctx** out, int device) {
   for (cudaEvent_t* ev : {&c->evs0, &c->evs1, &c->evh0, &c->evh1, &c->plain.fork, &c->plain.join[0],
                           &c->plain.join[1], &c->plain.join[2]})
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  for (cudaEvent_t& ev : c->evband)
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
   for (cudaStream_t* st : {&c->plain.side[0], &c->plain.side[1], &c->plain.side[2]})
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -376,6 +480,8 @@ int stdic_ctx_destroy(stdic_ctx* c) {
   if (c->es1) cudaEventDestroy(c->es1);
   for (cudaEvent_t ev : {c->evs0, c->evs1, c->evh0, c->evh1, c->plain.fork, c->plain.join[0], c->plain.join[1],
                          c->plain.join[2]})
+    if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : c->evband)
     if (ev) cudaEventDestroy(ev);
   if (c->side) cudaStreamDestroy(c->side);
   for (cudaStream_t st : {c->plain.side[0], c->plain.side[1], c->plain.side[2]})
@@ -551,16 +657,26 @@ struct FrameDev {
 
 // late_g: a host deformed frame is uploaded on the side stream (Plan::in_late)
 // while the first kernels run; the caller waits for it before reading g.
+// banded: the reference frame, its gradients and the mask are uploaded in row
+// bands (Plan::in_banded; the gradient arrays' row r is image row r + 3).
 int stage_frame(stdic_ctx* c, Plan& pl, const stdic_frame* fr, FrameDev* d, bool want_f32,
-                int frames, bool late_g = false) {
+                int frames, bool late_g = false, bool banded = false) {
   const size_t es = fr->dtype == STDIC_F64 ? 8 : 4;
   const size_t np = (size_t)fr->W * fr->H, ng = (size_t)(fr->W - 6) * (fr->H - 6);
-  pl.in((const unsigned char*)fr->f, es * np, (unsigned char**)&d->f);
+  const int W = fr->W, H = fr->H;
+  if (banded) pl.in_banded((const unsigned char*)fr->f, es * np, (unsigned char**)&d->f, es * W, H, 0);
+  else pl.in((const unsigned char*)fr->f, es * np, (unsigned char**)&d->f);
   if (late_g) pl.in_late((const unsigned char*)fr->g, es * np * frames, (unsigned char**)&d->g);
   else pl.in((const unsigned char*)fr->g, es * np * frames, (unsigned char**)&d->g);
-  pl.in((const unsigned char*)fr->dfdx, es * ng, (unsigned char**)&d->dfdx);
-  pl.in((const unsigned char*)fr->dfdy, es * ng, (unsigned char**)&d->dfdy);
-  pl.in(fr->mask, np, (uint8_t**)&d->mask);
+  if (banded) {
+    pl.in_banded((const unsigned char*)fr->dfdx, es * ng, (unsigned char**)&d->dfdx, es * (W - 6), H - 6, 3);
+    pl.in_banded((const unsigned char*)fr->dfdy, es * ng, (unsigned char**)&d->dfdy, es * (W - 6), H - 6, 3);
+    pl.in_banded(fr->mask, np, (uint8_t**)&d->mask, (size_t)W, H, 0);
+  } else {
+    pl.in((const unsigned char*)fr->dfdx, es * ng, (unsigned char**)&d->dfdx);
+    pl.in((const unsigned char*)fr->dfdy, es * ng, (unsigned char**)&d->dfdy);
+    pl.in(fr->mask, np, (uint8_t**)&d->mask);
+  }
   d->f32 = d->g32 = d->dfdx32 = d->dfdy32 = nullptr;
   if (want_f32 && fr->dtype == STDIC_F64) {
     pl.scratch(np, (float**)&d->f32);
@@ -675,6 +791,18 @@ int tune_pick() {
   return k;
 }
 
+// STDIC_UPLOAD_BANDS=<n> (0, 1, 2, 4 or 8, default 4; other values round
+// down): row bands of a host reference frame in pinned memory (0: upload it
+// whole before the set-up stage).
+int upload_bands() {
+  static const int n = [] {
+    const char* e = std::getenv("STDIC_UPLOAD_BANDS");
+    const int v = e && *e ? std::max(0, std::min(8, std::atoi(e))) : 4;
+    return v >= 8 ? 8 : v >= 4 ? 4 : v >= 2 ? 2 : v;
+  }();
+  return n;
+}
+
 // Subset sizes the work queue is sorted by (one of ws_list, wsl2, ws_all).
 struct QueueKeys {
   const int32_t* ws_list;
@@ -682,12 +810,24 @@ struct QueueKeys {
   int ws_all;
 };
 
+// Row bands of a frame uploaded band by band (Plan::in_banded): nb bands of
+// an H-row frame, with kBandScratch ints of device scratch for the banded
+// queue (its histogram and cursors, then each band's first position and
+// wide-team count).
+struct Bands {
+  int nb = 0, H = 0;
+  int32_t* buf = nullptr;
+};
+
 // pl (optional): the call's plan; the iteration stage waits for its late
 // inputs, and early_slot names an output (the Hessians) that the set-up stage
 // completes and that the side stream copies to the host during the iterations
-// of the final launch.
+// of the final launch.  bands (optional, 6-DOF, one frame): when the plan
+// uploads the frame in row bands, the final launch runs the set-up stage band
+// by band, each part as soon as its rows are on the device.
 int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector<BatchedCand>& cands,
-                const QueueKeys& qk, Plan* pl = nullptr, const void* const* early_slot = nullptr) {
+                const QueueKeys& qk, Plan* pl = nullptr, const void* const* early_slot = nullptr,
+                const Bands* bands = nullptr) {
   const bool two = b.two_dof != 0;
   if (cands.empty()) return fail(c, STDIC_E_UNSUPPORTED, "no launch shape fits this subset size");
   b.queue_head = c->scal + 4;  // [4] team phase, [5] single-warp phase
@@ -719,9 +859,19 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
     // (the long chains) in the 6-DOF iteration stage, and the single-warp
     // list, filled in set-up order, then runs largest first too.
     const int mode = cd.split ? (two ? 2 : 0) : (cd.tw == 1 ? 1 : 0);
-    int rc = check_launch(c, stdic::launch_build_queue(qk.ws_list, qk.wsl2, qk.ws_all, b.a.N,
-                                                       (int32_t*)b.order, c->scal + 6, c->scal + 64, c->stream,
-                                                       mode, cd.split),
+    // set-up by row band (final launch of a frame uploaded in bands): the
+    // queue grouped by band, then one set-up launch per band, each after its
+    // band's copies
+    const bool banded = final && !two && b.frames <= 1 && !qk.wsl2 && bands && bands->nb > 0 && pl &&
+                        pl->bands_pending;
+    int* boff = banded ? bands->buf + 2 * 256 * stdic::kQueueMaxBands : nullptr;
+    int rc = check_launch(c, banded ? stdic::launch_build_band_queue(qk.ws_list, qk.ws_all, b.a.N, b.a.coords + b.a.N,
+                                                                     bands->H, bands->nb, (int32_t*)b.order,
+                                                                     c->scal + 6, boff, boff + bands->nb + 1,
+                                                                     bands->buf, c->stream, mode, cd.split)
+                                    : stdic::launch_build_queue(qk.ws_list, qk.wsl2, qk.ws_all, b.a.N,
+                                                                (int32_t*)b.order, c->scal + 6, c->scal + 64,
+                                                                c->stream, mode, cd.split),
                           "queue", 3);
     if (rc) return rc;
     // 2-DOF: one fused pass; 6-DOF: set-up, FP64 factorisation, iterations
@@ -732,23 +882,46 @@ int run_batched(stdic_ctx* c, stdic::BatchedArgs& b, int Ntot, const std::vector
       cudaError_t e = cudaMemsetAsync(b.n2, 0, 2 * sizeof(int), c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "list reset");
     }
-    for (int k = 0; k < (two ? 1 : 2); ++k) {
-      cudaError_t e = cudaMemsetAsync(b.queue_head, 0, 2 * sizeof(int), c->stream);
-      if (e != cudaSuccess) return cuda_fail(c, e, "queue reset");
-      b.stage = stages[k];
-      // the deformed frame is read from the iteration stage on (the fused
-      // 2-DOF pass reads it throughout)
-      if (pl && b.stage != 1) pl->wait_late();
-      rc = check_launch(c, stdic::launch_icgn_batched(b, b.stage == 1 ? cd.blocks1 : cd.blocks, cd.threads, c->stream),
-                        "IC-GN batched");
+    if (banded) {
+      b.stage = 1;
+      for (int k = 0; k < bands->nb; ++k) {
+        rc = pl->wait_band(k);
+        if (rc) return rc;
+        cudaError_t e = cudaMemsetAsync(b.queue_head, 0, 2 * sizeof(int), c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "queue reset");
+        b.band_list = (const int32_t*)b.order;
+        b.band_off = boff;
+        b.band_nbig = boff + bands->nb + 1;
+        b.band = k;
+        rc = check_launch(c, stdic::launch_icgn_batched(b, cd.blocks1, cd.threads, c->stream), "IC-GN batched");
+        b.band_list = nullptr;
+        b.band_off = b.band_nbig = nullptr;
+        b.band = 0;
+        if (rc) return rc;
+      }
+    } else if (pl) {
+      rc = pl->wait_band(pl->nbands - 1);  // the whole frame (no-op when not banded)
       if (rc) return rc;
+    }
+    for (int k = 0; k < (two ? 1 : 2); ++k) {
+      b.stage = stages[k];
+      if (!(banded && b.stage == 1)) {
+        cudaError_t e = cudaMemsetAsync(b.queue_head, 0, 2 * sizeof(int), c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "queue reset");
+        // the deformed frame is read from the iteration stage on (the fused
+        // 2-DOF pass reads it throughout)
+        if (pl && b.stage != 1) rc = pl->wait_late();
+        if (rc) return rc;
+        rc = check_launch(c, stdic::launch_icgn_batched(b, b.stage == 1 ? cd.blocks1 : cd.blocks, cd.threads, c->stream),
+                          "IC-GN batched");
+        if (rc) return rc;
+      }
       if (!two && k == 0) {
         rc = check_launch(c, stdic::launch_factor6((const stdic::SubsetState6*)b.st6, b.H6, b.Hinv6, Ntot,
                                                    b.order2, b.order2 ? b.n2 : nullptr, c->stream),
                           "Hessian factorisation");
         if (rc) return rc;
         if (final && pl && early_slot) pl->copy_early(early_slot);
-
       }
     }
     return STDIC_OK;
@@ -816,8 +989,15 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
   Plan pl;
   FrameDev d;
   // batched FP32 frames: g is first read by the iteration stage, so a host
-  // g is uploaded while the queue, set-up and factorisation kernels run
-  stage_frame(c, pl, fr, &d, batched, frames, batched && fr->dtype == STDIC_F32);
+  // g is uploaded while the queue, set-up and factorisation kernels run; one
+  // frame: the rest of the frame is uploaded in row bands, each band's
+  // set-up starting as soon as its rows are on the device
+  const bool f32b = batched && fr->dtype == STDIC_F32;
+  Bands bands;
+  if (f32b && frames == 1 && N > 0 && upload_bands() > 0 && fr->H >= upload_bands() * kBandMinRows)
+    bands.nb = upload_bands(), bands.H = fr->H;
+  stage_frame(c, pl, fr, &d, batched, frames, f32b, bands.nb > 0);
+  pl.set_bands(bands.nb, bands.H);
   stdic::IcgnArgs a{};
   pl.in(U0, 2 * NT, (double**)&a.U0);
   pl.in(coords, 2 * (size_t)N, (double**)&a.coords);
@@ -843,6 +1023,7 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
     pl.scratch(21 * nt, &H6);
     pl.scratch(36 * nt, &Hinv6);
     pl.scratch(2 * nt, &order2);
+    if (bands.nb > 0) pl.scratch((size_t)kBandScratch, &bands.buf);
   }
   int rc = pl.commit(c);
   if (rc) return rc;
@@ -878,7 +1059,7 @@ static int icgn_local_impl(stdic_ctx* c, const stdic_frame* fr, const double* U0
         // then zeroes in its copy from the codes
         early_h = pl.host_output((const void* const*)&a.Hpk) && pl.host_output((const void* const*)&a.conv);
         rc = run_batched(c, b, (int)NT, cands, QueueKeys{a.ws_list, nullptr, winsize}, &pl,
-                         early_h ? (const void* const*)&a.Hpk : nullptr);
+                         early_h ? (const void* const*)&a.Hpk : nullptr, &bands);
         early_h = early_h && pl.copied_early((const void* const*)&a.Hpk);
       }
     }

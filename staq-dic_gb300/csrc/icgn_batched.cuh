@@ -1452,6 +1452,24 @@ __global__ void __launch_bounds__(256, STAGE == 1 ? 3 : 2) icgn_batched_kernel(c
     }
     return;
   }
+  if (STAGE == 1 && B.band_list) {
+    // one band of a frame uploaded in row bands: its nodes, big ones first
+    const int lo = B.band_off[B.band], n = B.band_off[B.band + 1] - lo;
+    const int32_t* lst = B.band_list + lo;
+    const int nbg = split ? min(B.band_nbig[B.band], n) : n;
+    team_loop<TW, TWO, STAGE, STG>(B, tm, B.queue_head, 0, nbg, tbase, B.smem_px, B.gtile, gteam, lst);
+    if constexpr (TW > 1) {
+      if (split) {
+        Team<1> t1;
+        t1.id = warp;
+        t1.tl = threadIdx.x & 31;
+        const size_t sub = (tb / TW) & ~(size_t)127;
+        team_loop<1, TWO, STAGE, STG>(B, t1, B.queue_head + 1, nbg, n, tbase + sub * (warp % TW),
+                                      B.smem_px_small, B.gtile_small, B.scratch + gstride * (gwarp0 + warp), lst);
+      }
+    }
+    return;
+  }
   const int split_q = split ? min(*B.n_big * nf, Ntot) : Ntot;
   team_loop<TW, TWO, STAGE, STG>(B, tm, B.queue_head, 0, split_q, tbase, B.smem_px, B.gtile, gteam);
   if constexpr (TW > 1) {

@@ -104,6 +104,15 @@ struct BatchedArgs {
   // per element (cp.async) or gathers from global memory instead
   int gbox_n;
   int* tma_err;           // set to 1 when a footprint copy's bounded wait gives up
+  // 6-DOF set-up stage over one band of a frame uploaded in row bands
+  // (band_list set): the queue's nodes regrouped by the band whose rows they
+  // need (band_list, with band_off[band] .. band_off[band + 1]), of which the
+  // first band_nbig[band] go to the wide teams of the split form; band_list
+  // null: the whole queue
+  const int32_t* band_list;
+  const int* band_off;
+  const int* band_nbig;
+  int band;
   CUtensorMap gmap[kGBoxes];
 };
 
@@ -178,6 +187,19 @@ cudaError_t launch_to_f32(const double* in, float* out, long long n, cudaStream_
 cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int ws_all, int N,
                                int32_t* order, int* n_big, int* scratch, cudaStream_t s, int ascending = 0,
                                int big_ws = 0);
+// The same sort of a 6-DOF queue (sizes ws_list or ws_all) with the nodes
+// first grouped by row band, for a frame of H rows uploaded in nb bands
+// (1, 2, 4 or 8; band b ends at row (b + 1) H / nb, the last at H): a node
+// goes to the first band whose rows cover every row its set-up may read (its
+// window grown to the largest size the mask can cause, around its rounded y
+// coordinate coord_y).  band_off (nb + 1 ints) receives each band's first
+// position and the total, band_big (nb ints) each band's nodes of at least
+// big_ws pixels a side; n_big the total of those.  scratch: 2 * 256 *
+// kQueueMaxBands device ints.
+constexpr int kQueueMaxBands = 8;
+cudaError_t launch_build_band_queue(const int32_t* ws_list, int ws_all, int N, const double* coord_y, int H, int nb,
+                                    int32_t* order, int* n_big, int* band_off, int* band_big, int* scratch,
+                                    cudaStream_t s, int ascending, int big_ws);
 // Largest tile of a single warp's share of a split team slot.
 int batched_small_px(int sm_px, bool two, int tw, int gtile);
 cudaError_t launch_icgn_batched(const BatchedArgs& b, int blocks, int threads, cudaStream_t s);

@@ -764,23 +764,48 @@ struct QueueKey {
   const int32_t* ws_list;
   const int32_t* wsl2;
   int ws_all, N, ascending, bw;
+  // row bands (NB > 1): the y coordinates of the nodes and the frame's rows
+  const double* coord_y;
+  int H;
   // order 0: larger subsets first; 1: smaller first; 2: subsets of at least
   // bw pixels a side first (larger first), then the rest smaller first
-  STDIC_DEV int operator()(int k) const {
-    int w = ws_all;
-    if (wsl2) w = max(wsl2[k], wsl2[N + k]);
-    else if (ws_list) w = ws_list[k];
+  STDIC_DEV int size_bin(int w) const {
     const int b = min(max(w, 0), 255);
     if (ascending == 2) return b >= bw ? 255 - b : 256 - bw + b;
     return ascending ? b : 255 - b;
+  }
+  STDIC_DEV int edge(int k) const {
+    int w = ws_all;
+    if (wsl2) w = max(wsl2[k], wsl2[N + k]);
+    else if (ws_list) w = ws_list[k];
+    return w;
+  }
+  // the first of NB bands (band b ends at row (b + 1) H / NB) whose rows
+  // cover every row the node's set-up may read: its window grown to the
+  // largest size the mask can cause (grown_tile_pixels), around the rounded
+  // centre (1-based rows y0 - wg / 2 .. y0 + wg / 2)
+  template <int NB>
+  STDIC_DEV int band(int k, int w) const {
+    if (NB == 1) return 0;
+    const int wg = 2 * (int)((1.2910 * w) / 2 + 1) + 2;
+    const long long need = llround(coord_y[k]) + wg / 2;  // 0-based rows [0, need)
+    int b = 0;
+    while (b < NB - 1 && (long long)(b + 1) * H / NB < need) ++b;
+    return b;
+  }
+  template <int NB>
+  STDIC_DEV int operator()(int k) const {
+    const int w = edge(k);
+    return band<NB>(k, w) * 256 + size_bin(w);
   }
 };
 
 constexpr int kQueueBlockItems = 2048;  // items per block of the histogram and scatter steps
 
+template <int NB>
 __global__ void __launch_bounds__(256) queue_hist_kernel(QueueKey key, int* __restrict__ ghist) {
-  __shared__ int hist[256];
-  hist[threadIdx.x] = 0;
+  __shared__ int hist[256 * NB];
+  for (int b = threadIdx.x; b < 256 * NB; b += 256) hist[b] = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int k0 = blockIdx.x * kQueueBlockItems;
@@ -788,61 +813,101 @@ __global__ void __launch_bounds__(256) queue_hist_kernel(QueueKey key, int* __re
   // the trip count is the same for every thread, so all lanes of a warp take
   // part in each match, whether or not they hold an item
   for (int k = k0 + threadIdx.x; k - threadIdx.x < k1; k += blockDim.x) {
-    const int kk = k < k1 ? key(k) : -1;
+    const int kk = k < k1 ? key.template operator()<NB>(k) : -1;
     const unsigned grp = __match_any_sync(0xffffffffu, kk);
     if (kk >= 0 && lane == __ffs(grp) - 1) atomicAdd(&hist[kk], __popc(grp));
   }
   __syncthreads();
-  if (hist[threadIdx.x]) atomicAdd(&ghist[threadIdx.x], hist[threadIdx.x]);
+  for (int b = threadIdx.x; b < 256 * NB; b += 256)
+    if (hist[b]) atomicAdd(&ghist[b], hist[b]);
 }
 
-// exclusive scan of the 256 bins into cursor, and the number of items of at
-// least big_ws pixels a side
+// exclusive scan of the 256 NB bins into cursor (thread t scans bins t NB ..
+// t NB + NB - 1), the number of items of at least big_ws pixels a side, and
+// (when given) each band's first position (band_off, NB + 1 ints) and its
+// items of at least big_ws pixels a side (band_big)
+template <int NB>
 __global__ void __launch_bounds__(256) queue_scan_kernel(const int* __restrict__ ghist, int* cursor,
-                                                         int ascending, int big_ws, int* n_big) {
-  __shared__ int wsum[8], wbig[8];
-  const int b = threadIdx.x, lane = b & 31, warp = b >> 5;
-  const int h = ghist[b];
-  int inc = h;
-  for (int o = 1; o < 32; o <<= 1) {
-    const int t = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += t;
+                                                         int ascending, int big_ws, int* n_big, int* band_off,
+                                                         int* band_big) {
+  __shared__ int wsum[8], wbig[8][NB];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  int h[NB], tot = 0;
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    h[j] = ghist[t * NB + j];
+    tot += h[j];
   }
-  // bin b holds subsets of edge w, with b = 255 - w (orders 0 and 2 for
-  // w >= big_ws) or b = w (order 1)
-  const int w = ascending == 2 ? 255 - b : (ascending ? b : 255 - b);
-  int big = w >= max(big_ws, 0) ? h : 0;
-  for (int o = 16; o > 0; o >>= 1) big += __shfl_xor_sync(0xffffffffu, big, o);
+  int inc = tot;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += v;
+  }
+  // bin b holds subsets of edge w in band b / 256, with b % 256 = 255 - w
+  // (orders 0 and 2 for w >= big_ws) or w (order 1)
+  int big[NB];
+#pragma unroll
+  for (int j = 0; j < NB; ++j) big[j] = 0;
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    const int bin = t * NB + j, sb = bin & 255;
+    const int w = ascending == 2 ? 255 - sb : (ascending ? sb : 255 - sb);
+    const int v = w >= max(big_ws, 0) ? h[j] : 0;
+    // band of this bin, accumulated per band slot (NB is small)
+#pragma unroll
+    for (int q = 0; q < NB; ++q)
+      if (q == bin / 256) big[q] += v;
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q)
+    for (int o = 16; o > 0; o >>= 1) big[q] += __shfl_xor_sync(0xffffffffu, big[q], o);
   if (lane == 31) wsum[warp] = inc;
-  if (lane == 0) wbig[warp] = big;
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < NB; ++q) wbig[warp][q] = big[q];
+  }
   __syncthreads();
   int off = 0;
   for (int q = 0; q < warp; ++q) off += wsum[q];
-  cursor[b] = off + inc - h;
-  if (b == 0 && n_big) {
-    int nb = 0;
-    for (int q = 0; q < 8; ++q) nb += wbig[q];
-    *n_big = nb;
+  int run = off + inc - tot;
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    const int bin = t * NB + j;
+    cursor[bin] = run;
+    if (band_off && (bin & 255) == 0) band_off[bin / 256] = run;
+    run += h[j];
+  }
+  if (t == 255 && band_off) band_off[NB] = run;
+  if (t == 0) {
+    int all = 0;
+    for (int q = 0; q < NB; ++q) {
+      int nb = 0;
+      for (int w8 = 0; w8 < 8; ++w8) nb += wbig[w8][q];
+      if (band_big) band_big[q] = nb;
+      all += nb;
+    }
+    if (n_big) *n_big = all;
   }
 }
 
+template <int NB>
 __global__ void __launch_bounds__(256) queue_scatter_kernel(QueueKey key, int* cursor, int32_t* __restrict__ order) {
-  __shared__ int cnt[256], base[256];
-  cnt[threadIdx.x] = 0;
+  __shared__ int cnt[256 * NB], base[256 * NB];
+  for (int b = threadIdx.x; b < 256 * NB; b += 256) cnt[b] = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int k0 = blockIdx.x * kQueueBlockItems;
   const int k1 = min(key.N, k0 + kQueueBlockItems);
   for (int k = k0 + threadIdx.x; k - threadIdx.x < k1; k += blockDim.x) {
-    const int kk = k < k1 ? key(k) : -1;
+    const int kk = k < k1 ? key.template operator()<NB>(k) : -1;
     const unsigned grp = __match_any_sync(0xffffffffu, kk);
     if (kk >= 0 && lane == __ffs(grp) - 1) atomicAdd(&cnt[kk], __popc(grp));
   }
   __syncthreads();
-  base[threadIdx.x] = cnt[threadIdx.x] ? atomicAdd(&cursor[threadIdx.x], cnt[threadIdx.x]) : 0;
+  for (int b = threadIdx.x; b < 256 * NB; b += 256) base[b] = cnt[b] ? atomicAdd(&cursor[b], cnt[b]) : 0;
   __syncthreads();
   for (int k = k0 + threadIdx.x; k - threadIdx.x < k1; k += blockDim.x) {
-    const int kk = k < k1 ? key(k) : -1;
+    const int kk = k < k1 ? key.template operator()<NB>(k) : -1;
     const unsigned grp = __match_any_sync(0xffffffffu, kk);
     const int leader = __ffs(grp) - 1;
     int pos = 0;
@@ -852,20 +917,40 @@ __global__ void __launch_bounds__(256) queue_scatter_kernel(QueueKey key, int* c
   }
 }
 
+template <int NB>
+cudaError_t build_queue_nb(const QueueKey& key, int big_ws, int32_t* order, int* n_big, int* ghist, int* cursor,
+                           int* band_off, int* band_big, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(ghist, 0, 256 * NB * sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  const int blocks = (key.N + kQueueBlockItems - 1) / kQueueBlockItems;
+  queue_hist_kernel<NB><<<blocks, 256, 0, s>>>(key, ghist);
+  queue_scan_kernel<NB><<<1, 256, 0, s>>>(ghist, cursor, key.ascending, big_ws, n_big, band_off, band_big);
+  queue_scatter_kernel<NB><<<blocks, 256, 0, s>>>(key, cursor, order);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_build_queue(const int32_t* ws_list, const int32_t* wsl2, int ws_all, int N,
                                int32_t* order, int* n_big, int* scratch, cudaStream_t s, int ascending,
                                int big_ws) {
   if (N <= 0) return cudaSuccess;
-  QueueKey key{ws_list, wsl2, ws_all, N, ascending, min(max(big_ws, 1), 255)};
+  QueueKey key{ws_list, wsl2, ws_all, N, ascending, min(max(big_ws, 1), 255), nullptr, 0};
+  return build_queue_nb<1>(key, big_ws, order, n_big, scratch, scratch + 256, nullptr, nullptr, s);
+}
+
+cudaError_t launch_build_band_queue(const int32_t* ws_list, int ws_all, int N, const double* coord_y, int H, int nb,
+                                    int32_t* order, int* n_big, int* band_off, int* band_big, int* scratch,
+                                    cudaStream_t s, int ascending, int big_ws) {
+  if (N <= 0) return cudaSuccess;
+  QueueKey key{ws_list, nullptr, ws_all, N, ascending, min(max(big_ws, 1), 255), coord_y, H};
   int* ghist = scratch;
-  int* cursor = scratch + 256;
-  cudaError_t e = cudaMemsetAsync(ghist, 0, 256 * sizeof(int), s);
-  if (e != cudaSuccess) return e;
-  const int blocks = (N + kQueueBlockItems - 1) / kQueueBlockItems;
-  queue_hist_kernel<<<blocks, 256, 0, s>>>(key, ghist);
-  queue_scan_kernel<<<1, 256, 0, s>>>(ghist, cursor, ascending, big_ws, n_big);
-  queue_scatter_kernel<<<blocks, 256, 0, s>>>(key, cursor, order);
-  return cudaGetLastError();
+  int* cursor = scratch + 256 * kQueueMaxBands;
+  switch (nb) {
+    case 1: return build_queue_nb<1>(key, big_ws, order, n_big, ghist, cursor, band_off, band_big, s);
+    case 2: return build_queue_nb<2>(key, big_ws, order, n_big, ghist, cursor, band_off, band_big, s);
+    case 4: return build_queue_nb<4>(key, big_ws, order, n_big, ghist, cursor, band_off, band_big, s);
+    case 8: return build_queue_nb<8>(key, big_ws, order, n_big, ghist, cursor, band_off, band_big, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace stdic

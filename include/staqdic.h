@@ -35,8 +35,11 @@
  * memory (cudaHostAlloc, cudaHostRegister) lets the batched LocalICGNQuadtree
  * calls overlap copies with kernels: the deformed frame is uploaded on a
  * context-owned second stream during the set-up kernels, and HtempPar is
- * downloaded during the iterations; pageable memory gives the same results
- * with the copies in order.
+ * downloaded during the iterations; in stdic_icgn_local the reference frame,
+ * its gradients and the mask are uploaded in row bands (STDIC_UPLOAD_BANDS:
+ * 0, 1, 2, 4 or 8, default 4), each band's set-up kernel starting when its
+ * rows arrive.  Pageable memory gives the same results with the copies in
+ * order.
  *
  * Errors: 0 on success, a negative STDIC_E_* code otherwise (stdic_last_error
  * gives text).  Per-node failures never raise: they are reported through the

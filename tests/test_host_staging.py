@@ -5,13 +5,19 @@ With pinned host buffers, stdic_icgn_local uploads the deformed frame on a
 side stream while the queue, set-up and factorisation kernels run, and
 downloads HtempPar during the iteration stage (the host then zeroes the rows
 of subsets that the iterations ended with code -1, which the iteration stage
-zeroes on the device).  Pageable buffers take the in-order copies, device
+zeroes on the device).  It also uploads the reference frame, its gradients
+and the mask in row bands (STDIC_UPLOAD_BANDS, default 4) and runs the set-up
+stage one band at a time; each band count is checked in a child process,
+since the library reads the variable once.  Pageable buffers take the in-order copies, device
 buffers no copies at all.  The same kernels run in all three, so every output
 must agree bit for bit: U, F, HtempPar, the codes, the hole marks and the
 bad-point count, on the 1024^2 plate with a hole (19,924 quadtree nodes, subsets
 8-64 px, masked subsets near the hole) and on a two-frame batch.
 """
 import ctypes
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -145,3 +151,18 @@ def test_frames_pinned_matches_device(torch_cuda, ctx):
     # both frames are the same pair: the same results per frame
     c = ref["conv"].reshape(2, N)
     assert np.array_equal(c[0], c[1])
+
+
+@pytest.mark.parametrize("bands", [0, 1, 2, 8])
+def test_local_band_counts_identical(torch_cuda, bands):
+    """The local pass with 0 (whole frame), 1, 2 and 8 upload bands: pinned,
+    pageable and device buffers agree bit for bit in a child process."""
+    if os.environ.get("STDIC_UPLOAD_BANDS") is not None:
+        pytest.skip("already in a child process with a fixed band count")
+    env = dict(os.environ, STDIC_UPLOAD_BANDS=str(bands))
+    here = os.path.dirname(os.path.abspath(__file__))
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-p", "no:cacheprovider",
+                        os.path.join(here, "test_host_staging.py") + "::test_local_pinned_pageable_device_identical"],
+                       env=env, cwd=os.path.dirname(here), capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    assert "1 passed" in r.stdout, r.stdout[-2000:]

@@ -139,6 +139,19 @@ def test_local_pinned_pageable_device_identical(torch_cuda, ctx):
         _same(ref, _call(torch, ctx, W, H, N, ins, where))
 
 
+def test_local_banded_uneven_rows(torch_cuda, ctx):
+    """A 1000^2 plate: four bands of 250 rows, so band edges fall at rows that
+    no subset grid lines up with; pinned (banded) and device buffers agree."""
+    from staqdic import workloads
+    torch = torch_cuda
+    w = workloads.hole1024(size=1000)
+    N = w["coordinatesFEM"].shape[0]
+    W, H, ins = _frame_and_inputs(torch, ctx, w)
+    ref = _call(torch, ctx, W, H, N, ins, "device")
+    assert np.count_nonzero((ref["conv"] >= 1) & (ref["conv"] <= 100)) > N // 2
+    _same(ref, _call(torch, ctx, W, H, N, ins, "pinned"))
+
+
 def test_frames_pinned_matches_device(torch_cuda, ctx):
     from staqdic import workloads
     torch = torch_cuda

@@ -659,6 +659,11 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
   bool has_masked = false;
   bool decided = false;  // outputs of this subset already written by the set-up stage
   const double npx0 = (double)(wx + 1) * (double)(wy + 1);
+  // 6-DOF set-up: the first pass keeps f .* mask of each pixel in the tile
+  // slot's f plane when the window fits the slot; if the window then neither
+  // grows nor holds a masked pixel, the tile is exactly that window and the
+  // mask tile and f pass read it back instead of f and the mask
+  bool fm_cached = false;
 
   // 6-DOF iterations: the subset's inverse Hessian pairs and f-side sums are
   // loaded here, with its state, and written to the control block after the
@@ -686,13 +691,18 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     int nanf = 0;
     if (crop_valid) {
       const int mx0 = wx + 1, np0 = (wx + 1) * (wy + 1);
+      const bool keep = STAGE == 1 && !TWO && np0 <= smpx;
+      // the f plane of the tile slot as the tile set-up below lays it out
+      float* fm = (float*)(base + 8 * (size_t)smpx);
       PixIter it(tm.tl, tm.TT, mx0);
       #pragma unroll 4
       for (int p = tm.tl; p < np0; p += tm.TT, it.next()) {
         const float t = fr.F(x1 + it.i, y1 + it.j) * fr.M(x1 + it.i, y1 + it.j);
+        if (keep) fm[p] = t;
         if (t != t) nanf = 1;
         if (t == 0.f) ++cntf;
       }
+      fm_cached = keep;
     }
     cntf = tm.sum_int(cntf, iscr);
     nanf = tm.any(nanf, iscr);
@@ -704,6 +714,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     } else if (!((double)cntf < 0.4 * npx0)) {
       code = kMaxIter + 2;
     } else if ((double)cntf > 0.0 * npx0) {
+      fm_cached = false;  // masked pixels, and the window grows
       if constexpr (TWO) {
         {
           const double aa = (double)(wx + 1) * (double)(wy + 1);
@@ -745,7 +756,11 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     // the mask tile: the set-up stage needs it to find masked subsets; the
     // iteration stage only for a masked subset (its f selection) and, lazily,
     // for the rare unmasked subset whose interpolated g has an exact zero
-    if (stage != 2 || has_masked) {
+    if (fm_cached) {
+      // no pixel of the window is masked (cntf == 0): every mask value is
+      // nonzero, so the mask tile is all ones and the f selection is whole
+      has_masked = false;
+    } else if (stage != 2 || has_masked) {
       int z = 0;
       PixIter it(pstart, mx);
       #pragma unroll 4
@@ -813,7 +828,7 @@ STDIC_DEV void run_subset(const BatchedArgs& B, const Team<TW>& tm, int item, un
     for (int p = tm.tl; p < npx; p += tm.TT, it.next()) {
       const int i = it.i, j = it.j;
       const float s = bw ? (float)bw[p] : 1.f;
-      const float fv = fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j) * s;
+      const float fv = (fm_cached ? tg[p] : fr.F(x1 + i, y1 + j) * fr.M(x1 + i, y1 + j)) * s;
       sa += fabsf(fv);
       if (fabsf(fv) > 1e-10f) { sf += fv; nf += 1.f; }
       float J[NQ];

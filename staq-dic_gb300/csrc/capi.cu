@@ -112,8 +112,9 @@ constexpr int kBandScratch = 2 * 256 * stdic::kQueueMaxBands + 2 * stdic::kQueue
 // only the first rows of a frame can start (wait_band) while the rest crosses
 // the host link.  A band's copies are issued when the call first waits for
 // it, so that the host queues the kernels of the earlier bands in between
-// (queuing a copy costs the host about as long as the kernels it overlaps);
-// the late copies follow the last band.
+// (queuing one pinned copy takes the host about 13 us, and queuing every
+// band up front delayed the first kernels); the late copies follow the last
+// band.
 // Under stream capture nothing goes to the side stream.
 struct Plan {
   struct Item {
